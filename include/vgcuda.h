@@ -1,0 +1,207 @@
+/* verion-gpu-cuda: C ABI of the GB300 (sm_103a) path-tracing backend.
+ *
+ * This is the surface a `verion-gpu-cuda` Rust crate binds to implement Verion's backend
+ * contract: the `RayTracingBackend` trait (crates/verion-gpu/src/lib.rs:12-58) and the
+ * `Accumulation` trait (crates/verion-gpu/src/lib.rs:74-93). Each entry point names the trait
+ * method it replaces. Tables cross the boundary in exactly the layout of `pack::Packed`
+ * (crates/verion-gpu/src/pack.rs:111-133), as pointer + length pairs, and are copied during the
+ * call (the copy semantics of the Metal backend's newBufferWithBytes,
+ * crates/verion-gpu-metal/src/renderer.rs:44-51).
+ *
+ * Handles are opaque and freed by the matching _destroy. A context and everything made from it
+ * belong to the thread that made them (the reference's GPU objects are not Send,
+ * crates/verion-render/src/session.rs:157-158). Every call returns a VgStatus; vg_last_error()
+ * gives the thread's last message.
+ */
+#ifndef VGCUDA_H
+#define VGCUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error kinds of the reference backends (crates/verion-gpu-metal/src/lib.rs:25-41,
+ * crates/verion-gpu-vulkan/src/lib.rs:23-44), plus a timeout for bounded host waits. */
+typedef enum VgStatus {
+    VG_OK = 0,
+    VG_ERR_NO_DEVICE = 1,   /* Error::NoDevice */
+    VG_ERR_UNSUPPORTED = 2, /* Error::RaytracingUnsupported / Unsupported */
+    VG_ERR_OOM = 3,         /* Error::OutOfMemory { needed, available } */
+    VG_ERR_RESOURCE = 4,    /* Error::Resource */
+    VG_ERR_KERNEL = 5,      /* Error::Shader: a kernel failed or reported an error status */
+    VG_ERR_SCENE = 6,       /* Error::Scene */
+    VG_ERR_TIMEOUT = 7,     /* the GPU did not finish within the host's deadline */
+    VG_ERR_INVALID = 8      /* malformed call: null handle, bad size, bad table */
+} VgStatus;
+
+typedef struct VgContext VgContext;
+typedef struct VgRenderer VgRenderer;
+typedef struct VgAccum VgAccum;
+
+/* lib.rs:240-249 MemoryUsage */
+typedef struct VgMemoryUsage {
+    uint64_t budget;
+    uint64_t allocated;
+    uint64_t uploaded;
+} VgMemoryUsage;
+
+/* pack.rs:43-49 MeshRange */
+typedef struct VgMeshRange {
+    uint32_t vertex_offset;
+    uint32_t vertex_count;
+    uint32_t index_offset;
+    uint32_t index_count;
+} VgMeshRange;
+
+/* pack.rs:54-69 SceneInfo */
+typedef struct VgSceneInfo {
+    uint32_t light_count;
+    uint32_t emitter_count;
+    uint32_t env_width;
+    uint32_t env_height;
+    float env_pdf_scale;
+    float sky[3];
+    uint32_t virtual_light;
+    uint32_t transparent_background;
+} VgSceneInfo;
+
+/* pack.rs:72-81 View: camera[2] = tan(fov/2), camera[4..16] the camera-to-world rows. */
+typedef struct VgView {
+    float camera[16];
+    float aperture;
+    float focus;
+    float shift[2];
+} VgView;
+
+/* pack.rs:111-133 Packed. `tlas_mesh` / `tlas_transform` are `Packed::tlas` (mesh index and 3x4
+ * row-major object-to-world transform per instance, in instance-table order). */
+typedef struct VgPacked {
+    const float* positions;     size_t positions_len;
+    const uint32_t* indices;    size_t indices_len;
+    const float* uvs;           size_t uvs_len;
+    const float* vnormals;      size_t vnormals_len;
+    const uint32_t* instances;  size_t instances_len;
+    const float* materials;     size_t materials_len;
+    const uint32_t* lights;     size_t lights_len;
+    const float* emitters;      size_t emitters_len;
+    const float* emit_cdf;      size_t emit_cdf_len;
+    const float* env_pixels;    size_t env_pixels_len;
+    const float* env_marginal;  size_t env_marginal_len;
+    const float* env_conditional; size_t env_conditional_len;
+    const float* texels;        size_t texels_len;
+    const uint32_t* tex_info;   size_t tex_info_len;
+    const VgMeshRange* meshes;  size_t mesh_count;
+    const uint32_t* tlas_mesh;
+    const float* tlas_transform; size_t instance_count;
+    VgSceneInfo info;
+    VgView view;
+} VgPacked;
+
+/* lib.rs:98-104 Integrator */
+typedef enum VgIntegrator { VG_MEGAKERNEL = 0, VG_WAVEFRONT = 1 } VgIntegrator;
+
+/* Statistics of the acceleration structure a renderer built (no reference counterpart: the
+ * reference's drivers build theirs). */
+typedef struct VgBvhInfo {
+    uint32_t triangles;
+    uint32_t wide_nodes;
+    uint32_t wide_depth;
+    uint32_t binary_nodes;
+    uint32_t binary_depth;
+    uint64_t node_bytes;
+    uint64_t triangle_bytes;
+    double build_seconds;
+} VgBvhInfo;
+
+/* Copies the calling thread's last error message (NUL-terminated, truncated to len). Returns the
+ * full message length. */
+size_t vg_last_error(char* buf, size_t len);
+/* OutOfMemory details of the thread's last VG_ERR_OOM. */
+void vg_last_oom(uint64_t* needed, uint64_t* available);
+
+/* RayTracingBackend::context (lib.rs:18-19): opens device 0; VG_ERR_NO_DEVICE without a GPU,
+ * VG_ERR_UNSUPPORTED unless it is an sm_103 device. */
+int vg_context_create(VgContext** out);
+void vg_context_destroy(VgContext* ctx);
+/* RayTracingBackend::memory (lib.rs:20) */
+int vg_memory(VgContext* ctx, VgMemoryUsage* out);
+
+/* RayTracingBackend::new (lib.rs:22): uploads the tables and builds the BVH. An empty instance
+ * table is VG_ERR_SCENE (pack.rs:727-729). */
+int vg_renderer_create(VgContext* ctx, const VgPacked* packed, VgRenderer** out);
+void vg_renderer_destroy(VgRenderer* r);
+int vg_renderer_bvh_info(const VgRenderer* r, VgBvhInfo* out);
+
+/* RayTracingBackend::set_camera (lib.rs:31) */
+int vg_set_camera(VgRenderer* r, const VgView* view);
+/* RayTracingBackend::set_multiscatter (lib.rs:33) */
+int vg_set_multiscatter(VgRenderer* r, int on);
+/* RayTracingBackend::set_integrator / integrator (lib.rs:34-35) */
+int vg_set_integrator(VgRenderer* r, int integrator);
+int vg_integrator(const VgRenderer* r);
+/* RayTracingBackend::set_stage_timing (lib.rs:37) */
+int vg_set_stage_timing(VgRenderer* r, int on);
+/* RayTracingBackend::set_adaptive (lib.rs:39): on = 0 is None. */
+int vg_set_adaptive(VgRenderer* r, int on, float threshold, uint32_t min_spp);
+/* RayTracingBackend::set_restir (lib.rs:42): on = 0 is None. ReSTIR GI is not built yet:
+ * gi != 0 returns VG_ERR_UNSUPPORTED. */
+int vg_set_restir(VgRenderer* r, int on, int di, int gi, uint32_t candidates, uint32_t history);
+
+/* Extensions with no reference counterpart. */
+/* Path length limit for accumulations (reference: the constant MAX_DEPTH = 8, pack.rs:13). */
+int vg_set_max_depth(VgRenderer* r, uint32_t depth);
+/* Precision of the per-pixel sums of accumulations made afterwards: 32 (the reference's f32
+ * sums) or 64 (double sums and double adaptive-sampling statistics, the default). */
+int vg_set_accum_precision(VgRenderer* r, int bits);
+
+/* RayTracingBackend::new_accumulation (lib.rs:45-51); zero size is VG_ERR_SCENE. */
+int vg_accum_create(VgRenderer* r, uint32_t width, uint32_t height, int lighting, VgAccum** out);
+void vg_accum_destroy(VgAccum* acc);
+/* RayTracingBackend::accumulate (lib.rs:50-52): blocking. Switching adaptive sampling or ReSTIR
+ * mid-accumulation is VG_ERR_SCENE (renderer.rs:800-828). */
+int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples);
+
+/* Accumulation getters (lib.rs:76-92). */
+uint32_t vg_accum_samples(const VgAccum* acc);
+double vg_accum_gpu_seconds(const VgAccum* acc);
+/* Stage seconds {extend, shade}; returns 0 when stage timing never ran (None). */
+int vg_accum_stage_seconds(const VgAccum* acc, double out[2]);
+size_t vg_accum_wavefront_bytes(const VgAccum* acc);
+size_t vg_accum_restir_bytes(const VgAccum* acc);
+/* Sum-precision of the accumulation in bits (32 or 64). */
+int vg_accum_precision(const VgAccum* acc);
+/* Raw sums for the shared readback arithmetic (readback.rs:18-137): 3 floats per pixel. A
+ * 64-bit accumulation is rounded to float here; vg_accum_read_sums_f64 returns it whole. */
+int vg_accum_read_sums(const VgAccum* acc, float* out, size_t len);
+int vg_accum_read_sums_f64(const VgAccum* acc, double* out, size_t len);
+/* Lighting split, LIGHTING_STRIDE = 65 floats per pixel (VG_ERR_INVALID without `lighting`). */
+int vg_accum_read_lighting(const VgAccum* acc, float* out, size_t len);
+/* Adaptive-sampling record, 3 floats per pixel: samples, luminance sum, square sum
+ * (VG_ERR_INVALID when adaptive sampling never ran). */
+int vg_accum_read_stats(const VgAccum* acc, float* out, size_t len);
+/* Wavefront queue lengths of the last sample traced: live paths at depths 0..max depth
+ * (max depth + 1 words; VG_ERR_INVALID before a wavefront accumulate). */
+int vg_accum_read_queue_counts(const VgAccum* acc, uint32_t* out, size_t len);
+/* Kernel launches made by vg_accumulate on this accumulation so far. */
+uint64_t vg_accum_launches(const VgAccum* acc);
+/* Average duration in seconds of one extend-kernel launch, from stage timing (0 if none). */
+double vg_accum_extend_launch_seconds(const VgAccum* acc);
+
+/* Traversal entry points (no reference counterpart; the reference's traversal is the driver's).
+ * Closest hits of n rays (6 floats each: origin xyz, direction xyz, host memory) into 4 words per
+ * ray (hit flag, instance, primitive, t bits) as the wavefront's hit record (wf_extend.slang:26-29). */
+int vg_trace_closest(VgRenderer* r, const float* rays, size_t n, uint32_t* hits);
+/* Shadow-ray queries of n rays (7 floats each: origin, direction, tmax): 1 occluded, 0 free,
+ * as pt_core.slang's occluded (:580-613). */
+int vg_trace_occluded(VgRenderer* r, const float* rays, size_t n, uint32_t* out);
+/* Device-resident form for timing: rays and hits are device pointers; returns the kernel time. */
+int vg_trace_closest_device(VgRenderer* r, const float* d_rays, size_t n, uint32_t* d_hits, double* seconds);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VGCUDA_H */

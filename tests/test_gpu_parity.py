@@ -1,0 +1,221 @@
+"""GPU parity: the CUDA backend (through the C ABI) against the CPU oracle on the same seeded
+inputs. Integer results (hit flags, instance and primitive ids, queue counts, sample counts) and,
+with single-precision sums, the float sums themselves are compared bit for bit: the kernels and the
+oracle evaluate the same IEEE single-precision operations in the same order.
+
+Reference tests these follow: crates/verion-gpu-metal/tests/pathtrace.rs (analytic scenes,
+wavefront == megakernel at :169-176, adaptive at :178-231), crates/verion-gpu-vulkan/tests/gpu.rs:50-67
+(bit-for-bit integrator equality), crates/verion-gpu-metal/tests/trace.rs:95-121 (hit distances).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from verion_gb300 import pack, scenes
+from verion_gb300 import scene as sc
+from verion_gb300.backend import Error, Integrator, Renderer
+from verion_gb300.readback import Adaptive, Restir
+
+pytestmark = pytest.mark.gpu
+
+
+def random_rays(n, seed, center=(0.0, 0.0, 0.0), spread=3.0):
+    rng = np.random.default_rng(seed)
+    o = rng.uniform(-spread, spread, (n, 3)) + np.asarray(center)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return np.concatenate([o, d], axis=1).astype(np.float32)
+
+
+def params(p, w, h, lighting=False, multiscatter=True, adaptive=None, restir=None, depth=8):
+    return pack.base_params(p.info, p.view, (w, h), lighting, multiscatter, adaptive, restir, depth)
+
+
+def gpu_render(ctx, p, w, h, spp, *, integrator=Integrator.MEGAKERNEL, precision=32, lighting=False,
+               adaptive=None, restir=None, depth=8, chunks=None):
+    r = Renderer(ctx, p)
+    r.set_accum_precision(precision)
+    r.set_integrator(integrator)
+    r.set_max_depth(depth)
+    r.set_adaptive(adaptive)
+    r.set_restir(restir)
+    acc = r.new_accumulation(w, h, lighting)
+    for n in (chunks or [spp]):
+        r.accumulate(acc, n)
+    return r, acc
+
+
+def oracle_render(p, w, h, spp, *, acc64=False, lighting=False, adaptive=None, restir=None, depth=8,
+                  wavefront=False):
+    o = oracle.OracleScene(p)
+    a = oracle.OracleAccumulation(w, h, lighting=lighting, acc64=acc64, adaptive=adaptive is not None,
+                                  restir=restir is not None)
+    oracle.render(o, params(p, w, h, lighting, True, adaptive, restir, depth), a, spp, wavefront=wavefront)
+    return a
+
+
+def assert_same(got, want, what):
+    got = np.asarray(got)
+    want = np.asarray(want)
+    bad = got != want
+    if bad.any():
+        i = np.flatnonzero(bad.ravel())[:5]
+        raise AssertionError(f"{what}: {int(bad.sum())} of {bad.size} differ, first {i.tolist()}: "
+                             f"{got.ravel()[i].tolist()} vs {want.ravel()[i].tolist()}")
+
+
+def test_trace_closest_cornell_matches_oracle(gpu_ctx):
+    p = pack.pack(scenes.cornell())
+    r = Renderer(gpu_ctx, p)
+    o = oracle.OracleScene(p)
+    rays = random_rays(200_000, 1, spread=1.2)
+    got = r.trace_closest(rays)
+    assert_same(got, o.trace_closest(rays, brute=True), "closest hits vs brute force")
+    assert got[:, 0].mean() > 0.9
+
+
+def test_trace_closest_many_spheres_matches_oracle(gpu_ctx):
+    p = pack.pack(scenes.many_spheres(hdri=None))
+    r = Renderer(gpu_ctx, p)
+    o = oracle.OracleScene(p)
+    rays = random_rays(300_000, 2, center=(0.0, 1.0, 0.0), spread=8.0)
+    got = r.trace_closest(rays)
+    assert_same(got, o.trace_closest(rays), "closest hits vs oracle BVH")
+    info = r.bvh_info()
+    assert info.triangles == 1_014_274 and info.wide_depth <= 30
+
+
+def test_trace_two_instances_hit_distances(gpu_ctx):
+    # crates/verion-gpu-metal/tests/trace.rs:95-121: two instances of a triangle at z = -1 and
+    # z = -2, rays from the origin down -z hit at distance 1; a ray beside them misses.
+    s = sc.Scene()
+    m = s.add_mesh(sc.Mesh(np.array([[-1, -1, 0], [1, -1, 0], [0, 1, 0]], np.float32), np.array([0, 1, 2])))
+    mat = s.add_material(scenes.material((0.5, 0.5, 0.5)))
+    s.add_instance(sc.Instance(m, mat, ((1, 0, 0, 0), (0, 1, 0, 0), (0, 0, 1, -1.0))))
+    s.add_instance(sc.Instance(m, mat, ((1, 0, 0, 3.0), (0, 1, 0, 0), (0, 0, 1, -1.0))))
+    r = Renderer(gpu_ctx, s)
+    rays = np.array([[0, 0, 0, 0, 0, -1], [3, 0, 0, 0, 0, -1], [10, 0, 0, 0, 0, -1]], np.float32)
+    h = r.trace_closest(rays)
+    t = [h[i, 3:4].view(np.float32)[0] if h[i, 0] else -1.0 for i in range(3)]
+    assert t == [1.0, 1.0, -1.0]
+    assert h[0, 1] == 0 and h[1, 1] == 1
+
+
+def test_occlusion_matches_oracle(gpu_ctx):
+    p = pack.pack(scenes.cornell())
+    r = Renderer(gpu_ctx, p)
+    o = oracle.OracleScene(p)
+    base = random_rays(100_000, 3, spread=0.9)
+    tmax = np.random.default_rng(4).uniform(0.01, 3.0, (len(base), 1)).astype(np.float32)
+    rays = np.concatenate([base, tmax], axis=1)
+    assert_same(r.trace_occluded(rays), o.trace_occluded(rays), "occlusion")
+
+
+def test_cornell_megakernel_bit_exact(gpu_ctx):
+    p = pack.pack(scenes.cornell())
+    w, h, spp = 96, 96, 8
+    _, acc = gpu_render(gpu_ctx, p, w, h, spp)
+    ref = oracle_render(p, w, h, spp)
+    assert_same(acc.sums(), ref.sums, "cornell megakernel sums")
+
+
+def test_cornell_wavefront_bit_exact_with_queue_counts(gpu_ctx):
+    p = pack.pack(scenes.cornell())
+    w, h = 80, 64
+    r = Renderer(gpu_ctx, p)
+    r.set_accum_precision(32)
+    r.set_integrator(Integrator.WAVEFRONT)
+    acc = r.new_accumulation(w, h)
+    o = oracle.OracleScene(p)
+    ref = oracle.OracleAccumulation(w, h)
+    for k in range(4):
+        r.accumulate(acc, 1)
+        oracle.render(o, params(p, w, h), ref, 1, wavefront=True)
+        assert_same(acc.queue_counts(8), np.array(ref.queue_counts[k], np.uint32), f"queue counts, sample {k}")
+    assert_same(acc.sums(), ref.sums, "cornell wavefront sums")
+
+
+def test_wavefront_equals_megakernel(gpu_ctx):
+    # pathtrace.rs:169-176 and gpu.rs:50-67: both integrators give the same image, bit for bit.
+    p = pack.pack(scenes.furnace_room(0.5, 1.0))
+    _, mega = gpu_render(gpu_ctx, p, 16, 16, 8, precision=64)
+    _, wave = gpu_render(gpu_ctx, p, 16, 16, 8, precision=64, integrator=Integrator.WAVEFRONT)
+    assert_same(wave.sums_f64(), mega.sums_f64(), "wavefront vs megakernel")
+
+
+def test_white_furnace_returns_the_sky(gpu_ctx):
+    # pathtrace.rs:117-137
+    r = Renderer(gpu_ctx, scenes.white_furnace())
+    img = r.render(32, 32, 4)
+    assert np.all(np.abs(img - 1.0) < 1e-4)
+
+
+def test_closed_room_series_sum(gpu_ctx):
+    # pathtrace.rs:103-115: L = E (1 - rho^8) / (1 - rho) within 1%.
+    r = Renderer(gpu_ctx, scenes.furnace_room(0.5, 1.0))
+    got = float(r.render(64, 64, 64)[:, 0].mean())
+    want = (1 - 0.5 ** 8) / (1 - 0.5)
+    assert abs(got - want) / want < 0.01
+
+
+def test_f64_sums_bit_exact(gpu_ctx):
+    p = pack.pack(scenes.cornell())
+    _, acc = gpu_render(gpu_ctx, p, 64, 48, 8, precision=64)
+    ref = oracle_render(p, 64, 48, 8, acc64=True)
+    assert_same(acc.sums_f64(), ref.sums, "double sums")
+
+
+@pytest.mark.parametrize("integrator", [Integrator.MEGAKERNEL, Integrator.WAVEFRONT])
+def test_adaptive_counts_and_sums_bit_exact(gpu_ctx, integrator):
+    p = pack.pack(scenes.furnace_room(0.5, 1.0))
+    a = Adaptive(threshold=0.05, min_spp=4)
+    _, acc = gpu_render(gpu_ctx, p, 16, 16, 32, integrator=integrator, adaptive=a, chunks=[8, 8, 8, 8])
+    ref = oracle_render(p, 16, 16, 32, adaptive=a)
+    assert_same(acc.sums(), ref.sums, "adaptive sums")
+    assert_same(acc.raw_stats(), ref.stats, "adaptive statistics")
+    counts = acc.sample_counts()
+    assert (counts < 32).any() and (counts == 32).any()
+
+
+def test_adaptive_switch_mid_accumulation_is_an_error(gpu_ctx):
+    # pathtrace.rs:216-231
+    r = Renderer(gpu_ctx, scenes.furnace_room(0.5, 1.0))
+    r.set_adaptive(Adaptive(threshold=1e9, min_spp=4))
+    acc = r.new_accumulation(16, 16)
+    r.accumulate(acc, 8)
+    assert (acc.sample_counts() == 4).all()
+    assert acc.active_pixels() == 0
+    r.set_adaptive(None)
+    with pytest.raises(Error) as e:
+        r.accumulate(acc, 1)
+    assert e.value.kind == "Scene"
+
+
+@pytest.mark.parametrize("integrator", [Integrator.MEGAKERNEL, Integrator.WAVEFRONT])
+def test_lighting_split_bit_exact(gpu_ctx, integrator):
+    s = scenes.cornell()
+    s.add_light(sc.Point((0.3, 0.8, 0.2), (1.0, 0.9, 0.8), 2.0))
+    s.add_light(sc.Directional((0.2, -1.0, -0.3), (0.5, 0.5, 0.6), 1.0))
+    p = pack.pack(s)
+    _, acc = gpu_render(gpu_ctx, p, 48, 40, 4, integrator=integrator, lighting=True)
+    ref = oracle_render(p, 48, 40, 4, lighting=True)
+    assert_same(acc.sums(), ref.sums, "sums with lighting split")
+    assert_same(acc.raw_lighting(), ref.lighting, "lighting split")
+
+
+@pytest.mark.parametrize("integrator", [Integrator.MEGAKERNEL, Integrator.WAVEFRONT])
+def test_restir_di_bit_exact(gpu_ctx, integrator):
+    p = pack.pack(scenes.cornell())
+    rs = Restir(di=True, gi=False, candidates=4, history=4)
+    _, acc = gpu_render(gpu_ctx, p, 48, 48, 6, integrator=integrator, restir=rs, chunks=[1, 2, 3])
+    ref = oracle_render(p, 48, 48, 6, restir=rs)
+    assert_same(acc.sums(), ref.sums, "ReSTIR DI sums")
+
+
+def test_many_spheres_depth16_env_bit_exact(gpu_ctx):
+    s = scenes.many_spheres(hdri=(256, 128))
+    p = pack.pack(s)
+    w, h = 64, 36
+    _, acc = gpu_render(gpu_ctx, p, w, h, 2, depth=16)
+    ref = oracle_render(p, w, h, 2, depth=16)
+    assert_same(acc.sums(), ref.sums, "1M-triangle scene, depth 16, environment map")

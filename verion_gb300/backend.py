@@ -1,0 +1,419 @@
+"""Python face of the CUDA backend: `Renderer` and `Accumulation` with the methods of Verion's
+`RayTracingBackend` and `Accumulation` traits (crates/verion-gpu/src/lib.rs:12-93), over the C ABI
+of include/vgcuda.h (libvgcuda.so, built in-tree by verion_gb300.build).
+
+There is no CPU fallback: without the library or a GB300 every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from enum import IntEnum
+from pathlib import Path
+from typing import Optional
+
+import numpy as np
+
+from . import readback as rb
+from .pack import Packed, View, pack
+from .readback import Adaptive, Restir
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "libvgcuda.so"
+
+VG_OK, VG_ERR_NO_DEVICE, VG_ERR_UNSUPPORTED, VG_ERR_OOM, VG_ERR_RESOURCE, VG_ERR_KERNEL, VG_ERR_SCENE, \
+    VG_ERR_TIMEOUT, VG_ERR_INVALID = range(9)
+_KIND = {VG_ERR_NO_DEVICE: "NoDevice", VG_ERR_UNSUPPORTED: "Unsupported", VG_ERR_OOM: "OutOfMemory",
+         VG_ERR_RESOURCE: "Resource", VG_ERR_KERNEL: "Kernel", VG_ERR_SCENE: "Scene", VG_ERR_TIMEOUT: "Timeout",
+         VG_ERR_INVALID: "Invalid"}
+
+
+class Error(RuntimeError):
+    """A backend error: `kind` is the reference's error variant (crates/verion-gpu-metal/src/lib.rs:25-41)."""
+
+    def __init__(self, status: int, message: str, needed: int = 0, available: int = 0):
+        super().__init__(f"{_KIND.get(status, status)}: {message}")
+        self.status = status
+        self.kind = _KIND.get(status, str(status))
+        self.needed = needed
+        self.available = available
+
+
+class Integrator(IntEnum):
+    MEGAKERNEL = 0
+    WAVEFRONT = 1
+
+
+class MemoryUsage(C.Structure):
+    _fields_ = [("budget", C.c_uint64), ("allocated", C.c_uint64), ("uploaded", C.c_uint64)]
+
+
+class _MeshRange(C.Structure):
+    _fields_ = [("vertex_offset", C.c_uint32), ("vertex_count", C.c_uint32), ("index_offset", C.c_uint32),
+                ("index_count", C.c_uint32)]
+
+
+class _SceneInfo(C.Structure):
+    _fields_ = [("light_count", C.c_uint32), ("emitter_count", C.c_uint32), ("env_width", C.c_uint32),
+                ("env_height", C.c_uint32), ("env_pdf_scale", C.c_float), ("sky", C.c_float * 3),
+                ("virtual_light", C.c_uint32), ("transparent_background", C.c_uint32)]
+
+
+class _View(C.Structure):
+    _fields_ = [("camera", C.c_float * 16), ("aperture", C.c_float), ("focus", C.c_float), ("shift", C.c_float * 2)]
+
+
+_P = C.c_void_p
+_S = C.c_size_t
+
+
+class _Packed(C.Structure):
+    _fields_ = [(n, t) for pair in [
+        (("positions", _P), ("positions_len", _S)), (("indices", _P), ("indices_len", _S)),
+        (("uvs", _P), ("uvs_len", _S)), (("vnormals", _P), ("vnormals_len", _S)),
+        (("instances", _P), ("instances_len", _S)), (("materials", _P), ("materials_len", _S)),
+        (("lights", _P), ("lights_len", _S)), (("emitters", _P), ("emitters_len", _S)),
+        (("emit_cdf", _P), ("emit_cdf_len", _S)), (("env_pixels", _P), ("env_pixels_len", _S)),
+        (("env_marginal", _P), ("env_marginal_len", _S)), (("env_conditional", _P), ("env_conditional_len", _S)),
+        (("texels", _P), ("texels_len", _S)), (("tex_info", _P), ("tex_info_len", _S)),
+        (("meshes", _P), ("mesh_count", _S)), (("tlas_mesh", _P),),
+        (("tlas_transform", _P), ("instance_count", _S)),
+        (("info", _SceneInfo), ("view", _View))] for n, t in pair]
+
+
+class BvhInfo(C.Structure):
+    _fields_ = [("triangles", C.c_uint32), ("wide_nodes", C.c_uint32), ("wide_depth", C.c_uint32),
+                ("binary_nodes", C.c_uint32), ("binary_depth", C.c_uint32), ("node_bytes", C.c_uint64),
+                ("triangle_bytes", C.c_uint64), ("build_seconds", C.c_double)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads libvgcuda.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise Error(VG_ERR_RESOURCE, f"{LIB_PATH} is missing: run `python -m verion_gb300.build`")
+        L = C.CDLL(str(LIB_PATH))
+        vp, u32, i32, f64 = C.c_void_p, C.c_uint32, C.c_int, C.c_double
+        sig = {
+            "vg_last_error": (_S, [C.c_char_p, _S]),
+            "vg_last_oom": (None, [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+            "vg_context_create": (i32, [C.POINTER(vp)]),
+            "vg_context_destroy": (None, [vp]),
+            "vg_memory": (i32, [vp, C.POINTER(MemoryUsage)]),
+            "vg_renderer_create": (i32, [vp, C.POINTER(_Packed), C.POINTER(vp)]),
+            "vg_renderer_destroy": (None, [vp]),
+            "vg_renderer_bvh_info": (i32, [vp, C.POINTER(BvhInfo)]),
+            "vg_set_camera": (i32, [vp, C.POINTER(_View)]),
+            "vg_set_multiscatter": (i32, [vp, i32]),
+            "vg_set_integrator": (i32, [vp, i32]),
+            "vg_integrator": (i32, [vp]),
+            "vg_set_stage_timing": (i32, [vp, i32]),
+            "vg_set_adaptive": (i32, [vp, i32, C.c_float, u32]),
+            "vg_set_restir": (i32, [vp, i32, i32, i32, u32, u32]),
+            "vg_set_max_depth": (i32, [vp, u32]),
+            "vg_set_accum_precision": (i32, [vp, i32]),
+            "vg_accum_create": (i32, [vp, u32, u32, i32, C.POINTER(vp)]),
+            "vg_accum_destroy": (None, [vp]),
+            "vg_accumulate": (i32, [vp, vp, u32]),
+            "vg_accum_samples": (u32, [vp]),
+            "vg_accum_gpu_seconds": (f64, [vp]),
+            "vg_accum_stage_seconds": (i32, [vp, C.POINTER(f64)]),
+            "vg_accum_wavefront_bytes": (_S, [vp]),
+            "vg_accum_restir_bytes": (_S, [vp]),
+            "vg_accum_precision": (i32, [vp]),
+            "vg_accum_read_sums": (i32, [vp, vp, _S]),
+            "vg_accum_read_sums_f64": (i32, [vp, vp, _S]),
+            "vg_accum_read_lighting": (i32, [vp, vp, _S]),
+            "vg_accum_read_stats": (i32, [vp, vp, _S]),
+            "vg_accum_launches": (C.c_uint64, [vp]),
+            "vg_accum_read_queue_counts": (i32, [vp, vp, _S]),
+            "vg_accum_extend_launch_seconds": (f64, [vp]),
+            "vg_trace_closest": (i32, [vp, vp, _S, vp]),
+            "vg_trace_occluded": (i32, [vp, vp, _S, vp]),
+            "vg_trace_closest_device": (i32, [vp, vp, _S, vp, C.POINTER(f64)]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status: int) -> None:
+    if status != VG_OK:
+        L = lib()
+        buf = C.create_string_buffer(1024)
+        L.vg_last_error(buf, 1024)
+        need, avail = C.c_uint64(), C.c_uint64()
+        if status == VG_ERR_OOM:
+            L.vg_last_oom(C.byref(need), C.byref(avail))
+        raise Error(status, buf.value.decode(errors="replace"), need.value, avail.value)
+
+
+def _ptr(a: np.ndarray) -> Optional[int]:
+    return a.ctypes.data if a.size else None
+
+
+def _view(v: View) -> _View:
+    out = _View()
+    out.camera[:] = [float(x) for x in v.camera]
+    out.aperture = v.aperture
+    out.focus = v.focus
+    out.shift[:] = [float(v.shift[0]), float(v.shift[1])]
+    return out
+
+
+class Context:
+    """The device and its stream (`RayTracingBackend::Context`)."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        _check(lib().vg_context_create(C.byref(h)))
+        self._h = h
+
+    def memory(self) -> MemoryUsage:
+        m = MemoryUsage()
+        _check(lib().vg_memory(self._h, C.byref(m)))
+        return m
+
+    def close(self):
+        if self._h:
+            lib().vg_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Accumulation:
+    """Running radiance sums of one image (`Accumulation` trait, lib.rs:74-93)."""
+
+    def __init__(self, renderer: "Renderer", width: int, height: int, lighting: bool):
+        h = C.c_void_p()
+        _check(lib().vg_accum_create(renderer._h, width, height, int(lighting), C.byref(h)))
+        self._h = h
+        self._r = renderer
+        self.width, self.height, self.has_lighting = width, height, lighting
+        self.adaptive: Optional[Adaptive] = None
+
+    @property
+    def pixels(self) -> int:
+        return self.width * self.height
+
+    def samples(self) -> int:
+        return lib().vg_accum_samples(self._h)
+
+    def gpu_seconds(self) -> float:
+        return lib().vg_accum_gpu_seconds(self._h)
+
+    def stage_seconds(self):
+        out = (C.c_double * 2)()
+        return (out[0], out[1]) if lib().vg_accum_stage_seconds(self._h, out) else None
+
+    def wavefront_bytes(self) -> int:
+        return lib().vg_accum_wavefront_bytes(self._h)
+
+    def restir_bytes(self) -> int:
+        return lib().vg_accum_restir_bytes(self._h)
+
+    def precision(self) -> int:
+        return lib().vg_accum_precision(self._h)
+
+    def queue_counts(self, depth: int) -> np.ndarray:
+        """Wavefront queue lengths of the last sample (depths 0..depth)."""
+        out = np.empty(depth + 1, np.uint32)
+        _check(lib().vg_accum_read_queue_counts(self._h, out.ctypes.data, out.size))
+        return out
+
+    def launches(self) -> int:
+        return lib().vg_accum_launches(self._h)
+
+    def extend_launch_seconds(self) -> float:
+        return lib().vg_accum_extend_launch_seconds(self._h)
+
+    def sums(self, into: Optional[np.ndarray] = None) -> np.ndarray:
+        out = into if into is not None else np.empty(3 * self.pixels, np.float32)
+        _check(lib().vg_accum_read_sums(self._h, out.ctypes.data, out.size))
+        return out
+
+    def sums_f64(self) -> np.ndarray:
+        out = np.empty(3 * self.pixels, np.float64)
+        _check(lib().vg_accum_read_sums_f64(self._h, out.ctypes.data, out.size))
+        return out
+
+    def raw_stats(self) -> Optional[np.ndarray]:
+        if self.adaptive is None:
+            return None
+        out = np.empty(3 * self.pixels, np.float32)
+        _check(lib().vg_accum_read_stats(self._h, out.ctypes.data, out.size))
+        return out
+
+    def raw_lighting(self) -> Optional[np.ndarray]:
+        if not self.has_lighting:
+            return None
+        out = np.empty(rb.LIGHTING_STRIDE * self.pixels, np.float32)
+        _check(lib().vg_accum_read_lighting(self._h, out.ctypes.data, out.size))
+        return out
+
+    def _inverse(self) -> np.ndarray:
+        return rb.inverse_samples(self.raw_stats(), self.pixels, self.samples())
+
+    def mean(self) -> np.ndarray:
+        """Mean radiance per pixel, (pixels, 3), row-major from the top-left."""
+        return rb.mean(self.sums(), self._inverse())
+
+    def lighting(self) -> Optional[rb.LightingAovs]:
+        data = self.raw_lighting()
+        return None if data is None else rb.lighting(data, self._inverse())
+
+    def sample_counts(self) -> Optional[np.ndarray]:
+        st = self.raw_stats()
+        return None if st is None else rb.sample_counts(st)
+
+    def active_pixels(self) -> int:
+        return rb.active_pixels(self.raw_stats(), self.adaptive, self.pixels)
+
+    def close(self):
+        if self._h:
+            lib().vg_accum_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Renderer:
+    """A scene on the GPU (`RayTracingBackend` implementation, lib.rs:12-58)."""
+
+    def __init__(self, ctx: Context, scene_or_packed):
+        packed = scene_or_packed if isinstance(scene_or_packed, Packed) else pack(scene_or_packed)
+        self.packed = packed
+        self._keep = []
+        pk = _Packed()
+
+        def put(name, arr, dtype):
+            a = np.ascontiguousarray(arr, dtype=dtype).reshape(-1)
+            self._keep.append(a)
+            setattr(pk, name, _ptr(a))
+            setattr(pk, name + "_len", a.size)
+
+        put("positions", packed.positions, np.float32)
+        put("indices", packed.indices, np.uint32)
+        put("uvs", packed.uvs, np.float32)
+        put("vnormals", packed.vnormals, np.float32)
+        put("instances", packed.instances, np.uint32)
+        put("materials", packed.materials, np.float32)
+        put("lights", packed.lights, np.uint32)
+        put("emitters", packed.emitters, np.float32)
+        put("emit_cdf", packed.emit_cdf, np.float32)
+        put("env_pixels", packed.env.pixels, np.float32)
+        put("env_marginal", packed.env.marginal, np.float32)
+        put("env_conditional", packed.env.conditional, np.float32)
+        put("texels", packed.texels, np.float32)
+        put("tex_info", packed.tex_info, np.uint32)
+        meshes = np.ascontiguousarray(packed.meshes, np.uint32).reshape(-1, 4)
+        tm = np.ascontiguousarray(packed.tlas_mesh, np.uint32)
+        tt = np.ascontiguousarray(packed.tlas_transform, np.float32)
+        self._keep += [meshes, tm, tt]
+        pk.meshes, pk.mesh_count = _ptr(meshes), len(meshes)
+        pk.tlas_mesh, pk.tlas_transform, pk.instance_count = _ptr(tm), _ptr(tt), len(tm)
+        i = packed.info
+        pk.info.light_count, pk.info.emitter_count = i.light_count, i.emitter_count
+        pk.info.env_width, pk.info.env_height, pk.info.env_pdf_scale = i.env_width, i.env_height, i.env_pdf_scale
+        pk.info.sky[:] = list(i.sky)
+        pk.info.virtual_light, pk.info.transparent_background = int(i.virtual_light), int(i.transparent_background)
+        pk.view = _view(packed.view)
+        h = C.c_void_p()
+        _check(lib().vg_renderer_create(ctx._h, C.byref(pk), C.byref(h)))
+        self._h = h
+        self._ctx = ctx
+        self._keep = []
+        self._adaptive: Optional[Adaptive] = None
+        self._restir: Optional[Restir] = None
+
+    # RayTracingBackend setters
+    def set_camera(self, view_or_camera) -> None:
+        v = view_or_camera if isinstance(view_or_camera, View) else View.new(view_or_camera)
+        cv = _view(v)
+        _check(lib().vg_set_camera(self._h, C.byref(cv)))
+
+    def set_multiscatter(self, on: bool) -> None:
+        _check(lib().vg_set_multiscatter(self._h, int(on)))
+
+    def set_integrator(self, integrator: Integrator) -> None:
+        _check(lib().vg_set_integrator(self._h, int(integrator)))
+
+    def integrator(self) -> Integrator:
+        return Integrator(lib().vg_integrator(self._h))
+
+    def set_stage_timing(self, on: bool) -> None:
+        _check(lib().vg_set_stage_timing(self._h, int(on)))
+
+    def set_adaptive(self, adaptive: Optional[Adaptive]) -> None:
+        a = adaptive
+        _check(lib().vg_set_adaptive(self._h, int(a is not None), a.threshold if a else 0.0, a.min_spp if a else 0))
+        self._adaptive = adaptive
+
+    def set_restir(self, restir: Optional[Restir]) -> None:
+        r = restir
+        _check(lib().vg_set_restir(self._h, int(r is not None), int(r.di) if r else 0, int(r.gi) if r else 0,
+                                   r.candidates if r else 0, r.history if r else 0))
+        self._restir = restir
+
+    def set_max_depth(self, depth: int) -> None:
+        _check(lib().vg_set_max_depth(self._h, depth))
+
+    def set_accum_precision(self, bits: int) -> None:
+        _check(lib().vg_set_accum_precision(self._h, bits))
+
+    def bvh_info(self) -> BvhInfo:
+        b = BvhInfo()
+        _check(lib().vg_renderer_bvh_info(self._h, C.byref(b)))
+        return b
+
+    def new_accumulation(self, width: int, height: int, lighting: bool = False) -> Accumulation:
+        return Accumulation(self, width, height, lighting)
+
+    def accumulate(self, acc: Accumulation, samples: int) -> None:
+        if acc.samples() == 0:
+            acc.adaptive = self._adaptive
+        _check(lib().vg_accumulate(self._h, acc._h, samples))
+
+    def render(self, width: int, height: int, samples: int) -> np.ndarray:
+        """One-shot mean radiance (the Metal renderer's `render`, renderer.rs:489-494)."""
+        acc = self.new_accumulation(width, height, False)
+        self.accumulate(acc, samples)
+        return acc.mean()
+
+    # Traversal entry points
+    def trace_closest(self, rays: np.ndarray) -> np.ndarray:
+        r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        out = np.empty((len(r), 4), np.uint32)
+        _check(lib().vg_trace_closest(self._h, _ptr(r), len(r), _ptr(out)))
+        return out
+
+    def trace_occluded(self, rays: np.ndarray) -> np.ndarray:
+        r = np.ascontiguousarray(rays, np.float32).reshape(-1, 7)
+        out = np.empty(len(r), np.uint32)
+        _check(lib().vg_trace_occluded(self._h, _ptr(r), len(r), _ptr(out)))
+        return out
+
+    def close(self):
+        if self._h:
+            lib().vg_renderer_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,89 @@
+"""Builds the CUDA backend library `verion_gb300/_build/libvgcuda.so` for sm_103a.
+
+The translation units compile in parallel (nvcc for the kernels, g++ for the BVH builder), then
+nvcc links them with the static CUDA runtime into one shared library with the C ABI of
+`include/vgcuda.h`. Device code is compiled without FMA contraction and with correctly rounded
+division and square root, host code with -ffp-contract=off: the kernels then compute exactly the
+single-precision operations their source spells out, which is what makes bit-exact comparison
+with a CPU restatement possible.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB = BUILD / "libvgcuda.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + [
+    "-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",
+    "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", str(CSRC),
+]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", str(CSRC)]
+
+CU_SOURCES = ["kern_mk.cu", "kern_wf.cu", "vgcuda.cu"]
+CXX_SOURCES = ["bvh_build.cpp"]
+DEPS = ["vg_math.h", "vg_layout.h", "vec3.h", "bvh8.h", "traverse.cuh", "pt_device.cuh", "kernels.cuh",
+        "launch.h", "bvh_build.h"]
+
+
+def _nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(cand).exists():
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build verion_gb300")
+    return cand
+
+
+def _stale(obj: Path, src: Path) -> bool:
+    if not obj.exists():
+        return True
+    t = obj.stat().st_mtime
+    deps = [src] + [CSRC / d for d in DEPS] + [PKG.parent / "include" / "vgcuda.h", Path(__file__)]
+    return any(d.exists() and d.stat().st_mtime > t for d in deps)
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build step failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    """Compiles the library if any source is newer than it; returns its path."""
+    BUILD.mkdir(exist_ok=True)
+    nvcc = _nvcc()
+    cxx = shutil.which("g++") or "g++"
+    jobs = []
+    objs = []
+    for s in CU_SOURCES:
+        o = BUILD / (Path(s).stem + ".o")
+        objs.append(o)
+        if force or _stale(o, CSRC / s):
+            jobs.append([nvcc] + NVCC_FLAGS + ["-c", str(CSRC / s), "-o", str(o)])
+    for s in CXX_SOURCES:
+        o = BUILD / (Path(s).stem + ".o")
+        objs.append(o)
+        if force or _stale(o, CSRC / s):
+            jobs.append([cxx] + CXX_FLAGS + ["-c", str(CSRC / s), "-o", str(o)])
+    if jobs:
+        with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
+            for cmd in jobs:
+                if verbose:
+                    print(" ".join(cmd), file=sys.stderr)
+            list(ex.map(_run, jobs))
+    if force or jobs or not LIB.exists():
+        tmp = BUILD / "libvgcuda.so.tmp"
+        _run([nvcc] + ARCH + ["-shared", "-o", str(tmp)] + [str(o) for o in objs])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

@@ -1,0 +1,73 @@
+// Plain data types shared by the kernels and the host code that launches them.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bvh8.h"
+#include "vg_layout.h"
+
+namespace vgd {
+
+using namespace vgl;
+
+// Device tables of one renderer.
+struct DeviceScene {
+    const float* positions;
+    const uint32_t* indices;
+    const uint32_t* instances;
+    const float* materials;
+    const uint32_t* lights;
+    const float* emitters;
+    const float* emit_cdf;
+    const float* env_pixels;
+    const float* env_marginal;
+    const float* env_cond;
+    const float* uvs;
+    const float* texels;
+    const uint32_t* tex_info;
+    const float* vnormals;
+    const uint4* nodes;
+    const float4* tris;
+    uint32_t shadow_any; // 1 when every surface is opaque: shadow rays stop at any hit
+};
+
+// ReSTIR DI reservoirs in structure-of-arrays form, one set per frame parity. The reference keeps
+// 80 floats per pixel interleaved (pt_core.slang:55-63); here each field a neighbour reads is a
+// 16-byte plane, so a reuse fetches three coalesced vectors.
+struct Reservoirs {
+    float4* g[2]; // shading point xyz, usable as a neighbour (bits, 1 or 0)   (words 8..10, 14)
+    float4* n[2]; // shading normal xyz, emitter + 1 (bits, 0 = none)          (words 11..13, 0)
+    float4* x[2]; // sample point xyz, contribution weight W                    (words 1..3, 4)
+    float* m[2];  // sample count M                                             (word 5)
+};
+
+// Everything a launch reads: the tables, the parameter block and the accumulation buffers.
+struct Ctx {
+    DeviceScene s;
+    uint32_t p[PARAM_WORDS];
+    void* accum;     // 3 sums per pixel, float or double
+    void* stats;     // adaptive sampling: samples, luminance sum, square sum per pixel
+    float* lighting; // LIGHTING_STRIDE floats per pixel
+    Reservoirs re;
+    uint32_t* err;
+};
+
+} // namespace vgd
+
+namespace vgk {
+
+constexpr uint32_t BASE_PLANES = 4;  // 16-byte state planes per path
+constexpr uint32_t SPLIT_PLANES = 5; // more planes with the lighting split
+
+// Wavefront buffers of one accumulation.
+struct Wave {
+    float4* state;
+    uint4* hits;       // hit flag, instance, primitive, t bits (wf_extend.slang:26-29)
+    uint32_t* queue[2];
+    uint32_t* counts;  // live paths per depth, max depth + 1 entries
+    uint32_t* fetch;   // work counters: extend of depth d at [d], shade at [(D + 1) + d]
+    uint32_t n;        // paths: one per pixel
+    uint32_t depth;    // max depth
+};
+
+} // namespace vgk

@@ -1,0 +1,92 @@
+// Wavefront kernel variants (shaders/wf_*.slang) and the traversal-only kernels.
+#include "kernels.cuh"
+#include "launch.h"
+
+namespace vgx {
+
+template <bool L, bool R, typename A>
+static cudaError_t shade(int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w, uint32_t d)
+{
+    vgk::wf_shade<L, R, A><<<blocks, 128, 0, s>>>(c, w, d);
+    return cudaGetLastError();
+}
+
+template <bool L, bool R, typename A>
+static int shade_occ()
+{
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, vgk::wf_shade<L, R, A>, 128, 0);
+    return n > 0 ? n : 1;
+}
+
+cudaError_t launch_wf_shade(Variant v, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w, uint32_t d)
+{
+    switch (v.index()) {
+    case 0: return shade<false, false, float>(blocks, s, c, w, d);
+    case 1: return shade<true, false, float>(blocks, s, c, w, d);
+    case 2: return shade<false, true, float>(blocks, s, c, w, d);
+    case 3: return shade<true, true, float>(blocks, s, c, w, d);
+    case 4: return shade<false, false, double>(blocks, s, c, w, d);
+    case 5: return shade<true, false, double>(blocks, s, c, w, d);
+    case 6: return shade<false, true, double>(blocks, s, c, w, d);
+    default: return shade<true, true, double>(blocks, s, c, w, d);
+    }
+}
+
+int wf_shade_blocks_per_sm(Variant v)
+{
+    switch (v.index()) {
+    case 0: return shade_occ<false, false, float>();
+    case 1: return shade_occ<true, false, float>();
+    case 2: return shade_occ<false, true, float>();
+    case 3: return shade_occ<true, true, float>();
+    case 4: return shade_occ<false, false, double>();
+    case 5: return shade_occ<true, false, double>();
+    case 6: return shade_occ<false, true, double>();
+    default: return shade_occ<true, true, double>();
+    }
+}
+
+cudaError_t launch_wf_begin(cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w)
+{
+    vgk::wf_begin<<<1, 64, 0, s>>>(c, w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wf_select(bool f64, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w)
+{
+    unsigned blocks = (w.n + 255) / 256;
+    if (f64)
+        vgk::wf_select<double><<<blocks, 256, 0, s>>>(c, w);
+    else
+        vgk::wf_select<float><<<blocks, 256, 0, s>>>(c, w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wf_extend(int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w, uint32_t d)
+{
+    vgk::wf_extend<<<blocks, 128, 0, s>>>(c, w, d);
+    return cudaGetLastError();
+}
+
+int wf_extend_blocks_per_sm()
+{
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, vgk::wf_extend, 128, 0);
+    return n > 0 ? n : 1;
+}
+
+cudaError_t launch_trace_rays(int blocks, cudaStream_t s, const vgd::Ctx& c, const float* rays, uint4* out, uint32_t n,
+                              uint32_t* fetch)
+{
+    vgk::trace_rays<<<blocks, 128, 0, s>>>(c, rays, out, n, fetch);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_occlusion_rays(cudaStream_t s, const vgd::Ctx& c, const float* rays, uint32_t* out, uint32_t n)
+{
+    vgk::occlusion_rays<<<(n + 127) / 128, 128, 0, s>>>(c, rays, out, n);
+    return cudaGetLastError();
+}
+
+} // namespace vgx

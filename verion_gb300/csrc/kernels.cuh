@@ -1,0 +1,260 @@
+// Kernels of the CUDA backend (sm_103a): the megakernel and the wavefront stages.
+//
+// Reference entry points: shaders/pathtrace.slang (megakernel), shaders/wf_select.slang,
+// shaders/wf_args.slang, shaders/wf_extend.slang, shaders/wf_shade.slang, with the path state of
+// shaders/include/wf_state.slang.
+//
+// GB300 design:
+// * Extend and shade are persistent kernels: a grid sized to fill the 152 SMs once, each warp
+//   fetching 32 consecutive queue entries with one atomic until the depth's queue is drained.
+//   The queue length is read on the device, so no indirect dispatch (wf_args) and no host wait
+//   sit between depths.
+// * Compaction (live paths into the next depth's queue, pixels into the depth-0 queue) is warp
+//   aggregated: one ballot, one atomic per warp, each lane writes at its rank.
+// * Path state is structure-of-arrays in 16-byte planes: a path's 16 words are four 128-bit
+//   loads, each plane contiguous over paths.
+#pragma once
+#include "pt_device.cuh"
+
+namespace vgk {
+
+using namespace vgd;
+
+constexpr uint32_t FULL = 0xffffffffu;
+
+// State planes (16 bytes each, plane k of path p at state[k * N + p]):
+//   0 (org.xyz, rng)  1 (dir.xyz, flags)  2 (thr.xyz, pathLen)  3 (total.xyz, qPrev)
+//   with the lighting split: 4 (directDiffuse.xyz, visLit) 5 (indirectDiffuse.xyz, visTotal)
+//   6 (specular.xyz, 0) 7 (transmission.xyz, 0) 8 (emission.xyz, 0)
+// flags as in wf_state.slang:42: cls bits 0-1, chan + 1 bits 2-3, misPrev bit 4, restir bit 5,
+// gi bit 6, prevInst bits 8 and up.
+
+static __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+// Appends `pred` lanes of a converged warp to `queue` (counter `count`); returns the slot.
+static __device__ __forceinline__ void warp_append(uint32_t* count, uint32_t* queue, bool pred, uint32_t value)
+{
+    uint32_t b = __ballot_sync(FULL, pred);
+    if (b == 0)
+        return;
+    uint32_t base = 0;
+    if (lane_id() == 0)
+        base = atomicAdd(count, __popc(b));
+    base = __shfl_sync(FULL, base, 0);
+    if (pred)
+        queue[base + __popc(b & ((1u << lane_id()) - 1u))] = value;
+}
+
+// Warp-wide work fetch: 32 consecutive items per atomic.
+static __device__ __forceinline__ uint32_t warp_fetch(uint32_t* counter)
+{
+    uint32_t base = 0;
+    if (lane_id() == 0)
+        base = atomicAdd(counter, 32u);
+    return __shfl_sync(FULL, base, 0);
+}
+
+template <bool LIGHT>
+__device__ __forceinline__ void storePath(const Wave& w, const PathState<LIGHT>& s, uint32_t p)
+{
+    uint32_t n = w.n;
+    uint32_t flags = s.cls | ((uint32_t)(s.chan + 1) << 2) | (s.misPrev ? 16u : 0u) | (s.restir ? 32u : 0u) |
+                     (s.gi ? 64u : 0u) | (s.prevInst << 8);
+    w.state[p] = make_float4(s.org.x, s.org.y, s.org.z, __uint_as_float(s.rng));
+    w.state[n + p] = make_float4(s.dir.x, s.dir.y, s.dir.z, __uint_as_float(flags));
+    w.state[2 * n + p] = make_float4(s.thr.x, s.thr.y, s.thr.z, s.pathLen);
+    w.state[3 * n + p] = make_float4(s.parts.total.x, s.parts.total.y, s.parts.total.z, s.qPrev);
+    if (LIGHT) {
+        const Parts<LIGHT>& q = s.parts;
+        w.state[4 * n + p] = make_float4(q.directDiffuse.x, q.directDiffuse.y, q.directDiffuse.z, s.visLit);
+        w.state[5 * n + p] = make_float4(q.indirectDiffuse.x, q.indirectDiffuse.y, q.indirectDiffuse.z, s.visTotal);
+        w.state[6 * n + p] = make_float4(q.specular.x, q.specular.y, q.specular.z, 0.0f);
+        w.state[7 * n + p] = make_float4(q.transmission.x, q.transmission.y, q.transmission.z, 0.0f);
+        w.state[8 * n + p] = make_float4(q.emission.x, q.emission.y, q.emission.z, 0.0f);
+    }
+}
+
+// wf_state.slang:60-92. Depth 0 keeps no state: the camera path is generated again.
+template <bool LIGHT>
+__device__ __forceinline__ PathState<LIGHT> loadPath(const Ctx& c, const Wave& w, uint32_t p, uint32_t depth)
+{
+    if (depth == 0)
+        return generatePathFor<LIGHT>(c, p % c.p[P_WIDTH], p / c.p[P_WIDTH], c.p[P_SAMPLE]);
+    uint32_t n = w.n;
+    PathState<LIGHT> s;
+    float4 a = w.state[p];
+    float4 b = w.state[n + p];
+    float4 t = w.state[2 * n + p];
+    float4 r = w.state[3 * n + p];
+    s.org = v3(a.x, a.y, a.z);
+    s.rng = __float_as_uint(a.w);
+    s.dir = v3(b.x, b.y, b.z);
+    uint32_t flags = __float_as_uint(b.w);
+    s.thr = v3(t.x, t.y, t.z);
+    s.pathLen = t.w;
+    s.cls = flags & 3u;
+    s.chan = (int)((flags >> 2) & 3u) - 1;
+    s.misPrev = (flags & 16u) != 0;
+    s.restir = (flags & 32u) != 0;
+    s.gi = (flags & 64u) != 0;
+    s.prevInst = flags >> 8;
+    s.qPrev = r.w;
+    s.parts.zero();
+    s.parts.total = v3(r.x, r.y, r.z);
+    s.visLit = 0.0f;
+    s.visTotal = 0.0f;
+    if (LIGHT) {
+        float4 q4 = w.state[4 * n + p], q5 = w.state[5 * n + p], q6 = w.state[6 * n + p], q7 = w.state[7 * n + p],
+               q8 = w.state[8 * n + p];
+        s.parts.directDiffuse = v3(q4.x, q4.y, q4.z);
+        s.visLit = q4.w;
+        s.parts.indirectDiffuse = v3(q5.x, q5.y, q5.z);
+        s.visTotal = q5.w;
+        s.parts.specular = v3(q6.x, q6.y, q6.z);
+        s.parts.transmission = v3(q7.x, q7.y, q7.z);
+        s.parts.emission = v3(q8.x, q8.y, q8.z);
+    }
+    return s;
+}
+
+// pathtrace.slang:9-26: one thread per pixel, params[35] samples from params[6].
+template <bool LIGHT, bool RESTIR, typename A>
+__global__ void __launch_bounds__(128) mk_pathtrace(const __grid_constant__ Ctx c)
+{
+    uint32_t x = blockIdx.x * 16 + (threadIdx.x & 15u);
+    uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 4);
+    if (x >= c.p[P_WIDTH] || y >= c.p[P_HEIGHT])
+        return;
+    uint32_t pixel = y * c.p[P_WIDTH] + x;
+    for (uint32_t k = 0; k < c.p[P_SAMPLES_PER_DISPATCH]; k++) {
+        if (c.p[P_ADAPTIVE] != 0 && !pixelActive<A>(c, pixel))
+            return;
+        PathState<LIGHT> st = generatePathFor<LIGHT>(c, x, y, c.p[P_SAMPLE] + k);
+        for (uint32_t depth = 0; depth < c.p[P_MAX_DEPTH]; depth++) {
+            if (!shadePath<LIGHT, RESTIR>(c, st, traceClosest(c, st.org, st.dir), depth, pixel))
+                break;
+        }
+        finishPath<LIGHT, A>(c, st, pixel);
+    }
+}
+
+// wf_args.slang:9-24 at depth 0: starts a sample. Every pixel's path is live unless adaptive
+// sampling fills the depth-0 queue (wf_select); the later queues and all work counters restart.
+static __global__ void wf_begin(const __grid_constant__ Ctx c, Wave w)
+{
+    uint32_t i = threadIdx.x;
+    for (uint32_t k = i; k <= w.depth; k += blockDim.x) {
+        w.counts[k] = (k == 0 && c.p[P_ADAPTIVE] == 0) ? w.n : 0u;
+        w.fetch[k] = 0;
+        w.fetch[w.depth + 1 + k] = 0;
+    }
+}
+
+// wf_select.slang:7-18: queues the pixels that still take samples, warp aggregated.
+template <typename A>
+__global__ void __launch_bounds__(256) wf_select(const __grid_constant__ Ctx c, Wave w)
+{
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    bool active = p < w.n && pixelActive<A>(c, p);
+    warp_append(&w.counts[0], w.queue[0], active, p);
+}
+
+// wf_extend.slang:6-30: closest hit for every live path of depth d.
+static __global__ void __launch_bounds__(128) wf_extend(const __grid_constant__ Ctx c, Wave w, uint32_t d)
+{
+    uint32_t count = w.counts[d];
+    const uint32_t* qin = w.queue[d & 1u];
+    bool direct = d == 0 && c.p[P_ADAPTIVE] == 0;
+    for (;;) {
+        uint32_t base = warp_fetch(&w.fetch[d]);
+        if (base >= count)
+            break;
+        uint32_t i = base + lane_id();
+        if (i < count) {
+            uint32_t p = direct ? i : qin[i];
+            V3 org, dir;
+            if (d == 0) {
+                PathState<false> s = generatePathFor<false>(c, p % c.p[P_WIDTH], p / c.p[P_WIDTH], c.p[P_SAMPLE]);
+                org = s.org;
+                dir = s.dir;
+            } else {
+                float4 a = w.state[p];
+                float4 b = w.state[w.n + p];
+                org = v3(a.x, a.y, a.z);
+                dir = v3(b.x, b.y, b.z);
+            }
+            Hit h = traceClosest(c, org, dir);
+            w.hits[p] = make_uint4(h.hit ? 1u : 0u, h.inst, h.prim, __float_as_uint(h.t));
+        }
+        __syncwarp();
+    }
+}
+
+// wf_shade.slang:7-29: shade each live path of depth d, then queue it for d + 1 or finish it.
+template <bool LIGHT, bool RESTIR, typename A>
+__global__ void __launch_bounds__(128) wf_shade(const __grid_constant__ Ctx c, Wave w, uint32_t d)
+{
+    uint32_t count = w.counts[d];
+    const uint32_t* qin = w.queue[d & 1u];
+    uint32_t* qout = w.queue[(d + 1) & 1u];
+    bool direct = d == 0 && c.p[P_ADAPTIVE] == 0;
+    for (;;) {
+        uint32_t base = warp_fetch(&w.fetch[w.depth + 1 + d]);
+        if (base >= count)
+            break;
+        uint32_t i = base + lane_id();
+        bool live = false;
+        uint32_t p = 0;
+        if (i < count) {
+            p = direct ? i : qin[i];
+            PathState<LIGHT> st = loadPath<LIGHT>(c, w, p, d);
+            uint4 hr = w.hits[p];
+            Hit h;
+            h.hit = hr.x != 0;
+            h.inst = hr.y;
+            h.prim = hr.z;
+            h.t = __uint_as_float(hr.w);
+            if (shadePath<LIGHT, RESTIR>(c, st, h, d, p) && d + 1 < w.depth) {
+                storePath<LIGHT>(w, st, p);
+                live = true;
+            } else {
+                finishPath<LIGHT, A>(c, st, p);
+            }
+        }
+        __syncwarp();
+        warp_append(&w.counts[d + 1], qout, live, p);
+    }
+}
+
+// Closest hits of caller-given rays (6 floats each: origin, direction): the traversal alone, for
+// checking it against an independent implementation and for timing it.
+static __global__ void __launch_bounds__(128) trace_rays(const __grid_constant__ Ctx c, const float* rays, uint4* out,
+                                                   uint32_t n, uint32_t* fetch)
+{
+    for (;;) {
+        uint32_t base = warp_fetch(fetch);
+        if (base >= n)
+            break;
+        uint32_t i = base + lane_id();
+        if (i < n) {
+            const float* r = rays + 6 * (size_t)i;
+            Hit h = traceClosest(c, v3(r[0], r[1], r[2]), v3(r[3], r[4], r[5]));
+            out[i] = make_uint4(h.hit ? 1u : 0u, h.inst, h.prim, __float_as_uint(h.t));
+        }
+        __syncwarp();
+    }
+}
+
+// Any-hit queries of caller-given rays (7 floats each: origin, direction, tmax) through the
+// shadow-ray path (`occluded`, including translucent layers).
+static __global__ void __launch_bounds__(128) occlusion_rays(const __grid_constant__ Ctx c, const float* rays, uint32_t* out,
+                                                       uint32_t n)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const float* r = rays + 7 * (size_t)i;
+    out[i] = occluded(c, v3(r[0], r[1], r[2]), v3(r[3], r[4], r[5]), r[6]) ? 1u : 0u;
+}
+
+} // namespace vgk

@@ -1,0 +1,31 @@
+// Host-side launchers of the kernel variants. The variants are compiled in separate translation
+// units (kern_mk.cu, kern_wf.cu) so the build runs them in parallel.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "ctx.h"
+
+namespace vgx {
+
+// Compile-time variant of the path core: lighting split on, ReSTIR compiled in (the reference's
+// `restirCompiled` specialisation constant, pt_core.slang:51-53), double-precision sums.
+struct Variant {
+    bool light;
+    bool restir;
+    bool f64;
+    int index() const { return (light ? 1 : 0) | (restir ? 2 : 0) | (f64 ? 4 : 0); }
+};
+
+cudaError_t launch_megakernel(Variant v, dim3 grid, cudaStream_t s, const vgd::Ctx& c);
+cudaError_t launch_wf_shade(Variant v, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w, uint32_t d);
+int wf_shade_blocks_per_sm(Variant v);
+
+cudaError_t launch_wf_begin(cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w);
+cudaError_t launch_wf_select(bool f64, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w);
+cudaError_t launch_wf_extend(int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w, uint32_t d);
+int wf_extend_blocks_per_sm();
+cudaError_t launch_trace_rays(int blocks, cudaStream_t s, const vgd::Ctx& c, const float* rays, uint4* out, uint32_t n,
+                              uint32_t* fetch);
+cudaError_t launch_occlusion_rays(cudaStream_t s, const vgd::Ctx& c, const float* rays, uint32_t* out, uint32_t n);
+
+} // namespace vgx

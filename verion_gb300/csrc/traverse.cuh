@@ -1,0 +1,229 @@
+// Software ray traversal of the quantised 8-wide BVH (bvh8.h) on sm_103a, standing in for the
+// hardware ray queries of Verion's kernels: `traceClosest` (shaders/include/pt_core.slang:684-700,
+// closest opaque hit, TMin 0, TMax 1e30) and the shadow-ray query inside `occluded` (:580-613,
+// accept the first hit and end the search).
+//
+// Hit rule, identical in the CPU oracle: a triangle is hit at distance t when the watertight test
+// of Woop, Benthin and Wald ("Watertight Ray/Triangle Intersection", JCGT 2013) accepts it and
+// 0 < t < tmax. The closest hit is the smallest t; equal distances go to the lower global triangle
+// index, so the answer does not depend on the order the tree is walked in.
+//
+// Child boxes are tested with the robust slab test (far distance scaled by 1 + 2 gamma(3), Ize
+// 2013), which never rejects a box the ray touches, so the culling cannot change the answer.
+#pragma once
+#include "bvh8.h"
+#include "vec3.h"
+
+namespace vgt {
+
+struct TRay {
+    V3 o, d;
+    float ix, iy, iz; // reciprocal direction for the slab test (tiny components clamped)
+    uint32_t oct;     // sign octant of the direction
+    int kx, ky, kz;   // watertight test axis permutation
+    float sx, sy, sz; // watertight test shear
+};
+
+__device__ __forceinline__ float slab_rcp(float d)
+{
+    float a = fabsf(d);
+    if (a < bvh8::MIN_DIR)
+        d = copysignf(bvh8::MIN_DIR, d);
+    return 1.0f / d;
+}
+
+__device__ __forceinline__ TRay make_ray(V3 o, V3 d)
+{
+    TRay r;
+    r.o = o;
+    r.d = d;
+    r.ix = slab_rcp(d.x);
+    r.iy = slab_rcp(d.y);
+    r.iz = slab_rcp(d.z);
+    r.oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = 0;
+    if (ay > ax)
+        kz = 1;
+    if (az > (kz == 0 ? ax : ay))
+        kz = 2;
+    int kx = kz + 1 == 3 ? 0 : kz + 1;
+    int ky = kx + 1 == 3 ? 0 : kx + 1;
+    float dz = comp(d, kz);
+    if (dz < 0.0f) {
+        int t = kx;
+        kx = ky;
+        ky = t;
+    }
+    r.kx = kx;
+    r.ky = ky;
+    r.kz = kz;
+    r.sx = comp(d, kx) / dz;
+    r.sy = comp(d, ky) / dz;
+    r.sz = 1.0f / dz;
+    return r;
+}
+
+// Watertight test. On success returns true with the distance t = T / det and the edge functions
+// (U, V, W weigh vertices 0, 1, 2; divided by det they are the barycentrics).
+__device__ __forceinline__ bool tri_test(const TRay& r, V3 v0, V3 v1, V3 v2, float& t, float& U, float& V, float& W,
+                                         float& det)
+{
+    V3 A = v0 - r.o;
+    V3 B = v1 - r.o;
+    V3 C = v2 - r.o;
+    float Akz = comp(A, r.kz), Bkz = comp(B, r.kz), Ckz = comp(C, r.kz);
+    float Ax = comp(A, r.kx) - r.sx * Akz;
+    float Ay = comp(A, r.ky) - r.sy * Akz;
+    float Bx = comp(B, r.kx) - r.sx * Bkz;
+    float By = comp(B, r.ky) - r.sy * Bkz;
+    float Cx = comp(C, r.kx) - r.sx * Ckz;
+    float Cy = comp(C, r.ky) - r.sy * Ckz;
+    U = Cx * By - Cy * Bx;
+    V = Ax * Cy - Ay * Cx;
+    W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        // Edge hit: redo the 2x2 determinants in double precision (the paper's fallback).
+        double cxby = (double)Cx * (double)By, cybx = (double)Cy * (double)Bx;
+        double axcy = (double)Ax * (double)Cy, aycx = (double)Ay * (double)Cx;
+        double bxay = (double)Bx * (double)Ay, byax = (double)By * (double)Ax;
+        U = (float)(cxby - cybx);
+        V = (float)(axcy - aycx);
+        W = (float)(bxay - byax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f))
+        return false;
+    det = U + V + W;
+    if (det == 0.0f)
+        return false;
+    float Az = r.sz * Akz;
+    float Bz = r.sz * Bkz;
+    float Cz = r.sz * Ckz;
+    float T = U * Az + V * Bz + W * Cz;
+    t = T / det;
+    return t > 0.0f;
+}
+
+struct TraceHit {
+    bool hit;
+    uint32_t inst, prim, gid;
+    float t;
+    float b1, b2; // barycentric weights of vertices 1 and 2
+};
+
+__device__ __forceinline__ uint32_t byte_of(uint32_t lo, uint32_t hi, int i)
+{
+    uint32_t w = i < 4 ? lo : hi;
+    return (w >> ((i & 3) * 8)) & 0xffu;
+}
+
+// Closest hit (ANY = false) or any hit (ANY = true) with 0 < t < tmax.
+template <bool ANY>
+__device__ __forceinline__ TraceHit trace_bvh(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
+                                              const TRay& r, float tmax, uint32_t* err)
+{
+    TraceHit h;
+    h.hit = false;
+    h.inst = h.prim = 0;
+    h.gid = 0xffffffffu;
+    h.t = tmax;
+    h.b1 = h.b2 = 0.0f;
+    float best_t = tmax;
+    uint2 stack[bvh8::STACK_SIZE];
+    int sp = 0;
+    uint32_t node = 0;
+    for (;;) {
+        const uint4* np = nodes + (size_t)node * bvh8::NODE_VEC4;
+        uint4 w0 = __ldg(np);
+        uint4 w1 = __ldg(np + 1);
+        uint4 w2 = __ldg(np + 2);
+        uint4 w3 = __ldg(np + 3);
+        uint4 w4 = __ldg(np + 4);
+        float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
+        uint32_t em = w0.w;
+        float scx = __uint_as_float((em & 0xffu) << 23);
+        float scy = __uint_as_float(((em >> 8) & 0xffu) << 23);
+        float scz = __uint_as_float(((em >> 16) & 0xffu) << 23);
+        uint32_t imask = em >> 24;
+        uint32_t child_base = w1.x, tri_base = w1.y, meta_lo = w1.z, meta_hi = w1.w;
+        bool px_pos = r.ix >= 0.0f, py_pos = r.iy >= 0.0f, pz_pos = r.iz >= 0.0f;
+        // Near and far quantised planes per axis (low words at w2.x .. high words at w4.w).
+        uint32_t nxl = px_pos ? w2.x : w3.z, nxh = px_pos ? w2.y : w3.w;
+        uint32_t fxl = px_pos ? w3.z : w2.x, fxh = px_pos ? w3.w : w2.y;
+        uint32_t nyl = py_pos ? w2.z : w4.x, nyh = py_pos ? w2.w : w4.y;
+        uint32_t fyl = py_pos ? w4.x : w2.z, fyh = py_pos ? w4.y : w2.w;
+        uint32_t nzl = pz_pos ? w3.x : w4.z, nzh = pz_pos ? w3.y : w4.w;
+        uint32_t fzl = pz_pos ? w4.z : w3.x, fzh = pz_pos ? w4.w : w3.y;
+        uint32_t inner_hits = 0;
+        uint32_t tri_bits = 0;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            float tnx = (fmaf((float)byte_of(nxl, nxh, i), scx, px) - r.o.x) * r.ix;
+            float tny = (fmaf((float)byte_of(nyl, nyh, i), scy, py) - r.o.y) * r.iy;
+            float tnz = (fmaf((float)byte_of(nzl, nzh, i), scz, pz) - r.o.z) * r.iz;
+            float tfx = (fmaf((float)byte_of(fxl, fxh, i), scx, px) - r.o.x) * r.ix;
+            float tfy = (fmaf((float)byte_of(fyl, fyh, i), scy, py) - r.o.y) * r.iy;
+            float tfz = (fmaf((float)byte_of(fzl, fzh, i), scz, pz) - r.o.z) * r.iz;
+            float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
+            float tf = fminf(fminf(fminf(tfx, tfy), tfz) * bvh8::ROBUST_FAR, best_t);
+            if (tn <= tf) {
+                if ((imask >> i) & 1u) {
+                    inner_hits |= 1u << (i ^ r.oct);
+                } else {
+                    uint32_t m = byte_of(meta_lo, meta_hi, i);
+                    uint32_t cnt = m >> 5;
+                    tri_bits |= ((1u << cnt) - 1u) << (m & 31u);
+                }
+            }
+        }
+        // Triangles of this node's leaf slots.
+        while (tri_bits) {
+            uint32_t j = __ffs(tri_bits) - 1;
+            tri_bits &= tri_bits - 1;
+            const float4* tp = tris + (size_t)(tri_base + j) * bvh8::TRI_VEC4;
+            float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            float t, U, V, W, det;
+            if (tri_test(r, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), t, U, V, W, det)) {
+                uint32_t gid = __float_as_uint(c.w);
+                bool take = ANY ? t < tmax : (t < best_t || (h.hit && t == best_t && gid < h.gid));
+                if (take) {
+                    h.hit = true;
+                    h.t = t;
+                    best_t = t;
+                    h.gid = gid;
+                    h.inst = __float_as_uint(a.w);
+                    h.prim = __float_as_uint(b.w);
+                    h.b1 = V / det;
+                    h.b2 = W / det;
+                    if (ANY)
+                        return h;
+                }
+            }
+        }
+        // Next node: from this node's hit children, else from the stack.
+        uint32_t hits = inner_hits;
+        uint32_t gbase = child_base, gmask = imask;
+        if (hits == 0) {
+            if (sp == 0)
+                break;
+            --sp;
+            gbase = stack[sp].x;
+            gmask = stack[sp].y & 0xffu;
+            hits = stack[sp].y >> 8;
+        }
+        uint32_t b = __ffs(hits) - 1;
+        hits &= hits - 1;
+        uint32_t slot = b ^ r.oct;
+        node = gbase + __popc(gmask & ((1u << slot) - 1u));
+        if (hits) {
+            if (sp >= (int)bvh8::STACK_SIZE) {
+                atomicOr(err, bvh8::ERR_STACK);
+                break;
+            }
+            stack[sp++] = make_uint2(gbase, gmask | (hits << 8));
+        }
+    }
+    return h;
+}
+
+} // namespace vgt

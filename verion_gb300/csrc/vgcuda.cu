@@ -1,0 +1,1063 @@
+// C-ABI implementation of the CUDA backend (include/vgcuda.h): context, renderer (table upload,
+// validation, BVH build), accumulations and the host loops that issue the kernels.
+//
+// Reference behaviour restated here:
+//   Renderer::build / new      crates/verion-gpu-metal/src/renderer.rs:151-219
+//   accumulate                 crates/verion-gpu-metal/src/renderer.rs:775-856
+//   encode_megakernel          crates/verion-gpu-metal/src/renderer.rs:449-487 (8 samples a dispatch)
+//   run_wavefront              crates/verion-gpu-metal/src/renderer/wavefront.rs:93-177
+//   new_accumulation           crates/verion-gpu-metal/src/renderer.rs:858-903
+//   base_params                crates/verion-gpu/src/pack.rs:828-874
+// The host compiler must not contract floating-point expressions (-ffp-contract=off): the world
+// vertices of the BVH are computed with the kernels' transformPoint arithmetic.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/vgcuda.h"
+#include "bvh_build.h"
+#include "launch.h"
+
+using namespace vgl;
+
+namespace {
+
+thread_local std::string g_err;
+thread_local uint64_t g_oom_needed = 0, g_oom_available = 0;
+
+int fail(int status, const std::string& msg)
+{
+    g_err = msg;
+    return status;
+}
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    if (e == cudaErrorMemoryAllocation)
+        return fail(VG_ERR_OOM, std::string(what) + ": " + cudaGetErrorString(e));
+    return fail(VG_ERR_KERNEL, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define VG_CHECK(expr, what)                                                                                        \
+    do {                                                                                                            \
+        cudaError_t e_ = (expr);                                                                                    \
+        if (e_ != cudaSuccess)                                                                                      \
+            return cuda_fail(e_, what);                                                                             \
+    } while (0)
+
+uint32_t f2u(float f)
+{
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return u;
+}
+
+float u2f(uint32_t u)
+{
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
+// Host deadline for one blocking call; GPU waits poll against it instead of blocking forever.
+double wait_deadline_seconds()
+{
+    const char* s = getenv("VG_TIMEOUT_S");
+    double v = s ? atof(s) : 0.0;
+    return v > 0.0 ? v : 600.0;
+}
+
+int wait_event(cudaEvent_t ev)
+{
+    auto t0 = std::chrono::steady_clock::now();
+    double limit = wait_deadline_seconds();
+    for (;;) {
+        cudaError_t e = cudaEventQuery(ev);
+        if (e == cudaSuccess)
+            return VG_OK;
+        if (e != cudaErrorNotReady)
+            return cuda_fail(e, "kernel execution");
+        double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (dt > limit)
+            return fail(VG_ERR_TIMEOUT, "the GPU did not finish within " + std::to_string(limit) + " s");
+        std::this_thread::sleep_for(std::chrono::microseconds(dt < 0.01 ? 20 : 200));
+    }
+}
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+} // namespace
+
+struct VgContext {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int sms = 0;
+    uint64_t uploaded = 0;
+};
+
+struct Restir {
+    bool on = false;
+    bool di = true, gi = false;
+    uint32_t candidates = 4, history = 4;
+    bool operator==(const Restir& o) const
+    {
+        return on == o.on && (!on || (di == o.di && gi == o.gi && candidates == o.candidates && history == o.history));
+    }
+};
+
+struct VgRenderer {
+    VgContext* ctx = nullptr;
+    DevBuf positions, indices, uvs, vnormals, instances, materials, lights, emitters, emit_cdf, env_pixels,
+        env_marginal, env_cond, texels, tex_info, nodes, tris, err, scratch;
+    vgd::DeviceScene ds{};
+    VgSceneInfo info{};
+    VgView view{};
+    VgBvhInfo bvh{};
+    uint32_t instance_count = 0;
+    bool multiscatter = true;
+    int integrator = VG_MEGAKERNEL;
+    bool stage_timing = false;
+    bool adaptive = false;
+    float adaptive_threshold = 0.02f;
+    uint32_t adaptive_min_spp = 16;
+    Restir restir;
+    uint32_t max_depth = DEFAULT_MAX_DEPTH;
+    int precision = 64;
+    int extend_blocks = 0;
+    int shade_blocks[8] = {};
+};
+
+struct VgAccum {
+    VgRenderer* owner = nullptr;
+    uint32_t width = 0, height = 0;
+    bool lighting = false;
+    int precision = 64;
+    uint32_t samples = 0;
+    double gpu_seconds = 0.0;
+    bool stage_ran = false;
+    double stage_seconds[2] = {0.0, 0.0};
+    uint64_t extend_launches_timed = 0;
+    uint64_t launches = 0;
+    DevBuf accum, stats, light;
+    bool adaptive_fixed = false; // adaptive setting captured at the first sample
+    bool adaptive = false;
+    Restir restir;               // captured at the first sample
+    DevBuf re_g[2], re_n[2], re_x[2], re_m[2];
+    DevBuf state, hits, queue[2], counts, fetch;
+    size_t wavefront_bytes = 0;
+    size_t restir_bytes = 0;
+    uint32_t last_depth = 0; // max depth of the last wavefront sample
+};
+
+namespace {
+
+int check_fits(size_t bytes)
+{
+    size_t free_b = 0, total_b = 0;
+    cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaMemGetInfo");
+    if (bytes > free_b) {
+        g_oom_needed = bytes;
+        g_oom_available = free_b;
+        return fail(VG_ERR_OOM, "out of GPU memory: needed " + std::to_string(bytes) + " bytes, available " +
+                                    std::to_string(free_b));
+    }
+    return VG_OK;
+}
+
+int alloc(DevBuf& b, size_t bytes, cudaStream_t s, bool zero)
+{
+    b.release();
+    size_t n = std::max<size_t>(bytes, 16);
+    int st = check_fits(n);
+    if (st != VG_OK)
+        return st;
+    cudaError_t e = cudaMalloc(&b.p, n);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        return cuda_fail(e, "cudaMalloc");
+    }
+    b.bytes = n;
+    if (zero) {
+        e = cudaMemsetAsync(b.p, 0, n, s);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaMemsetAsync");
+    }
+    return VG_OK;
+}
+
+int upload(VgContext* ctx, DevBuf& b, const void* src, size_t bytes)
+{
+    int st = alloc(b, bytes, ctx->stream, bytes == 0);
+    if (st != VG_OK)
+        return st;
+    if (bytes > 0) {
+        if (!src)
+            return fail(VG_ERR_INVALID, "null table pointer with non-zero length");
+        VG_CHECK(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, ctx->stream), "upload");
+        ctx->uploaded += bytes;
+    }
+    return VG_OK;
+}
+
+// Checks every index the kernels follow, so a malformed table is an error here instead of an
+// out-of-bounds read on the GPU.
+int validate(const VgPacked* pk)
+{
+    if (pk->instance_count == 0 || pk->instances_len == 0)
+        return fail(VG_ERR_SCENE, "scene has no instances");
+    if (pk->instances_len != (size_t)pk->instance_count * INSTANCE_WORDS)
+        return fail(VG_ERR_INVALID, "instance table length does not match the instance count");
+    size_t verts = pk->positions_len / 3;
+    if (pk->positions_len % 3 != 0 || pk->uvs_len != 2 * verts || pk->vnormals_len != 3 * verts)
+        return fail(VG_ERR_INVALID, "vertex tables disagree in length");
+    if (pk->materials_len % MATERIAL_WORDS != 0 || pk->materials_len == 0)
+        return fail(VG_ERR_INVALID, "material table length is not a multiple of 24");
+    size_t materials = pk->materials_len / MATERIAL_WORDS;
+    size_t textures = pk->tex_info_len / 4;
+    if (pk->tex_info_len % 4 != 0)
+        return fail(VG_ERR_INVALID, "texture info length is not a multiple of 4");
+    for (size_t t = 0; t < textures; t++) {
+        uint64_t off = pk->tex_info[4 * t], w = pk->tex_info[4 * t + 1], h = pk->tex_info[4 * t + 2],
+                 levels = pk->tex_info[4 * t + 3];
+        if (w == 0 || h == 0 || levels == 0)
+            return fail(VG_ERR_INVALID, "texture with zero size");
+        uint64_t end = off, lw = w, lh = h;
+        for (uint64_t k = 0; k < levels; k++) {
+            end += lw * lh;
+            lw = std::max<uint64_t>(lw / 2, 1);
+            lh = std::max<uint64_t>(lh / 2, 1);
+        }
+        if (3 * end > pk->texels_len)
+            return fail(VG_ERR_INVALID, "texture mip chain beyond the texel table");
+    }
+    for (size_t m = 0; m < materials; m++) {
+        for (int k : {10, 11, 12, 13, 23}) {
+            float v = pk->materials[m * MATERIAL_WORDS + k];
+            if (!(v >= 0.0f) || v > (float)textures)
+                return fail(VG_ERR_INVALID, "material refers to a missing texture");
+        }
+    }
+    uint32_t ec = pk->info.emitter_count;
+    if (pk->emitters_len != (size_t)ec * EMITTER_WORDS || pk->emit_cdf_len != ec)
+        return fail(VG_ERR_INVALID, "emitter tables disagree with the emitter count");
+    uint32_t lc = pk->info.light_count;
+    size_t light_need = (size_t)lc * LIGHT_WORDS + ALBEDO_WORDS + 2 * (size_t)pk->instance_count;
+    if (pk->lights_len < light_need)
+        return fail(VG_ERR_INVALID, "light table shorter than lights + albedo tables + link masks");
+    for (uint32_t l = 0; l < lc; l++) {
+        uint32_t kind = pk->lights[l * LIGHT_WORDS];
+        if (kind > 3)
+            return fail(VG_ERR_INVALID, "unknown light kind");
+        if (pk->lights[l * LIGHT_WORDS + 13] > 3)
+            return fail(VG_ERR_INVALID, "light slot beyond 3");
+        uint32_t ies = pk->lights[l * LIGHT_WORDS + 15];
+        if (ies != 0 && (size_t)(ies - 1) + 9 + 361 * 181 > pk->lights_len)
+            return fail(VG_ERR_INVALID, "IES profile beyond the light table");
+    }
+    if (pk->mesh_count == 0 || !pk->tlas_mesh)
+        return fail(VG_ERR_INVALID, "missing mesh ranges");
+    for (size_t i = 0; i < pk->instance_count; i++) {
+        const uint32_t* rec = &pk->instances[i * INSTANCE_WORDS];
+        uint32_t m = pk->tlas_mesh[i];
+        if (m >= pk->mesh_count)
+            return fail(VG_ERR_INVALID, "instance refers to a missing mesh");
+        const VgMeshRange& mr = pk->meshes[m];
+        if (rec[0] != mr.vertex_offset || rec[1] != mr.index_offset)
+            return fail(VG_ERR_INVALID, "instance record disagrees with its mesh range");
+        if (mr.index_count % 3 != 0 || (uint64_t)mr.index_offset + mr.index_count > pk->indices_len)
+            return fail(VG_ERR_INVALID, "mesh index range beyond the index table");
+        if ((uint64_t)mr.vertex_offset + mr.vertex_count > verts)
+            return fail(VG_ERR_INVALID, "mesh vertex range beyond the vertex table");
+        for (uint32_t k = 0; k < mr.index_count; k++)
+            if (pk->indices[mr.index_offset + k] >= mr.vertex_count)
+                return fail(VG_ERR_INVALID, "triangle index beyond its mesh's vertices");
+        if (rec[2] >= materials)
+            return fail(VG_ERR_INVALID, "instance refers to a missing material");
+        if (rec[3] != 0 && (uint64_t)rec[3] - 1 + mr.index_count / 3 > ec)
+            return fail(VG_ERR_INVALID, "instance emitter range beyond the emitter table");
+    }
+    uint32_t ew = pk->info.env_width, eh = pk->info.env_height;
+    if (ew > 0) {
+        if (eh == 0 || pk->env_pixels_len != 3 * (size_t)ew * eh || pk->env_marginal_len != eh ||
+            pk->env_conditional_len != (size_t)ew * eh)
+            return fail(VG_ERR_INVALID, "environment tables disagree with their size");
+    }
+    return VG_OK;
+}
+
+int blocks_for(VgRenderer* r, int per_sm) { return std::max(1, per_sm) * r->ctx->sms; }
+
+vgx::Variant variant_of(const VgRenderer* r, const VgAccum* acc)
+{
+    vgx::Variant v;
+    v.light = acc->lighting;
+    v.restir = acc->restir.on;
+    v.f64 = acc->precision == 64;
+    return v;
+}
+
+// pack.rs:828-874, with the renderer's depth in word 7.
+void base_params(const VgRenderer* r, const VgAccum* acc, uint32_t* p)
+{
+    memset(p, 0, PARAM_WORDS * 4);
+    p[P_WIDTH] = acc->width;
+    p[P_HEIGHT] = acc->height;
+    p[P_TAN_HALF_FOV] = f2u(r->view.camera[2]);
+    p[P_APERTURE] = f2u(r->view.aperture);
+    p[P_FOCUS] = f2u(r->view.focus);
+    p[P_LIGHT_COUNT] = r->info.light_count;
+    p[P_MAX_DEPTH] = r->max_depth;
+    for (int i = 0; i < 12; i++)
+        p[P_CAMERA + i] = f2u(r->view.camera[4 + i]);
+    for (int i = 0; i < 3; i++)
+        p[P_SKY + i] = f2u(r->info.sky[i]);
+    p[P_EMITTER_COUNT] = r->info.emitter_count;
+    p[P_ENV_W] = r->info.env_width;
+    p[P_ENV_H] = r->info.env_height;
+    p[P_ENV_PDF_SCALE] = f2u(r->info.env_pdf_scale);
+    p[P_PIXEL_CONE] = f2u(2.0f * r->view.camera[2] / (float)acc->height);
+    p[P_VIRTUAL_LIGHT] = r->info.virtual_light;
+    p[P_TRANSPARENT_BG] = r->info.transparent_background;
+    p[P_SHIFT_X] = f2u(r->view.shift[0]);
+    p[P_SHIFT_Y] = f2u(r->view.shift[1]);
+    p[P_LIGHTING] = acc->lighting ? 1u : 0u;
+    p[P_MULTISCATTER] = r->multiscatter ? 1u : 0u;
+    if (r->adaptive) {
+        p[P_ADAPTIVE] = 1;
+        p[P_ADAPTIVE_THRESHOLD] = f2u(r->adaptive_threshold);
+        p[P_ADAPTIVE_MIN_SPP] = r->adaptive_min_spp;
+    }
+    if (r->restir.on) {
+        p[P_RESTIR] = (r->restir.di ? 1u : 0u) | (r->restir.gi ? 2u : 0u);
+        p[P_RESTIR_CANDIDATES] = r->restir.candidates;
+        p[P_RESTIR_HISTORY] = r->restir.history;
+    }
+}
+
+vgd::Ctx make_ctx(VgRenderer* r, VgAccum* acc)
+{
+    vgd::Ctx c;
+    memset(&c, 0, sizeof(c));
+    c.s = r->ds;
+    if (acc) {
+        base_params(r, acc, c.p);
+        c.accum = acc->accum.p;
+        c.stats = acc->stats.p;
+        c.lighting = (float*)acc->light.p;
+        for (int h = 0; h < 2; h++) {
+            c.re.g[h] = (float4*)acc->re_g[h].p;
+            c.re.n[h] = (float4*)acc->re_n[h].p;
+            c.re.x[h] = (float4*)acc->re_x[h].p;
+            c.re.m[h] = (float*)acc->re_m[h].p;
+        }
+    }
+    c.err = (uint32_t*)r->err.p;
+    return c;
+}
+
+int read_err(VgRenderer* r)
+{
+    uint32_t e = 0;
+    VG_CHECK(cudaMemcpyAsync(&e, r->err.p, 4, cudaMemcpyDeviceToHost, r->ctx->stream), "error flag");
+    VG_CHECK(cudaStreamSynchronize(r->ctx->stream), "error flag");
+    if (e & bvh8::ERR_STACK)
+        return fail(VG_ERR_KERNEL, "BVH traversal stack overflow");
+    if (e)
+        return fail(VG_ERR_KERNEL, "kernel reported error status " + std::to_string(e));
+    return VG_OK;
+}
+
+struct EventPool {
+    std::vector<cudaEvent_t> ev;
+    size_t used = 0;
+    cudaEvent_t get()
+    {
+        if (used == ev.size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            ev.push_back(e);
+        }
+        return ev[used++];
+    }
+    ~EventPool()
+    {
+        for (auto e : ev)
+            cudaEventDestroy(e);
+    }
+};
+
+} // namespace
+
+extern "C" {
+
+size_t vg_last_error(char* buf, size_t len)
+{
+    if (buf && len > 0) {
+        size_t n = std::min(len - 1, g_err.size());
+        memcpy(buf, g_err.data(), n);
+        buf[n] = 0;
+    }
+    return g_err.size();
+}
+
+void vg_last_oom(uint64_t* needed, uint64_t* available)
+{
+    if (needed)
+        *needed = g_oom_needed;
+    if (available)
+        *available = g_oom_available;
+}
+
+int vg_context_create(VgContext** out)
+{
+    if (!out)
+        return fail(VG_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(VG_ERR_NO_DEVICE, "no CUDA device");
+    }
+    cudaDeviceProp prop;
+    VG_CHECK(cudaGetDeviceProperties(&prop, 0), "cudaGetDeviceProperties");
+    if (prop.major != 10 || prop.minor != 3)
+        return fail(VG_ERR_UNSUPPORTED, std::string("device ") + prop.name + " is not sm_103 (GB300)");
+    VG_CHECK(cudaSetDevice(0), "cudaSetDevice");
+    VgContext* ctx = new VgContext();
+    ctx->device = 0;
+    ctx->sms = prop.multiProcessorCount;
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return cuda_fail(e, "cudaStreamCreate");
+    }
+    *out = ctx;
+    return VG_OK;
+}
+
+void vg_context_destroy(VgContext* ctx)
+{
+    if (!ctx)
+        return;
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+int vg_memory(VgContext* ctx, VgMemoryUsage* out)
+{
+    if (!ctx || !out)
+        return fail(VG_ERR_INVALID, "null argument");
+    size_t free_b = 0, total_b = 0;
+    VG_CHECK(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+    out->budget = total_b;
+    out->allocated = total_b - free_b;
+    out->uploaded = ctx->uploaded;
+    return VG_OK;
+}
+
+int vg_renderer_create(VgContext* ctx, const VgPacked* pk, VgRenderer** out)
+{
+    if (!ctx || !pk || !out)
+        return fail(VG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    int st = validate(pk);
+    if (st != VG_OK)
+        return st;
+    VgRenderer* r = new VgRenderer();
+    r->ctx = ctx;
+    r->info = pk->info;
+    r->view = pk->view;
+    r->instance_count = (uint32_t)pk->instance_count;
+    // World-space triangles for the BVH: each instance's mesh through its transform, with the
+    // arithmetic of transformPoint (pt_core.slang:90-99) so the kernels' vertices match.
+    std::vector<float> verts;
+    std::vector<uint32_t> tinst, tprim;
+    size_t total = 0;
+    for (size_t i = 0; i < pk->instance_count; i++)
+        total += pk->meshes[pk->tlas_mesh[i]].index_count / 3;
+    if (total > 0xffffffffu / 2) {
+        delete r;
+        return fail(VG_ERR_SCENE, "too many triangles");
+    }
+    verts.reserve(total * 9);
+    tinst.reserve(total);
+    tprim.reserve(total);
+    for (size_t i = 0; i < pk->instance_count; i++) {
+        const uint32_t* rec = &pk->instances[i * INSTANCE_WORDS];
+        const VgMeshRange& mr = pk->meshes[pk->tlas_mesh[i]];
+        float m[12];
+        for (int k = 0; k < 12; k++)
+            m[k] = u2f(rec[4 + k]);
+        for (uint32_t t = 0; t < mr.index_count / 3; t++) {
+            for (int v = 0; v < 3; v++) {
+                uint32_t vi = pk->indices[mr.index_offset + 3 * t + v] + rec[0];
+                float x = pk->positions[3 * vi], y = pk->positions[3 * vi + 1], z = pk->positions[3 * vi + 2];
+                for (int row = 0; row < 3; row++)
+                    verts.push_back(m[4 * row] * x + m[4 * row + 1] * y + m[4 * row + 2] * z + m[4 * row + 3]);
+            }
+            tinst.push_back((uint32_t)i);
+            tprim.push_back(t);
+        }
+    }
+    Bvh8Host bvh;
+    std::string err;
+    if (!build_bvh8(verts.data(), tinst.data(), tprim.data(), (uint32_t)total, bvh, err)) {
+        delete r;
+        return fail(VG_ERR_SCENE, err);
+    }
+    r->bvh.triangles = bvh.triangles;
+    r->bvh.wide_nodes = bvh.wide_nodes;
+    r->bvh.wide_depth = bvh.wide_depth;
+    r->bvh.binary_nodes = bvh.binary_nodes;
+    r->bvh.binary_depth = bvh.binary_depth;
+    r->bvh.node_bytes = bvh.nodes.size() * 4;
+    r->bvh.triangle_bytes = bvh.tris.size() * 4;
+    r->bvh.build_seconds = bvh.build_seconds;
+
+    bool translucent = false;
+    for (size_t m = 0; m < pk->materials_len / MATERIAL_WORDS; m++)
+        if (pk->materials[m * MATERIAL_WORDS + 22] < 1.0f || pk->materials[m * MATERIAL_WORDS + 23] > 0.0f)
+            translucent = true;
+
+#define UP(buf, src, n)                                                                                             \
+    do {                                                                                                            \
+        st = upload(ctx, r->buf, src, (n));                                                                         \
+        if (st != VG_OK) {                                                                                          \
+            vg_renderer_destroy(r);                                                                                 \
+            return st;                                                                                              \
+        }                                                                                                           \
+    } while (0)
+    UP(positions, pk->positions, pk->positions_len * 4);
+    UP(indices, pk->indices, pk->indices_len * 4);
+    UP(uvs, pk->uvs, pk->uvs_len * 4);
+    UP(vnormals, pk->vnormals, pk->vnormals_len * 4);
+    UP(instances, pk->instances, pk->instances_len * 4);
+    UP(materials, pk->materials, pk->materials_len * 4);
+    UP(lights, pk->lights, pk->lights_len * 4);
+    UP(emitters, pk->emitters, pk->emitters_len * 4);
+    UP(emit_cdf, pk->emit_cdf, pk->emit_cdf_len * 4);
+    UP(env_pixels, pk->env_pixels, pk->env_pixels_len * 4);
+    UP(env_marginal, pk->env_marginal, pk->env_marginal_len * 4);
+    UP(env_cond, pk->env_conditional, pk->env_conditional_len * 4);
+    UP(texels, pk->texels, pk->texels_len * 4);
+    UP(tex_info, pk->tex_info, pk->tex_info_len * 4);
+    UP(nodes, bvh.nodes.data(), bvh.nodes.size() * 4);
+    UP(tris, bvh.tris.data(), bvh.tris.size() * 4);
+#undef UP
+    st = alloc(r->err, 16, ctx->stream, true);
+    if (st != VG_OK) {
+        vg_renderer_destroy(r);
+        return st;
+    }
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        vg_renderer_destroy(r);
+        return cuda_fail(e, "upload");
+    }
+    r->ds.positions = (const float*)r->positions.p;
+    r->ds.indices = (const uint32_t*)r->indices.p;
+    r->ds.instances = (const uint32_t*)r->instances.p;
+    r->ds.materials = (const float*)r->materials.p;
+    r->ds.lights = (const uint32_t*)r->lights.p;
+    r->ds.emitters = (const float*)r->emitters.p;
+    r->ds.emit_cdf = (const float*)r->emit_cdf.p;
+    r->ds.env_pixels = (const float*)r->env_pixels.p;
+    r->ds.env_marginal = (const float*)r->env_marginal.p;
+    r->ds.env_cond = (const float*)r->env_cond.p;
+    r->ds.uvs = (const float*)r->uvs.p;
+    r->ds.texels = (const float*)r->texels.p;
+    r->ds.tex_info = (const uint32_t*)r->tex_info.p;
+    r->ds.vnormals = (const float*)r->vnormals.p;
+    r->ds.nodes = (const uint4*)r->nodes.p;
+    r->ds.tris = (const float4*)r->tris.p;
+    r->ds.shadow_any = translucent ? 0u : 1u;
+    r->extend_blocks = vgx::wf_extend_blocks_per_sm();
+    *out = r;
+    return VG_OK;
+}
+
+void vg_renderer_destroy(VgRenderer* r)
+{
+    if (!r)
+        return;
+    cudaStreamSynchronize(r->ctx->stream);
+    delete r;
+}
+
+int vg_renderer_bvh_info(const VgRenderer* r, VgBvhInfo* out)
+{
+    if (!r || !out)
+        return fail(VG_ERR_INVALID, "null argument");
+    *out = r->bvh;
+    return VG_OK;
+}
+
+int vg_set_camera(VgRenderer* r, const VgView* view)
+{
+    if (!r || !view)
+        return fail(VG_ERR_INVALID, "null argument");
+    r->view = *view;
+    return VG_OK;
+}
+
+int vg_set_multiscatter(VgRenderer* r, int on)
+{
+    if (!r)
+        return fail(VG_ERR_INVALID, "null renderer");
+    r->multiscatter = on != 0;
+    return VG_OK;
+}
+
+int vg_set_integrator(VgRenderer* r, int integrator)
+{
+    if (!r || (integrator != VG_MEGAKERNEL && integrator != VG_WAVEFRONT))
+        return fail(VG_ERR_INVALID, "bad integrator");
+    r->integrator = integrator;
+    return VG_OK;
+}
+
+int vg_integrator(const VgRenderer* r) { return r ? r->integrator : -1; }
+
+int vg_set_stage_timing(VgRenderer* r, int on)
+{
+    if (!r)
+        return fail(VG_ERR_INVALID, "null renderer");
+    r->stage_timing = on != 0;
+    return VG_OK;
+}
+
+int vg_set_adaptive(VgRenderer* r, int on, float threshold, uint32_t min_spp)
+{
+    if (!r)
+        return fail(VG_ERR_INVALID, "null renderer");
+    r->adaptive = on != 0;
+    r->adaptive_threshold = threshold;
+    r->adaptive_min_spp = min_spp;
+    return VG_OK;
+}
+
+int vg_set_restir(VgRenderer* r, int on, int di, int gi, uint32_t candidates, uint32_t history)
+{
+    if (!r)
+        return fail(VG_ERR_INVALID, "null renderer");
+    if (on && gi)
+        return fail(VG_ERR_UNSUPPORTED, "ReSTIR GI is not available in this backend");
+    r->restir.on = on != 0;
+    r->restir.di = di != 0;
+    r->restir.gi = gi != 0;
+    r->restir.candidates = candidates;
+    r->restir.history = history;
+    return VG_OK;
+}
+
+int vg_set_max_depth(VgRenderer* r, uint32_t depth)
+{
+    if (!r || depth == 0 || depth > 64)
+        return fail(VG_ERR_INVALID, "max depth must be in 1..64");
+    r->max_depth = depth;
+    return VG_OK;
+}
+
+int vg_set_accum_precision(VgRenderer* r, int bits)
+{
+    if (!r || (bits != 32 && bits != 64))
+        return fail(VG_ERR_INVALID, "precision must be 32 or 64");
+    r->precision = bits;
+    return VG_OK;
+}
+
+int vg_accum_create(VgRenderer* r, uint32_t width, uint32_t height, int lighting, VgAccum** out)
+{
+    if (!r || !out)
+        return fail(VG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (width == 0 || height == 0)
+        return fail(VG_ERR_SCENE, "image size must be non-zero");
+    if ((uint64_t)width * height > 0x7fffffffull)
+        return fail(VG_ERR_INVALID, "image too large");
+    VgAccum* acc = new VgAccum();
+    acc->owner = r;
+    acc->width = width;
+    acc->height = height;
+    acc->lighting = lighting != 0;
+    acc->precision = r->precision;
+    size_t px = (size_t)width * height;
+    size_t es = acc->precision == 64 ? 8 : 4;
+    int st = alloc(acc->accum, px * 3 * es, r->ctx->stream, true);
+    if (st == VG_OK && acc->lighting)
+        st = alloc(acc->light, px * LIGHTING_STRIDE * 4, r->ctx->stream, true);
+    if (st == VG_OK) {
+        cudaError_t e = cudaStreamSynchronize(r->ctx->stream);
+        if (e != cudaSuccess)
+            st = cuda_fail(e, "accumulation clear");
+    }
+    if (st != VG_OK) {
+        delete acc;
+        return st;
+    }
+    *out = acc;
+    return VG_OK;
+}
+
+void vg_accum_destroy(VgAccum* acc)
+{
+    if (!acc)
+        return;
+    if (acc->owner)
+        cudaStreamSynchronize(acc->owner->ctx->stream);
+    delete acc;
+}
+
+int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
+{
+    if (!r || !acc || acc->owner != r)
+        return fail(VG_ERR_INVALID, "accumulation does not belong to this renderer");
+    cudaStream_t s = r->ctx->stream;
+    size_t px = (size_t)acc->width * acc->height;
+    size_t es = acc->precision == 64 ? 8 : 4;
+    int st;
+    // Adaptive sampling: the statistics must count every sample from the first one on.
+    if (acc->samples == 0) {
+        acc->adaptive_fixed = true;
+        acc->adaptive = r->adaptive;
+    }
+    if (acc->adaptive && !acc->stats.p) {
+        if ((st = alloc(acc->stats, px * 3 * es, s, true)) != VG_OK)
+            return st;
+    }
+    if (acc->adaptive != r->adaptive)
+        return fail(VG_ERR_SCENE, "adaptive sampling was switched mid-accumulation; start a new accumulation");
+    if (acc->samples == 0) {
+        acc->restir = r->restir;
+        for (int h = 0; h < 2; h++) {
+            acc->re_g[h].release();
+            acc->re_n[h].release();
+            acc->re_x[h].release();
+            acc->re_m[h].release();
+        }
+        acc->restir_bytes = 0;
+        if (r->restir.on) {
+            for (int h = 0; h < 2; h++) {
+                if ((st = alloc(acc->re_g[h], px * 16, s, true)) != VG_OK ||
+                    (st = alloc(acc->re_n[h], px * 16, s, true)) != VG_OK ||
+                    (st = alloc(acc->re_x[h], px * 16, s, true)) != VG_OK ||
+                    (st = alloc(acc->re_m[h], px * 4, s, true)) != VG_OK)
+                    return st;
+            }
+            acc->restir_bytes = px * 2 * (16 * 3 + 4);
+        }
+    }
+    if (!(acc->restir == r->restir))
+        return fail(VG_ERR_SCENE, "ReSTIR was switched mid-accumulation; start a new accumulation");
+    bool wavefront = r->integrator == VG_WAVEFRONT;
+    const uint32_t max_depth_alloc = 64;
+    if (wavefront && !acc->state.p) {
+        uint32_t planes = vgk::BASE_PLANES + (acc->lighting ? vgk::SPLIT_PLANES : 0);
+        if ((st = alloc(acc->state, px * planes * 16, s, false)) != VG_OK ||
+            (st = alloc(acc->hits, px * 16, s, false)) != VG_OK ||
+            (st = alloc(acc->queue[0], px * 4, s, false)) != VG_OK ||
+            (st = alloc(acc->queue[1], px * 4, s, false)) != VG_OK ||
+            (st = alloc(acc->counts, (max_depth_alloc + 1) * 4, s, true)) != VG_OK ||
+            (st = alloc(acc->fetch, 2 * (max_depth_alloc + 1) * 4, s, true)) != VG_OK)
+            return st;
+        acc->wavefront_bytes = acc->state.bytes + acc->hits.bytes + acc->queue[0].bytes + acc->queue[1].bytes +
+                               acc->counts.bytes + acc->fetch.bytes;
+    }
+    vgd::Ctx c = make_ctx(r, acc);
+    vgx::Variant v = variant_of(r, acc);
+    EventPool pool;
+    cudaEvent_t t0 = pool.get(), t1 = pool.get();
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> stages;
+    bool timed = r->stage_timing && wavefront;
+    VG_CHECK(cudaMemsetAsync(r->err.p, 0, 4, s), "error flag");
+    VG_CHECK(cudaEventRecord(t0, s), "event");
+    if (!wavefront) {
+        dim3 grid((acc->width + 15) / 16, (acc->height + 7) / 8);
+        uint32_t k = 0;
+        while (k < samples) {
+            c.p[P_SAMPLE] = acc->samples + k;
+            c.p[P_SAMPLES_PER_DISPATCH] = std::min<uint32_t>(samples - k, acc->restir.on ? 1u : 8u);
+            k += c.p[P_SAMPLES_PER_DISPATCH];
+            VG_CHECK(vgx::launch_megakernel(v, grid, s, c), "megakernel launch");
+            acc->launches++;
+        }
+    } else {
+        vgk::Wave w;
+        uint32_t planes = vgk::BASE_PLANES + (acc->lighting ? vgk::SPLIT_PLANES : 0);
+        (void)planes;
+        w.state = (float4*)acc->state.p;
+        w.hits = (uint4*)acc->hits.p;
+        w.queue[0] = (uint32_t*)acc->queue[0].p;
+        w.queue[1] = (uint32_t*)acc->queue[1].p;
+        w.counts = (uint32_t*)acc->counts.p;
+        w.fetch = (uint32_t*)acc->fetch.p;
+        w.n = (uint32_t)px;
+        w.depth = r->max_depth;
+        c.p[P_WF_PATHS] = (uint32_t)px;
+        int vi = v.index();
+        if (r->shade_blocks[vi] == 0)
+            r->shade_blocks[vi] = vgx::wf_shade_blocks_per_sm(v);
+        int eb = blocks_for(r, r->extend_blocks);
+        int sb = blocks_for(r, r->shade_blocks[vi]);
+        for (uint32_t k = 0; k < samples; k++) {
+            c.p[P_SAMPLE] = acc->samples + k;
+            VG_CHECK(vgx::launch_wf_begin(s, c, w), "wf_begin launch");
+            acc->launches++;
+            if (acc->adaptive) {
+                VG_CHECK(vgx::launch_wf_select(v.f64, s, c, w), "wf_select launch");
+                acc->launches++;
+            }
+            for (uint32_t d = 0; d < r->max_depth; d++) {
+                c.p[P_WF_DEPTH] = d;
+                cudaEvent_t a = nullptr, b = nullptr, m = nullptr;
+                if (timed) {
+                    a = pool.get();
+                    m = pool.get();
+                    b = pool.get();
+                    VG_CHECK(cudaEventRecord(a, s), "event");
+                }
+                VG_CHECK(vgx::launch_wf_extend(eb, s, c, w, d), "wf_extend launch");
+                if (timed)
+                    VG_CHECK(cudaEventRecord(m, s), "event");
+                VG_CHECK(vgx::launch_wf_shade(v, sb, s, c, w, d), "wf_shade launch");
+                if (timed) {
+                    VG_CHECK(cudaEventRecord(b, s), "event");
+                    stages.push_back({0, {a, m}});
+                    stages.push_back({1, {m, b}});
+                }
+                acc->launches += 2;
+            }
+        }
+    }
+    VG_CHECK(cudaEventRecord(t1, s), "event");
+    st = wait_event(t1);
+    if (st != VG_OK)
+        return st;
+    float ms = 0.0f;
+    VG_CHECK(cudaEventElapsedTime(&ms, t0, t1), "event");
+    acc->gpu_seconds += ms * 1e-3;
+    if (timed) {
+        acc->stage_ran = true;
+        for (auto& sp : stages) {
+            float sm = 0.0f;
+            VG_CHECK(cudaEventElapsedTime(&sm, sp.second.first, sp.second.second), "event");
+            acc->stage_seconds[sp.first] += sm * 1e-3;
+            if (sp.first == 0)
+                acc->extend_launches_timed++;
+        }
+    }
+    st = read_err(r);
+    if (st != VG_OK)
+        return st;
+    if (wavefront && samples > 0)
+        acc->last_depth = r->max_depth;
+    acc->samples += samples;
+    return VG_OK;
+}
+
+uint32_t vg_accum_samples(const VgAccum* acc) { return acc ? acc->samples : 0; }
+double vg_accum_gpu_seconds(const VgAccum* acc) { return acc ? acc->gpu_seconds : 0.0; }
+
+int vg_accum_stage_seconds(const VgAccum* acc, double out[2])
+{
+    if (!acc || !acc->stage_ran)
+        return 0;
+    out[0] = acc->stage_seconds[0];
+    out[1] = acc->stage_seconds[1];
+    return 1;
+}
+
+size_t vg_accum_wavefront_bytes(const VgAccum* acc) { return acc ? acc->wavefront_bytes : 0; }
+size_t vg_accum_restir_bytes(const VgAccum* acc) { return acc ? acc->restir_bytes : 0; }
+int vg_accum_precision(const VgAccum* acc) { return acc ? acc->precision : 0; }
+uint64_t vg_accum_launches(const VgAccum* acc) { return acc ? acc->launches : 0; }
+
+double vg_accum_extend_launch_seconds(const VgAccum* acc)
+{
+    if (!acc || acc->extend_launches_timed == 0)
+        return 0.0;
+    return acc->stage_seconds[0] / (double)acc->extend_launches_timed;
+}
+
+static int read_dev(const VgAccum* acc, const DevBuf& b, void* out, size_t bytes)
+{
+    cudaStream_t s = acc->owner->ctx->stream;
+    VG_CHECK(cudaMemcpyAsync(out, b.p, bytes, cudaMemcpyDeviceToHost, s), "readback");
+    VG_CHECK(cudaStreamSynchronize(s), "readback");
+    return VG_OK;
+}
+
+int vg_accum_read_sums(const VgAccum* acc, float* out, size_t len)
+{
+    if (!acc || !out)
+        return fail(VG_ERR_INVALID, "null argument");
+    size_t n = (size_t)acc->width * acc->height * 3;
+    if (len < n)
+        return fail(VG_ERR_INVALID, "output too short");
+    if (acc->precision == 32)
+        return read_dev(acc, acc->accum, out, n * 4);
+    std::vector<double> tmp(n);
+    int st = read_dev(acc, acc->accum, tmp.data(), n * 8);
+    if (st != VG_OK)
+        return st;
+    for (size_t i = 0; i < n; i++)
+        out[i] = (float)tmp[i];
+    return VG_OK;
+}
+
+int vg_accum_read_sums_f64(const VgAccum* acc, double* out, size_t len)
+{
+    if (!acc || !out)
+        return fail(VG_ERR_INVALID, "null argument");
+    size_t n = (size_t)acc->width * acc->height * 3;
+    if (len < n)
+        return fail(VG_ERR_INVALID, "output too short");
+    if (acc->precision == 64)
+        return read_dev(acc, acc->accum, out, n * 8);
+    std::vector<float> tmp(n);
+    int st = read_dev(acc, acc->accum, tmp.data(), n * 4);
+    if (st != VG_OK)
+        return st;
+    for (size_t i = 0; i < n; i++)
+        out[i] = tmp[i];
+    return VG_OK;
+}
+
+int vg_accum_read_lighting(const VgAccum* acc, float* out, size_t len)
+{
+    if (!acc || !out)
+        return fail(VG_ERR_INVALID, "null argument");
+    if (!acc->lighting)
+        return fail(VG_ERR_INVALID, "accumulation has no lighting split");
+    size_t n = (size_t)acc->width * acc->height * LIGHTING_STRIDE;
+    if (len < n)
+        return fail(VG_ERR_INVALID, "output too short");
+    return read_dev(acc, acc->light, out, n * 4);
+}
+
+int vg_accum_read_stats(const VgAccum* acc, float* out, size_t len)
+{
+    if (!acc || !out)
+        return fail(VG_ERR_INVALID, "null argument");
+    if (!acc->stats.p)
+        return fail(VG_ERR_INVALID, "adaptive sampling never ran on this accumulation");
+    size_t n = (size_t)acc->width * acc->height * 3;
+    if (len < n)
+        return fail(VG_ERR_INVALID, "output too short");
+    if (acc->precision == 32)
+        return read_dev(acc, acc->stats, out, n * 4);
+    std::vector<double> tmp(n);
+    int st = read_dev(acc, acc->stats, tmp.data(), n * 8);
+    if (st != VG_OK)
+        return st;
+    for (size_t i = 0; i < n; i++)
+        out[i] = (float)tmp[i];
+    return VG_OK;
+}
+
+int vg_accum_read_queue_counts(const VgAccum* acc, uint32_t* out, size_t len)
+{
+    if (!acc || !out)
+        return fail(VG_ERR_INVALID, "null argument");
+    if (!acc->counts.p || acc->samples == 0 || acc->last_depth == 0)
+        return fail(VG_ERR_INVALID, "no wavefront sample has run on this accumulation");
+    if (len < acc->last_depth + 1)
+        return fail(VG_ERR_INVALID, "output too short");
+    return read_dev(acc, acc->counts, out, (acc->last_depth + 1) * 4);
+}
+
+int vg_trace_closest_device(VgRenderer* r, const float* d_rays, size_t n, uint32_t* d_hits, double* seconds)
+{
+    if (!r || (n > 0 && (!d_rays || !d_hits)))
+        return fail(VG_ERR_INVALID, "null argument");
+    if (n > 0xffffffffull)
+        return fail(VG_ERR_INVALID, "too many rays");
+    cudaStream_t s = r->ctx->stream;
+    int st = VG_OK;
+    if (!r->scratch.p && (st = alloc(r->scratch, 256, s, false)) != VG_OK)
+        return st;
+    vgd::Ctx c = make_ctx(r, nullptr);
+    EventPool pool;
+    cudaEvent_t a = pool.get(), b = pool.get();
+    VG_CHECK(cudaMemsetAsync(r->err.p, 0, 4, s), "error flag");
+    VG_CHECK(cudaMemsetAsync(r->scratch.p, 0, 4, s), "fetch counter");
+    VG_CHECK(cudaEventRecord(a, s), "event");
+    if (n > 0)
+        VG_CHECK(vgx::launch_trace_rays(blocks_for(r, r->extend_blocks), s, c, d_rays, (uint4*)d_hits, (uint32_t)n,
+                                        (uint32_t*)r->scratch.p),
+                 "trace launch");
+    VG_CHECK(cudaEventRecord(b, s), "event");
+    if ((st = wait_event(b)) != VG_OK)
+        return st;
+    float ms = 0.0f;
+    VG_CHECK(cudaEventElapsedTime(&ms, a, b), "event");
+    if (seconds)
+        *seconds = ms * 1e-3;
+    return read_err(r);
+}
+
+int vg_trace_closest(VgRenderer* r, const float* rays, size_t n, uint32_t* hits)
+{
+    if (!r || (n > 0 && (!rays || !hits)))
+        return fail(VG_ERR_INVALID, "null argument");
+    DevBuf dr, dh;
+    cudaStream_t s = r->ctx->stream;
+    int st;
+    if ((st = alloc(dr, n * 24, s, false)) != VG_OK || (st = alloc(dh, n * 16, s, false)) != VG_OK)
+        return st;
+    if (n > 0)
+        VG_CHECK(cudaMemcpyAsync(dr.p, rays, n * 24, cudaMemcpyHostToDevice, s), "ray upload");
+    if ((st = vg_trace_closest_device(r, (const float*)dr.p, n, (uint32_t*)dh.p, nullptr)) != VG_OK)
+        return st;
+    if (n > 0) {
+        VG_CHECK(cudaMemcpyAsync(hits, dh.p, n * 16, cudaMemcpyDeviceToHost, s), "hit readback");
+        VG_CHECK(cudaStreamSynchronize(s), "hit readback");
+    }
+    return VG_OK;
+}
+
+int vg_trace_occluded(VgRenderer* r, const float* rays, size_t n, uint32_t* out)
+{
+    if (!r || (n > 0 && (!rays || !out)))
+        return fail(VG_ERR_INVALID, "null argument");
+    if (n > 0xffffffffull)
+        return fail(VG_ERR_INVALID, "too many rays");
+    DevBuf dr, dh;
+    cudaStream_t s = r->ctx->stream;
+    int st;
+    if ((st = alloc(dr, n * 28, s, false)) != VG_OK || (st = alloc(dh, n * 4, s, false)) != VG_OK)
+        return st;
+    vgd::Ctx c = make_ctx(r, nullptr);
+    VG_CHECK(cudaMemsetAsync(r->err.p, 0, 4, s), "error flag");
+    if (n > 0) {
+        VG_CHECK(cudaMemcpyAsync(dr.p, rays, n * 28, cudaMemcpyHostToDevice, s), "ray upload");
+        VG_CHECK(vgx::launch_occlusion_rays(s, c, (const float*)dr.p, (uint32_t*)dh.p, (uint32_t)n), "occlusion launch");
+        VG_CHECK(cudaMemcpyAsync(out, dh.p, n * 4, cudaMemcpyDeviceToHost, s), "readback");
+    }
+    VG_CHECK(cudaStreamSynchronize(s), "occlusion");
+    return read_err(r);
+}
+
+} // extern "C"
