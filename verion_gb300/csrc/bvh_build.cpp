@@ -436,5 +436,31 @@ bool build_bvh8(const float* verts, const uint32_t* inst, const uint32_t* prim, 
         err = "BVH deeper than the traversal stack allows";
         return false;
     }
+    // Every index the traversal follows must stay inside the tables it reads.
+    for (uint32_t i = 0; i < wide_count; i++) {
+        const uint32_t* w = &out.nodes[(size_t)i * bvh8::NODE_WORDS];
+        uint32_t imask = w[3] >> 24;
+        uint8_t meta[8];
+        memcpy(meta, &w[6], 8);
+        uint32_t inner = (uint32_t)__builtin_popcount(imask);
+        if (inner > 0 && (w[4] == 0 || (uint64_t)w[4] + inner > wide_count)) {
+            err = "BVH child index out of range";
+            return false;
+        }
+        for (int s = 0; s < 8; s++) {
+            if ((imask >> s) & 1u) {
+                if (meta[s] != 0) {
+                    err = "BVH internal slot with leaf data";
+                    return false;
+                }
+                continue;
+            }
+            uint32_t cnt = meta[s] >> 5, off = meta[s] & 31u;
+            if (cnt > bvh8::MAX_LEAF_TRIS || (uint64_t)w[5] + off + cnt > tri_count) {
+                err = "BVH triangle range out of range";
+                return false;
+            }
+        }
+    }
     return true;
 }
