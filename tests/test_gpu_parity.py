@@ -71,7 +71,7 @@ def test_trace_closest_cornell_matches_oracle(gpu_ctx):
     rays = random_rays(200_000, 1, spread=1.2)
     got = r.trace_closest(rays)
     assert_same(got, o.trace_closest(rays, brute=True), "closest hits vs brute force")
-    assert got[:, 0].mean() > 0.9
+    assert got[:, 0].mean() > 0.5
 
 
 def test_trace_closest_many_spheres_matches_oracle(gpu_ctx):

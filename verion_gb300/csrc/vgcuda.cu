@@ -600,9 +600,7 @@ int vg_renderer_create(VgContext* ctx, const VgPacked* pk, VgRenderer** out)
 
 void vg_renderer_destroy(VgRenderer* r)
 {
-    if (!r)
-        return;
-    cudaStreamSynchronize(r->ctx->stream);
+    // As vg_accum_destroy: frees device memory only, independent of the context's lifetime.
     delete r;
 }
 
@@ -723,10 +721,8 @@ int vg_accum_create(VgRenderer* r, uint32_t width, uint32_t height, int lighting
 
 void vg_accum_destroy(VgAccum* acc)
 {
-    if (!acc)
-        return;
-    if (acc->owner)
-        cudaStreamSynchronize(acc->owner->ctx->stream);
+    // Frees device memory only (cudaFree waits for work in flight); it does not touch the
+    // renderer or context, so handles may be destroyed in any order.
     delete acc;
 }
 
