@@ -1,0 +1,404 @@
+"""Benchmark of the CUDA path-tracing backend on the 1M-triangle wavefront workload.
+
+Workload (configs[1] of the benchmark plan): 64 subdivided spheres on a noise-displaced 512 x 512 grid
+(1,014,274 triangles; GGX conductor / dielectric / Lambertian materials), a 2048 x 1024 float HDRI,
+1920 x 1080, max depth 16, wavefront integrator with adaptive sampling (threshold 0.02, 16 minimum
+samples), double-precision sums. All inputs are generated from seeds (`data: synthetic`).
+
+One step = `accumulate(acc, 8)`: eight samples per pixel of the running render (the reference
+session's 8-sample chunk, crates/verion-render/src/session.rs:244-248). `value` is camera paths
+traced per second (Mpaths/s), counted exactly from the adaptive sample counts, over the device time
+of the timed steps (CUDA events on the backend's stream); L2 is flushed (a 256 MiB write) between
+steps. `e2e` is the same metric through the C ABI with host buffers: each step sets the camera
+(host to device) and reads the pixel sums into pinned host memory (device to host), timed on the
+host clock.
+
+`--impl reference` times the CPU restatement of the reference's integrator (the oracle) on the host
+cores instead: the reference itself (Rust + Slang on Metal / Vulkan hardware ray tracing) cannot run
+on this machine.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WIDTH, HEIGHT, DEPTH, SPP_STEP = 1920, 1080, 16, 8
+ADAPTIVE = (0.02, 16)
+METRIC = "Mpaths/s (camera paths traced per second), 1M-triangle scene, 1920x1080, depth 16"
+UNIT = "Mpaths/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["cuda", "reference"], default="cuda")
+    ap.add_argument("--integrator", choices=["wavefront", "megakernel"], default="wavefront")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload():
+    from verion_gb300 import pack, scenes
+
+    s = scenes.many_spheres()
+    return s, pack.pack(s)
+
+
+def config(args, extra=None):
+    c = {"workload": "many_spheres_1M_tris_hdri2048", "triangles": 1_014_274, "width": WIDTH, "height": HEIGHT,
+         "max_depth": DEPTH, "spp_per_step": SPP_STEP, "integrator": args.integrator,
+         "adaptive": {"threshold": ADAPTIVE[0], "min_spp": ADAPTIVE[1]}, "sums": "f64",
+         "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{args.gpus}"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if args.impl == "cuda" else "gloo"
+        dist.init_process_group(backend)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allmax(world, v: float) -> float:
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(world, v: float) -> float:
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self._p = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                        "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except FileNotFoundError:
+            self._p = None
+        return self
+
+    def _read(self):
+        for line in self._p.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self._p:
+            self._p.terminate()
+            try:
+                self._p.wait(timeout=5)
+            except Exception:
+                self._p.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[4 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_ray():
+    """DRAM bytes per extend ray from the committed ncu summary of wf_extend, if present."""
+    p = ROOT / "profiles" / "wf_extend_traffic.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["dram_bytes_per_ray"]), d.get("source", str(p.name))
+    return None, None
+
+
+def cpu_baseline(packed, seconds: float, threads: int = 0):
+    """The oracle (single-precision restatement of the reference integrator) on a bounded row sample
+    of the same frame: 8 samples per pixel, every k-th row, all host threads."""
+    import oracle
+    from verion_gb300 import pack
+
+    o = oracle.OracleScene(packed)
+    threads = threads or oracle.default_threads()
+    prm = pack.base_params(packed.info, packed.view, (WIDTH, HEIGHT), False, True, max_depth=DEPTH)
+
+    def run(rows):
+        acc = oracle.OracleAccumulation(WIDTH, HEIGHT)
+        t0 = time.perf_counter()
+        oracle.render(o, prm, acc, SPP_STEP, threads=threads, rows=rows)
+        return time.perf_counter() - t0
+
+    probe_rows = list(range(0, HEIGHT, 135))[:8]
+    dt = run(probe_rows)
+    per_row = dt / len(probe_rows)
+    n = int(max(1, min(HEIGHT, seconds / max(per_row, 1e-6))))
+    step = max(1, HEIGHT // n)
+    rows = list(range(step // 2, HEIGHT, step))[:n]
+    dt = run(rows)
+    paths = len(rows) * WIDTH * SPP_STEP
+    return {"value": paths / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(rows)} of {HEIGHT} rows (every {step}th) x {WIDTH} px x {SPP_STEP} spp, "
+                      f"single-precision oracle, {dt:.1f} s"}, dt
+
+
+def run_reference(args):
+    rank, world = dist_init(args)
+    if rank != 0:
+        return 0
+    from verion_gb300 import pack
+    import oracle
+
+    _, packed = workload()
+    o = oracle.OracleScene(packed)
+    threads = oracle.default_threads()
+    prm = pack.base_params(packed.info, packed.view, (WIDTH, HEIGHT), False, True, max_depth=DEPTH)
+    # Each step: a bounded sample of the frame (every k-th row) at 8 spp, sized to ~2 s.
+    t0 = time.perf_counter()
+    acc = oracle.OracleAccumulation(WIDTH, HEIGHT)
+    oracle.render(o, prm, acc, SPP_STEP, threads=threads, rows=list(range(0, HEIGHT, 135))[:8])
+    per_row = (time.perf_counter() - t0) / 8
+    n = int(max(1, min(HEIGHT, 2.0 / max(per_row, 1e-6))))
+    stride = max(1, HEIGHT // n)
+    rows = list(range(stride // 2, HEIGHT, stride))[:n]
+    times = []
+    for k in range(args.warmup + args.steps):
+        acc = oracle.OracleAccumulation(WIDTH, HEIGHT)
+        t = time.perf_counter()
+        oracle.render(o, prm, acc, SPP_STEP, threads=threads, rows=rows)
+        if k >= args.warmup:
+            times.append(time.perf_counter() - t)
+    paths = len(rows) * WIDTH * SPP_STEP * len(times)
+    value = paths / sum(times) / 1e6
+    sample = f"{len(rows)} of {HEIGHT} rows (every {stride}th) x {WIDTH} px x {SPP_STEP} spp per step"
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config(args, {"sums": "f32", "integrator": "megakernel (CPU)"}), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_cuda(args):
+    rank, world = dist_init(args)
+    import torch
+
+    from verion_gb300 import build
+    from verion_gb300.backend import Context, Integrator, Renderer
+    from verion_gb300.readback import Adaptive
+
+    build.build()
+    _, packed = workload()
+    ctx = Context()
+    r = Renderer(ctx, packed)
+    r.set_integrator(Integrator.WAVEFRONT if args.integrator == "wavefront" else Integrator.MEGAKERNEL)
+    r.set_max_depth(DEPTH)
+    r.set_adaptive(Adaptive(*ADAPTIVE))
+    r.set_accum_precision(64)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    total = args.warmup + args.steps
+
+    def paths_of(acc):
+        st = acc.raw_stats()
+        return float(st.reshape(-1, 3)[:, 0].astype(np.float64).sum())
+
+    # Device-timed run.
+    r.set_stage_timing(False)
+    acc = r.new_accumulation(WIDTH, HEIGHT)
+    for _ in range(args.warmup):
+        flush.zero_()
+        torch.cuda.synchronize()
+        r.accumulate(acc, SPP_STEP)
+    p0 = paths_of(acc)
+    launches0 = acc.launches()
+    r.set_stage_timing(True)
+    step_times = []
+    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            barrier(world)
+            g0 = acc.gpu_seconds()
+            r.accumulate(acc, SPP_STEP)
+            torch.cuda.synchronize()
+            step_times.append(acc.gpu_seconds() - g0)
+        barrier(world)
+    paths = paths_of(acc) - p0
+    gpu_launches = acc.launches() - launches0
+    stage = acc.stage_seconds() or (0.0, 0.0)
+    extend_launch_s = acc.extend_launch_seconds()
+    t_local = sum(step_times)
+    t = allmax(world, t_local)
+    paths_all = allsum(world, paths)
+    value = paths_all / t / 1e6
+
+    # Traversal counters for the same steps (deterministic replay with counting on, untimed).
+    r.set_stage_timing(False)
+    r.set_traversal_stats(True)
+    acc_s = r.new_accumulation(WIDTH, HEIGHT)
+    for _ in range(args.warmup):
+        r.accumulate(acc_s, SPP_STEP)
+    s0 = acc_s.traversal_stats() if args.integrator == "wavefront" else None
+    for _ in range(args.steps):
+        r.accumulate(acc_s, SPP_STEP)
+    s1 = acc_s.traversal_stats() if args.integrator == "wavefront" else None
+    r.set_traversal_stats(False)
+    del acc_s
+
+    # End to end through the C ABI with host buffers.
+    pinned = torch.empty(3 * WIDTH * HEIGHT, dtype=torch.float32, pin_memory=True)
+    host_sums = pinned.numpy()
+    view = packed.view
+    acc_e = r.new_accumulation(WIDTH, HEIGHT)
+    for _ in range(args.warmup):
+        r.accumulate(acc_e, SPP_STEP)
+    pe0 = paths_of(acc_e)
+    wall = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r.set_camera(view)
+        r.accumulate(acc_e, SPP_STEP)
+        acc_e.sums(into=host_sums)
+        wall.append(time.perf_counter() - t0)
+    pe = paths_of(acc_e) - pe0
+    e2e_t = allmax(world, sum(wall))
+    e2e_value = allsum(world, pe) / e2e_t / 1e6
+    del acc_e
+
+    # Megakernel on the same steps, for comparison (device time).
+    mega = None
+    if args.integrator == "wavefront":
+        r.set_integrator(Integrator.MEGAKERNEL)
+        acc_m = r.new_accumulation(WIDTH, HEIGHT)
+        for _ in range(args.warmup):
+            r.accumulate(acc_m, SPP_STEP)
+        pm0 = paths_of(acc_m)
+        g0 = acc_m.gpu_seconds()
+        for _ in range(min(args.steps, 4)):
+            flush.zero_()
+            torch.cuda.synchronize()
+            r.accumulate(acc_m, SPP_STEP)
+        mega = (paths_of(acc_m) - pm0) / (acc_m.gpu_seconds() - g0) / 1e6
+        r.set_integrator(Integrator.WAVEFRONT)
+        del acc_m
+
+    roofline = None
+    peak, peak_kind = peaks()
+    if s0 is not None and extend_launch_s > 0:
+        rays = s1["rays"] - s0["rays"]
+        nodes = s1["nodes"] - s0["nodes"]
+        tests = s1["tests"] - s0["tests"]
+        rays1 = s1["rays_after_depth0"] - s0["rays_after_depth0"]
+        node_b, tri_b = 80, 48
+        alg_bytes = 20 * rays + 24 * rays1 + node_b * nodes + tri_b * tests
+        extend_launches = args.steps * SPP_STEP * DEPTH
+        per_launch_bytes = alg_bytes / extend_launches
+        achieved = per_launch_bytes / extend_launch_s / 1e9
+        tpr, tsrc = traffic_per_ray()
+        roofline = {"kernel": "wf_extend", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "peak_kind": f"{peak_kind} (hbm_gbs)",
+                    "traffic": (tpr * rays / extend_launches) if tpr else None,
+                    "traffic_source": tsrc,
+                    "algorithmic_bytes_per_launch": per_launch_bytes,
+                    "avg_launch_ms": extend_launch_s * 1e3,
+                    "per_ray": {"nodes": nodes / max(rays, 1), "triangle_tests": tests / max(rays, 1),
+                                "bytes": alg_bytes / max(rays, 1)},
+                    "formula": "20 B/ray (queue id + hit record) + 24 B/ray past depth 0 (origin, direction) "
+                               "+ 80 B/node visited + 48 B/triangle tested"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu, _ = cpu_baseline(packed, args.cpu_seconds)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": config(args), "impl": "cuda",
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 80,
+                        "d2h_bytes_per_step": 3 * 4 * WIDTH * HEIGHT},
+                "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": gpu_launches,
+                "clocks": clk.summary(),
+                "stage_seconds": {"extend": stage[0], "shade": stage[1]},
+                "paths_per_step": paths_all / args.steps,
+                "megakernel_value": mega}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_cuda(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -153,6 +153,9 @@ int vg_set_restir(VgRenderer* r, int on, int di, int gi, uint32_t candidates, ui
 /* Extensions with no reference counterpart. */
 /* Path length limit for accumulations (reference: the constant MAX_DEPTH = 8, pack.rs:13). */
 int vg_set_max_depth(VgRenderer* r, uint32_t depth);
+/* Wavefront only: count rays, BVH nodes visited and triangles tested in the extend stage of
+ * later accumulate calls (read with vg_accum_traversal_stats). */
+int vg_set_traversal_stats(VgRenderer* r, int on);
 /* Precision of the per-pixel sums of accumulations made afterwards: 32 (the reference's f32
  * sums) or 64 (double sums and double adaptive-sampling statistics, the default). */
 int vg_set_accum_precision(VgRenderer* r, int bits);
@@ -185,6 +188,9 @@ int vg_accum_read_stats(const VgAccum* acc, float* out, size_t len);
 /* Wavefront queue lengths of the last sample traced: live paths at depths 0..max depth
  * (max depth + 1 words; VG_ERR_INVALID before a wavefront accumulate). */
 int vg_accum_read_queue_counts(const VgAccum* acc, uint32_t* out, size_t len);
+/* Extend-stage counters since the accumulation began (with traversal stats on): rays, BVH nodes
+ * visited, triangles tested, rays past depth 0. */
+int vg_accum_traversal_stats(const VgAccum* acc, uint64_t out[4]);
 /* Kernel launches made by vg_accumulate on this accumulation so far. */
 uint64_t vg_accum_launches(const VgAccum* acc);
 /* Average duration in seconds of one extend-kernel launch, from stage timing (0 if none). */

@@ -113,6 +113,8 @@ def lib() -> C.CDLL:
             "vg_set_adaptive": (i32, [vp, i32, C.c_float, u32]),
             "vg_set_restir": (i32, [vp, i32, i32, i32, u32, u32]),
             "vg_set_max_depth": (i32, [vp, u32]),
+            "vg_set_traversal_stats": (i32, [vp, i32]),
+            "vg_accum_traversal_stats": (i32, [vp, C.POINTER(C.c_uint64)]),
             "vg_set_accum_precision": (i32, [vp, i32]),
             "vg_accum_create": (i32, [vp, u32, u32, i32, C.POINTER(vp)]),
             "vg_accum_destroy": (None, [vp]),
@@ -230,6 +232,11 @@ class Accumulation:
         out = np.empty(depth + 1, np.uint32)
         _check(lib().vg_accum_read_queue_counts(self._h, out.ctypes.data, out.size))
         return out
+
+    def traversal_stats(self) -> dict:
+        out = (C.c_uint64 * 4)()
+        _check(lib().vg_accum_traversal_stats(self._h, out))
+        return {"rays": out[0], "nodes": out[1], "tests": out[2], "rays_after_depth0": out[3]}
 
     def launches(self) -> int:
         return lib().vg_accum_launches(self._h)
@@ -368,6 +375,9 @@ class Renderer:
         _check(lib().vg_set_restir(self._h, int(r is not None), int(r.di) if r else 0, int(r.gi) if r else 0,
                                    r.candidates if r else 0, r.history if r else 0))
         self._restir = restir
+
+    def set_traversal_stats(self, on: bool) -> None:
+        _check(lib().vg_set_traversal_stats(self._h, int(on)))
 
     def set_max_depth(self, depth: int) -> None:
         _check(lib().vg_set_max_depth(self._h, depth))

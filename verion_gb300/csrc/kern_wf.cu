@@ -63,16 +63,20 @@ cudaError_t launch_wf_select(bool f64, cudaStream_t s, const vgd::Ctx& c, const 
     return cudaGetLastError();
 }
 
-cudaError_t launch_wf_extend(int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w, uint32_t d)
+cudaError_t launch_wf_extend(bool stats, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                             uint32_t d)
 {
-    vgk::wf_extend<<<blocks, 128, 0, s>>>(c, w, d);
+    if (stats)
+        vgk::wf_extend<true><<<blocks, 128, 0, s>>>(c, w, d);
+    else
+        vgk::wf_extend<false><<<blocks, 128, 0, s>>>(c, w, d);
     return cudaGetLastError();
 }
 
 int wf_extend_blocks_per_sm()
 {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, vgk::wf_extend, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, vgk::wf_extend<false>, 128, 0);
     return n > 0 ? n : 1;
 }
 

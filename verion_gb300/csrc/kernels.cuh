@@ -159,12 +159,25 @@ __global__ void __launch_bounds__(256) wf_select(const __grid_constant__ Ctx c, 
     warp_append(&w.counts[0], w.queue[0], active, p);
 }
 
-// wf_extend.slang:6-30: closest hit for every live path of depth d.
-static __global__ void __launch_bounds__(128) wf_extend(const __grid_constant__ Ctx c, Wave w, uint32_t d)
+// Sums a per-lane counter over the warp and adds it to a global 64-bit counter (lane 0).
+static __device__ __forceinline__ void warp_count(unsigned long long* dst, uint32_t v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(FULL, v, o);
+    if (lane_id() == 0 && v)
+        atomicAdd(dst, (unsigned long long)v);
+}
+
+// wf_extend.slang:6-30: closest hit for every live path of depth d. STATS also counts rays,
+// BVH nodes visited and triangles tested into w.tstats[0..2] (rays at depth > 0 into [3]).
+template <bool STATS>
+__global__ void __launch_bounds__(128) wf_extend(const __grid_constant__ Ctx c, Wave w, uint32_t d)
 {
     uint32_t count = w.counts[d];
     const uint32_t* qin = w.queue[d & 1u];
     bool direct = d == 0 && c.p[P_ADAPTIVE] == 0;
+    uint32_t n_rays = 0, n_nodes = 0, n_tests = 0;
     for (;;) {
         uint32_t base = warp_fetch(&w.fetch[d]);
         if (base >= count)
@@ -183,10 +196,23 @@ static __global__ void __launch_bounds__(128) wf_extend(const __grid_constant__ 
                 org = v3(a.x, a.y, a.z);
                 dir = v3(b.x, b.y, b.z);
             }
-            Hit h = traceClosest(c, org, dir);
-            w.hits[p] = make_uint4(h.hit ? 1u : 0u, h.inst, h.prim, __float_as_uint(h.t));
+            vgt::TRay r = vgt::make_ray(org, dir);
+            vgt::TraceHit q = vgt::trace_bvh<false>(c.s.nodes, c.s.tris, r, 1.0e30f, c.err);
+            w.hits[p] = make_uint4(q.hit ? 1u : 0u, q.hit ? q.inst : 0u, q.hit ? q.prim : 0u,
+                                   __float_as_uint(q.hit ? q.t : 0.0f));
+            if (STATS) {
+                n_rays++;
+                n_nodes += q.nodes;
+                n_tests += q.tests;
+            }
         }
         __syncwarp();
+    }
+    if (STATS) {
+        warp_count(&w.tstats[0], n_rays);
+        warp_count(&w.tstats[1], n_nodes);
+        warp_count(&w.tstats[2], n_tests);
+        warp_count(&w.tstats[3], d > 0 ? n_rays : 0u);
     }
 }
 

@@ -22,7 +22,7 @@ int wf_shade_blocks_per_sm(Variant v);
 
 cudaError_t launch_wf_begin(cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w);
 cudaError_t launch_wf_select(bool f64, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w);
-cudaError_t launch_wf_extend(int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w, uint32_t d);
+cudaError_t launch_wf_extend(bool stats, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w, uint32_t d);
 int wf_extend_blocks_per_sm();
 cudaError_t launch_trace_rays(int blocks, cudaStream_t s, const vgd::Ctx& c, const float* rays, uint4* out, uint32_t n,
                               uint32_t* fetch);

@@ -108,7 +108,8 @@ struct TraceHit {
     bool hit;
     uint32_t inst, prim, gid;
     float t;
-    float b1, b2; // barycentric weights of vertices 1 and 2
+    float b1, b2;           // barycentric weights of vertices 1 and 2
+    uint32_t nodes, tests;  // nodes visited and triangles tested (dropped by the compiler unless read)
 };
 
 __device__ __forceinline__ uint32_t byte_of(uint32_t lo, uint32_t hi, int i)
@@ -128,12 +129,14 @@ __device__ __forceinline__ TraceHit trace_bvh(const uint4* __restrict__ nodes, c
     h.gid = 0xffffffffu;
     h.t = tmax;
     h.b1 = h.b2 = 0.0f;
+    h.nodes = h.tests = 0;
     float best_t = tmax;
     uint2 stack[bvh8::STACK_SIZE];
     int sp = 0;
     uint32_t node = 0;
     for (;;) {
         const uint4* np = nodes + (size_t)node * bvh8::NODE_VEC4;
+        h.nodes++;
         uint4 w0 = __ldg(np);
         uint4 w1 = __ldg(np + 1);
         uint4 w2 = __ldg(np + 2);
@@ -183,6 +186,7 @@ __device__ __forceinline__ TraceHit trace_bvh(const uint4* __restrict__ nodes, c
             const float4* tp = tris + (size_t)(tri_base + j) * bvh8::TRI_VEC4;
             float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
             float t, U, V, W, det;
+            h.tests++;
             if (tri_test(r, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), t, U, V, W, det)) {
                 uint32_t gid = __float_as_uint(c.w);
                 bool take = ANY ? t < tmax : (t < best_t || (h.hit && t == best_t && gid < h.gid));

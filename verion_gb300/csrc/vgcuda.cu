@@ -136,6 +136,7 @@ struct VgRenderer {
     bool multiscatter = true;
     int integrator = VG_MEGAKERNEL;
     bool stage_timing = false;
+    bool traversal_stats = false;
     bool adaptive = false;
     float adaptive_threshold = 0.02f;
     uint32_t adaptive_min_spp = 16;
@@ -162,7 +163,7 @@ struct VgAccum {
     bool adaptive = false;
     Restir restir;               // captured at the first sample
     DevBuf re_g[2], re_n[2], re_x[2], re_m[2];
-    DevBuf state, hits, queue[2], counts, fetch;
+    DevBuf state, hits, queue[2], counts, fetch, tstats;
     size_t wavefront_bytes = 0;
     size_t restir_bytes = 0;
     uint32_t last_depth = 0; // max depth of the last wavefront sample
@@ -646,6 +647,14 @@ int vg_set_stage_timing(VgRenderer* r, int on)
     return VG_OK;
 }
 
+int vg_set_traversal_stats(VgRenderer* r, int on)
+{
+    if (!r)
+        return fail(VG_ERR_INVALID, "null renderer");
+    r->traversal_stats = on != 0;
+    return VG_OK;
+}
+
 int vg_set_adaptive(VgRenderer* r, int on, float threshold, uint32_t min_spp)
 {
     if (!r)
@@ -776,7 +785,8 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
             (st = alloc(acc->queue[0], px * 4, s, false)) != VG_OK ||
             (st = alloc(acc->queue[1], px * 4, s, false)) != VG_OK ||
             (st = alloc(acc->counts, (max_depth_alloc + 1) * 4, s, true)) != VG_OK ||
-            (st = alloc(acc->fetch, 2 * (max_depth_alloc + 1) * 4, s, true)) != VG_OK)
+            (st = alloc(acc->fetch, 2 * (max_depth_alloc + 1) * 4, s, true)) != VG_OK ||
+            (st = alloc(acc->tstats, 4 * 8, s, true)) != VG_OK)
             return st;
         acc->wavefront_bytes = acc->state.bytes + acc->hits.bytes + acc->queue[0].bytes + acc->queue[1].bytes +
                                acc->counts.bytes + acc->fetch.bytes;
@@ -809,6 +819,7 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
         w.queue[1] = (uint32_t*)acc->queue[1].p;
         w.counts = (uint32_t*)acc->counts.p;
         w.fetch = (uint32_t*)acc->fetch.p;
+        w.tstats = (unsigned long long*)acc->tstats.p;
         w.n = (uint32_t)px;
         w.depth = r->max_depth;
         c.p[P_WF_PATHS] = (uint32_t)px;
@@ -834,7 +845,7 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
                     b = pool.get();
                     VG_CHECK(cudaEventRecord(a, s), "event");
                 }
-                VG_CHECK(vgx::launch_wf_extend(eb, s, c, w, d), "wf_extend launch");
+                VG_CHECK(vgx::launch_wf_extend(r->traversal_stats, eb, s, c, w, d), "wf_extend launch");
                 if (timed)
                     VG_CHECK(cudaEventRecord(m, s), "event");
                 VG_CHECK(vgx::launch_wf_shade(v, sb, s, c, w, d), "wf_shade launch");
@@ -971,6 +982,15 @@ int vg_accum_read_stats(const VgAccum* acc, float* out, size_t len)
     for (size_t i = 0; i < n; i++)
         out[i] = (float)tmp[i];
     return VG_OK;
+}
+
+int vg_accum_traversal_stats(const VgAccum* acc, uint64_t out[4])
+{
+    if (!acc || !out)
+        return fail(VG_ERR_INVALID, "null argument");
+    if (!acc->tstats.p)
+        return fail(VG_ERR_INVALID, "no wavefront sample has run on this accumulation");
+    return read_dev(acc, acc->tstats, out, 4 * 8);
 }
 
 int vg_accum_read_queue_counts(const VgAccum* acc, uint32_t* out, size_t len)
