@@ -41,6 +41,7 @@ UNIT = "Mpaths/s"
 
 
 def parse():
+    global WIDTH, HEIGHT
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=8)
@@ -49,7 +50,11 @@ def parse():
     ap.add_argument("--integrator", choices=["wavefront", "megakernel"], default="wavefront")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    ap.add_argument("--width", type=int, default=WIDTH, help="smaller frames are for profiling runs only")
+    ap.add_argument("--height", type=int, default=HEIGHT)
+    a = ap.parse_args()
+    WIDTH, HEIGHT = a.width, a.height
+    return a
 
 
 def workload():
@@ -182,22 +187,23 @@ def cpu_baseline(packed, seconds: float, threads: int = 0):
     threads = threads or oracle.default_threads()
     prm = pack.base_params(packed.info, packed.view, (WIDTH, HEIGHT), False, True, max_depth=DEPTH)
 
-    def run(rows):
+    def run(rows, spp):
         acc = oracle.OracleAccumulation(WIDTH, HEIGHT)
         t0 = time.perf_counter()
-        oracle.render(o, prm, acc, SPP_STEP, threads=threads, rows=rows)
+        oracle.render(o, prm, acc, spp, threads=threads, rows=rows)
         return time.perf_counter() - t0
 
     probe_rows = list(range(0, HEIGHT, 135))[:8]
-    dt = run(probe_rows)
-    per_row = dt / len(probe_rows)
+    per_row = run(probe_rows, SPP_STEP) / len(probe_rows)
     n = int(max(1, min(HEIGHT, seconds / max(per_row, 1e-6))))
     step = max(1, HEIGHT // n)
     rows = list(range(step // 2, HEIGHT, step))[:n]
-    dt = run(rows)
-    paths = len(rows) * WIDTH * SPP_STEP
+    # When the whole frame is faster than the target, trace more samples per pixel.
+    spp = SPP_STEP * max(1, int(round(seconds / max(len(rows) * per_row, 1e-6)))) if n == HEIGHT else SPP_STEP
+    dt = run(rows, spp)
+    paths = len(rows) * WIDTH * spp
     return {"value": paths / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{len(rows)} of {HEIGHT} rows (every {step}th) x {WIDTH} px x {SPP_STEP} spp, "
+            "sample": f"{len(rows)} of {HEIGHT} rows (every {step}th) x {WIDTH} px x {spp} spp, "
                       f"single-precision oracle, {dt:.1f} s"}, dt
 
 
