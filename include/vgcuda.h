@@ -153,6 +153,15 @@ int vg_set_restir(VgRenderer* r, int on, int di, int gi, uint32_t candidates, ui
 /* Extensions with no reference counterpart. */
 /* Path length limit for accumulations (reference: the constant MAX_DEPTH = 8, pack.rs:13). */
 int vg_set_max_depth(VgRenderer* r, uint32_t depth);
+/* Wavefront scheduling. VG_WAVEFRONT_PER_SAMPLE is the reference's order: one sample at a time,
+ * one extend and one shade launch per depth, with per-depth queue counts readable afterwards.
+ * VG_WAVEFRONT_STREAMING (default) regenerates paths: each pixel's slot runs the call's samples
+ * back to back, so a launch covers every live path whatever its depth; per pixel the samples are
+ * still added in order, and the sums are identical. ReSTIR always runs per sample. */
+typedef enum VgWavefrontMode { VG_WAVEFRONT_PER_SAMPLE = 0, VG_WAVEFRONT_STREAMING = 1 } VgWavefrontMode;
+int vg_set_wavefront_mode(VgRenderer* r, int mode);
+/* Streaming mode: waves (extend + shade pairs) issued by the last vg_accumulate. */
+uint32_t vg_accum_last_waves(const VgAccum* acc);
 /* Wavefront only: count rays, BVH nodes visited and triangles tested in the extend stage of
  * later accumulate calls (read with vg_accum_traversal_stats). */
 int vg_set_traversal_stats(VgRenderer* r, int on);

@@ -13,7 +13,7 @@ import pytest
 import oracle
 from verion_gb300 import pack, scenes
 from verion_gb300 import scene as sc
-from verion_gb300.backend import Error, Integrator, Renderer
+from verion_gb300.backend import Error, Integrator, Renderer, WavefrontMode
 from verion_gb300.readback import Adaptive, Restir
 
 pytestmark = pytest.mark.gpu
@@ -32,10 +32,11 @@ def params(p, w, h, lighting=False, multiscatter=True, adaptive=None, restir=Non
 
 
 def gpu_render(ctx, p, w, h, spp, *, integrator=Integrator.MEGAKERNEL, precision=32, lighting=False,
-               adaptive=None, restir=None, depth=8, chunks=None):
+               adaptive=None, restir=None, depth=8, chunks=None, mode=WavefrontMode.STREAMING):
     r = Renderer(ctx, p)
     r.set_accum_precision(precision)
     r.set_integrator(integrator)
+    r.set_wavefront_mode(mode)
     r.set_max_depth(depth)
     r.set_adaptive(adaptive)
     r.set_restir(restir)
@@ -125,6 +126,7 @@ def test_cornell_wavefront_bit_exact_with_queue_counts(gpu_ctx):
     r = Renderer(gpu_ctx, p)
     r.set_accum_precision(32)
     r.set_integrator(Integrator.WAVEFRONT)
+    r.set_wavefront_mode(WavefrontMode.PER_SAMPLE)
     acc = r.new_accumulation(w, h)
     o = oracle.OracleScene(p)
     ref = oracle.OracleAccumulation(w, h)
@@ -219,3 +221,29 @@ def test_many_spheres_depth16_env_bit_exact(gpu_ctx):
     _, acc = gpu_render(gpu_ctx, p, w, h, 2, depth=16)
     ref = oracle_render(p, w, h, 2, depth=16)
     assert_same(acc.sums(), ref.sums, "1M-triangle scene, depth 16, environment map")
+
+
+@pytest.mark.parametrize("mode", [WavefrontMode.PER_SAMPLE, WavefrontMode.STREAMING])
+@pytest.mark.parametrize("adaptive", [None, Adaptive(threshold=0.05, min_spp=4)])
+def test_wavefront_modes_match_the_oracle(gpu_ctx, mode, adaptive):
+    s = scenes.many_spheres(hdri=(256, 128))
+    p = pack.pack(s)
+    w, h = 48, 27
+    _, acc = gpu_render(gpu_ctx, p, w, h, 12, integrator=Integrator.WAVEFRONT, depth=16, adaptive=adaptive,
+                        mode=mode, chunks=[5, 7])
+    ref = oracle_render(p, w, h, 12, depth=16, adaptive=adaptive)
+    assert_same(acc.sums(), ref.sums, f"{mode.name} wavefront sums")
+    if adaptive is not None:
+        assert_same(acc.raw_stats(), ref.stats, "adaptive statistics")
+    if mode == WavefrontMode.STREAMING:
+        assert 0 < acc.last_waves() <= 7 * 16 + 3
+
+
+def test_streaming_lighting_split_bit_exact(gpu_ctx):
+    s = scenes.cornell()
+    s.add_light(sc.Spot((0.0, 0.9, 0.0), (0.0, -1.0, 0.1), (1.0, 0.8, 0.6), 3.0, 0.3, 0.6))
+    p = pack.pack(s)
+    _, acc = gpu_render(gpu_ctx, p, 40, 30, 6, integrator=Integrator.WAVEFRONT, lighting=True, chunks=[2, 4])
+    ref = oracle_render(p, 40, 30, 6, lighting=True)
+    assert_same(acc.sums(), ref.sums, "sums")
+    assert_same(acc.raw_lighting(), ref.lighting, "lighting split")

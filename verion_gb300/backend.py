@@ -42,6 +42,13 @@ class Integrator(IntEnum):
     WAVEFRONT = 1
 
 
+class WavefrontMode(IntEnum):
+    """PER_SAMPLE: the reference's depth-by-depth order (per-depth queue counts readable).
+    STREAMING: path regeneration, the same sums with far fewer, fuller launches."""
+    PER_SAMPLE = 0
+    STREAMING = 1
+
+
 class MemoryUsage(C.Structure):
     _fields_ = [("budget", C.c_uint64), ("allocated", C.c_uint64), ("uploaded", C.c_uint64)]
 
@@ -114,6 +121,8 @@ def lib() -> C.CDLL:
             "vg_set_restir": (i32, [vp, i32, i32, i32, u32, u32]),
             "vg_set_max_depth": (i32, [vp, u32]),
             "vg_set_traversal_stats": (i32, [vp, i32]),
+            "vg_set_wavefront_mode": (i32, [vp, i32]),
+            "vg_accum_last_waves": (u32, [vp]),
             "vg_accum_traversal_stats": (i32, [vp, C.POINTER(C.c_uint64)]),
             "vg_set_accum_precision": (i32, [vp, i32]),
             "vg_accum_create": (i32, [vp, u32, u32, i32, C.POINTER(vp)]),
@@ -232,6 +241,9 @@ class Accumulation:
         out = np.empty(depth + 1, np.uint32)
         _check(lib().vg_accum_read_queue_counts(self._h, out.ctypes.data, out.size))
         return out
+
+    def last_waves(self) -> int:
+        return lib().vg_accum_last_waves(self._h)
 
     def traversal_stats(self) -> dict:
         out = (C.c_uint64 * 4)()
@@ -375,6 +387,9 @@ class Renderer:
         _check(lib().vg_set_restir(self._h, int(r is not None), int(r.di) if r else 0, int(r.gi) if r else 0,
                                    r.candidates if r else 0, r.history if r else 0))
         self._restir = restir
+
+    def set_wavefront_mode(self, mode: "WavefrontMode") -> None:
+        _check(lib().vg_set_wavefront_mode(self._h, int(mode)))
 
     def set_traversal_stats(self, on: bool) -> None:
         _check(lib().vg_set_traversal_stats(self._h, int(on)))

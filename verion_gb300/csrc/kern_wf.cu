@@ -94,3 +94,69 @@ cudaError_t launch_occlusion_rays(cudaStream_t s, const vgd::Ctx& c, const float
 }
 
 } // namespace vgx
+
+namespace vgx {
+
+template <bool L, typename A>
+static cudaError_t sshade(int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w, uint32_t wave)
+{
+    vgk::wf_stream_shade<L, A><<<blocks, 128, 0, s>>>(c, w, wave);
+    return cudaGetLastError();
+}
+
+template <bool L, typename A>
+static int sshade_occ()
+{
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, vgk::wf_stream_shade<L, A>, 128, 0);
+    return n > 0 ? n : 1;
+}
+
+cudaError_t launch_stream_start(Variant v, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w)
+{
+    unsigned blocks = (w.n + 255) / 256;
+    if (v.light && v.f64)
+        vgk::wf_stream_start<true, double><<<blocks, 256, 0, s>>>(c, w);
+    else if (v.light)
+        vgk::wf_stream_start<true, float><<<blocks, 256, 0, s>>>(c, w);
+    else if (v.f64)
+        vgk::wf_stream_start<false, double><<<blocks, 256, 0, s>>>(c, w);
+    else
+        vgk::wf_stream_start<false, float><<<blocks, 256, 0, s>>>(c, w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_extend(bool stats, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                                 uint32_t wave)
+{
+    if (stats)
+        vgk::wf_stream_extend<true><<<blocks, 128, 0, s>>>(c, w, wave);
+    else
+        vgk::wf_stream_extend<false><<<blocks, 128, 0, s>>>(c, w, wave);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_shade(Variant v, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                                uint32_t wave)
+{
+    if (v.light && v.f64)
+        return sshade<true, double>(blocks, s, c, w, wave);
+    if (v.light)
+        return sshade<true, float>(blocks, s, c, w, wave);
+    if (v.f64)
+        return sshade<false, double>(blocks, s, c, w, wave);
+    return sshade<false, float>(blocks, s, c, w, wave);
+}
+
+int stream_shade_blocks_per_sm(Variant v)
+{
+    if (v.light && v.f64)
+        return sshade_occ<true, double>();
+    if (v.light)
+        return sshade_occ<true, float>();
+    if (v.f64)
+        return sshade_occ<false, double>();
+    return sshade_occ<false, float>();
+}
+
+} // namespace vgx

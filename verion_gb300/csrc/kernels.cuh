@@ -252,6 +252,160 @@ __global__ void __launch_bounds__(128) wf_shade(const __grid_constant__ Ctx c, W
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Streaming wavefront (path regeneration). The reference's wavefront runs one sample at a time,
+// depth by depth (renderer/wavefront.rs:93-177): 2 x depth launches per sample, most of them on a
+// small tail of long paths. Here each pixel's slot runs the batch's params[35] samples back to
+// back: when its path ends, the same thread adds it to the pixel's sums and starts the pixel's next
+// sample in the same slot. A wave is one extend plus one shade over every live slot, whatever the
+// depth of its path. Per pixel the samples are still added in order, one at a time, and adaptive
+// sampling still decides before each sample from the statistics of the samples before it, so the
+// sums are those of the sample-by-sample loop, bit for bit.
+// Counters: queue lengths counts[wave & 1] (in) / counts[~wave & 1] (out), extend work counters
+// fetch[0..1], shade work counters fetch[2..3]; each kernel clears the ones the next kernel uses.
+
+// Path state as stored, for any depth (depth 0 included: it was stored when the sample started).
+template <bool LIGHT>
+__device__ __forceinline__ PathState<LIGHT> loadState(const Wave& w, uint32_t p)
+{
+    uint32_t n = w.n;
+    PathState<LIGHT> s;
+    float4 a = w.state[p], b = w.state[n + p], t = w.state[2 * n + p], r = w.state[3 * n + p];
+    s.org = v3(a.x, a.y, a.z);
+    s.rng = __float_as_uint(a.w);
+    s.dir = v3(b.x, b.y, b.z);
+    uint32_t flags = __float_as_uint(b.w);
+    s.thr = v3(t.x, t.y, t.z);
+    s.pathLen = t.w;
+    s.cls = flags & 3u;
+    s.chan = (int)((flags >> 2) & 3u) - 1;
+    s.misPrev = (flags & 16u) != 0;
+    s.restir = (flags & 32u) != 0;
+    s.gi = (flags & 64u) != 0;
+    s.prevInst = flags >> 8;
+    s.qPrev = r.w;
+    s.parts.zero();
+    s.parts.total = v3(r.x, r.y, r.z);
+    s.visLit = 0.0f;
+    s.visTotal = 0.0f;
+    if (LIGHT) {
+        float4 q4 = w.state[4 * n + p], q5 = w.state[5 * n + p], q6 = w.state[6 * n + p], q7 = w.state[7 * n + p],
+               q8 = w.state[8 * n + p];
+        s.parts.directDiffuse = v3(q4.x, q4.y, q4.z);
+        s.visLit = q4.w;
+        s.parts.indirectDiffuse = v3(q5.x, q5.y, q5.z);
+        s.visTotal = q5.w;
+        s.parts.specular = v3(q6.x, q6.y, q6.z);
+        s.parts.transmission = v3(q7.x, q7.y, q7.z);
+        s.parts.emission = v3(q8.x, q8.y, q8.z);
+    }
+    return s;
+}
+
+// Starts the batch: every pixel that takes a sample (wf_select's test) begins sample params[6].
+template <bool LIGHT, typename A>
+__global__ void __launch_bounds__(256) wf_stream_start(const __grid_constant__ Ctx c, Wave w)
+{
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = false;
+    if (p < w.n && c.p[P_SAMPLES_PER_DISPATCH] > 0 && (c.p[P_ADAPTIVE] == 0 || pixelActive<A>(c, p))) {
+        PathState<LIGHT> st = generatePathFor<LIGHT>(c, p % c.p[P_WIDTH], p / c.p[P_WIDTH], c.p[P_SAMPLE]);
+        storePath<LIGHT>(w, st, p);
+        w.meta[p] = 0;
+        live = true;
+    }
+    warp_append(&w.counts[0], w.queue[0], live, p);
+}
+
+template <bool STATS>
+__global__ void __launch_bounds__(128) wf_stream_extend(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
+{
+    uint32_t in = wave & 1u, out = in ^ 1u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        w.counts[out] = 0;
+        w.fetch[2 + in] = 0;
+    }
+    uint32_t count = w.counts[in];
+    const uint32_t* qin = w.queue[in];
+    uint32_t n_rays = 0, n_nodes = 0, n_tests = 0, n_later = 0;
+    for (;;) {
+        uint32_t base = warp_fetch(&w.fetch[in]);
+        if (base >= count)
+            break;
+        uint32_t i = base + lane_id();
+        if (i < count) {
+            uint32_t p = qin[i];
+            float4 a = w.state[p];
+            float4 b = w.state[w.n + p];
+            vgt::TRay r = vgt::make_ray(v3(a.x, a.y, a.z), v3(b.x, b.y, b.z));
+            vgt::TraceHit q = vgt::trace_bvh<false>(c.s.nodes, c.s.tris, r, 1.0e30f, c.err);
+            w.hits[p] = make_uint4(q.hit ? 1u : 0u, q.hit ? q.inst : 0u, q.hit ? q.prim : 0u,
+                                   __float_as_uint(q.hit ? q.t : 0.0f));
+            if (STATS) {
+                n_rays++;
+                n_nodes += q.nodes;
+                n_tests += q.tests;
+                n_later += (w.meta[p] & 0xffu) != 0 ? 1u : 0u;
+            }
+        }
+        __syncwarp();
+    }
+    if (STATS) {
+        warp_count(&w.tstats[0], n_rays);
+        warp_count(&w.tstats[1], n_nodes);
+        warp_count(&w.tstats[2], n_tests);
+        warp_count(&w.tstats[3], n_later);
+    }
+}
+
+template <bool LIGHT, typename A>
+__global__ void __launch_bounds__(128) wf_stream_shade(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
+{
+    uint32_t in = wave & 1u, out = in ^ 1u;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        w.fetch[out] = 0;
+    uint32_t count = w.counts[in];
+    const uint32_t* qin = w.queue[in];
+    uint32_t* qout = w.queue[out];
+    uint32_t batch = c.p[P_SAMPLES_PER_DISPATCH];
+    for (;;) {
+        uint32_t base = warp_fetch(&w.fetch[2 + in]);
+        if (base >= count)
+            break;
+        uint32_t i = base + lane_id();
+        bool live = false;
+        uint32_t p = 0;
+        if (i < count) {
+            p = qin[i];
+            uint32_t meta = w.meta[p];
+            uint32_t depth = meta & 0xffu, k = meta >> 8;
+            PathState<LIGHT> st = loadState<LIGHT>(w, p);
+            uint4 hr = w.hits[p];
+            Hit h;
+            h.hit = hr.x != 0;
+            h.inst = hr.y;
+            h.prim = hr.z;
+            h.t = __uint_as_float(hr.w);
+            if (shadePath<LIGHT, false>(c, st, h, depth, p) && depth + 1 < w.depth) {
+                storePath<LIGHT>(w, st, p);
+                w.meta[p] = (depth + 1) | (k << 8);
+                live = true;
+            } else {
+                finishPath<LIGHT, A>(c, st, p);
+                if (k + 1 < batch && (c.p[P_ADAPTIVE] == 0 || pixelActive<A>(c, p))) {
+                    PathState<LIGHT> nx =
+                        generatePathFor<LIGHT>(c, p % c.p[P_WIDTH], p / c.p[P_WIDTH], c.p[P_SAMPLE] + k + 1);
+                    storePath<LIGHT>(w, nx, p);
+                    w.meta[p] = (k + 1) << 8;
+                    live = true;
+                }
+            }
+        }
+        __syncwarp();
+        warp_append(&w.counts[out], qout, live, p);
+    }
+}
+
 // Closest hits of caller-given rays (6 floats each: origin, direction): the traversal alone, for
 // checking it against an independent implementation and for timing it.
 static __global__ void __launch_bounds__(128) trace_rays(const __grid_constant__ Ctx c, const float* rays, uint4* out,

@@ -24,6 +24,13 @@ cudaError_t launch_wf_begin(cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& 
 cudaError_t launch_wf_select(bool f64, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w);
 cudaError_t launch_wf_extend(bool stats, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w, uint32_t d);
 int wf_extend_blocks_per_sm();
+// Streaming wavefront (path regeneration); see kernels.cuh.
+cudaError_t launch_stream_start(Variant v, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w);
+cudaError_t launch_stream_extend(bool stats, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                                 uint32_t wave);
+cudaError_t launch_stream_shade(Variant v, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                                uint32_t wave);
+int stream_shade_blocks_per_sm(Variant v);
 cudaError_t launch_trace_rays(int blocks, cudaStream_t s, const vgd::Ctx& c, const float* rays, uint4* out, uint32_t n,
                               uint32_t* fetch);
 cudaError_t launch_occlusion_rays(cudaStream_t s, const vgd::Ctx& c, const float* rays, uint32_t* out, uint32_t n);

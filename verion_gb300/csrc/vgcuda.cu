@@ -137,6 +137,7 @@ struct VgRenderer {
     int integrator = VG_MEGAKERNEL;
     bool stage_timing = false;
     bool traversal_stats = false;
+    int wavefront_mode = VG_WAVEFRONT_STREAMING;
     bool adaptive = false;
     float adaptive_threshold = 0.02f;
     uint32_t adaptive_min_spp = 16;
@@ -145,6 +146,7 @@ struct VgRenderer {
     int precision = 64;
     int extend_blocks = 0;
     int shade_blocks[8] = {};
+    int stream_shade_blocks[8] = {};
 };
 
 struct VgAccum {
@@ -163,7 +165,14 @@ struct VgAccum {
     bool adaptive = false;
     Restir restir;               // captured at the first sample
     DevBuf re_g[2], re_n[2], re_x[2], re_m[2];
-    DevBuf state, hits, queue[2], counts, fetch, tstats;
+    DevBuf state, hits, queue[2], counts, fetch, tstats, meta;
+    uint32_t* host_counts = nullptr; // pinned ring of wave output counts (streaming wavefront)
+    uint32_t last_waves = 0;
+    ~VgAccum()
+    {
+        if (host_counts)
+            cudaFreeHost(host_counts);
+    }
     size_t wavefront_bytes = 0;
     size_t restir_bytes = 0;
     uint32_t last_depth = 0; // max depth of the last wavefront sample
@@ -647,6 +656,16 @@ int vg_set_stage_timing(VgRenderer* r, int on)
     return VG_OK;
 }
 
+int vg_set_wavefront_mode(VgRenderer* r, int mode)
+{
+    if (!r || (mode != VG_WAVEFRONT_PER_SAMPLE && mode != VG_WAVEFRONT_STREAMING))
+        return fail(VG_ERR_INVALID, "bad wavefront mode");
+    r->wavefront_mode = mode;
+    return VG_OK;
+}
+
+uint32_t vg_accum_last_waves(const VgAccum* acc) { return acc ? acc->last_waves : 0; }
+
 int vg_set_traversal_stats(VgRenderer* r, int on)
 {
     if (!r)
@@ -786,8 +805,13 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
             (st = alloc(acc->queue[1], px * 4, s, false)) != VG_OK ||
             (st = alloc(acc->counts, (max_depth_alloc + 1) * 4, s, true)) != VG_OK ||
             (st = alloc(acc->fetch, 2 * (max_depth_alloc + 1) * 4, s, true)) != VG_OK ||
-            (st = alloc(acc->tstats, 4 * 8, s, true)) != VG_OK)
+            (st = alloc(acc->tstats, 4 * 8, s, true)) != VG_OK ||
+            (st = alloc(acc->meta, px * 4, s, false)) != VG_OK)
             return st;
+        if (!acc->host_counts && cudaHostAlloc((void**)&acc->host_counts, 64 * 4, cudaHostAllocDefault) != cudaSuccess) {
+            acc->host_counts = nullptr;
+            return fail(VG_ERR_RESOURCE, "pinned host buffer");
+        }
         acc->wavefront_bytes = acc->state.bytes + acc->hits.bytes + acc->queue[0].bytes + acc->queue[1].bytes +
                                acc->counts.bytes + acc->fetch.bytes;
     }
@@ -799,6 +823,7 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
     bool timed = r->stage_timing && wavefront;
     VG_CHECK(cudaMemsetAsync(r->err.p, 0, 4, s), "error flag");
     VG_CHECK(cudaEventRecord(t0, s), "event");
+    bool streamed = false;
     if (!wavefront) {
         dim3 grid((acc->width + 15) / 16, (acc->height + 7) / 8);
         uint32_t k = 0;
@@ -828,7 +853,68 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
             r->shade_blocks[vi] = vgx::wf_shade_blocks_per_sm(v);
         int eb = blocks_for(r, r->extend_blocks);
         int sb = blocks_for(r, r->shade_blocks[vi]);
-        for (uint32_t k = 0; k < samples; k++) {
+        w.meta = (uint32_t*)acc->meta.p;
+        bool streaming = r->wavefront_mode == VG_WAVEFRONT_STREAMING && !acc->restir.on;
+        if (streaming && samples > 0) {
+            streamed = true;
+            int svi = v.index() & 5;
+            if (r->stream_shade_blocks[svi] == 0)
+                r->stream_shade_blocks[svi] = vgx::stream_shade_blocks_per_sm(v);
+            int ssb = blocks_for(r, r->stream_shade_blocks[svi]);
+            c.p[P_SAMPLE] = acc->samples;
+            c.p[P_SAMPLES_PER_DISPATCH] = samples;
+            VG_CHECK(cudaMemsetAsync(acc->counts.p, 0, 2 * 4, s), "counters");
+            VG_CHECK(cudaMemsetAsync(acc->fetch.p, 0, 4 * 4, s), "counters");
+            VG_CHECK(vgx::launch_stream_start(v, s, c, w), "stream start launch");
+            acc->launches++;
+            // Waves until no slot is live. The host reads each wave's output count LAG waves later,
+            // so the GPU never idles on the poll; extra waves on an empty queue exit at once.
+            const uint32_t LAG = 2, RING = 64;
+            uint64_t max_waves = (uint64_t)samples * r->max_depth + LAG + 1;
+            uint32_t* ring = acc->host_counts;
+            std::vector<cudaEvent_t> ring_ev(RING);
+            for (auto& e : ring_ev)
+                e = pool.get();
+            bool done = false;
+            uint64_t wave = 0;
+            for (; wave < max_waves && !done; wave++) {
+                cudaEvent_t a = nullptr, m = nullptr, b = nullptr;
+                if (timed) {
+                    a = pool.get();
+                    m = pool.get();
+                    b = pool.get();
+                    VG_CHECK(cudaEventRecord(a, s), "event");
+                }
+                VG_CHECK(vgx::launch_stream_extend(r->traversal_stats, eb, s, c, w, (uint32_t)wave), "extend launch");
+                if (timed)
+                    VG_CHECK(cudaEventRecord(m, s), "event");
+                VG_CHECK(vgx::launch_stream_shade(v, ssb, s, c, w, (uint32_t)wave), "shade launch");
+                if (timed) {
+                    VG_CHECK(cudaEventRecord(b, s), "event");
+                    stages.push_back({0, {a, m}});
+                    stages.push_back({1, {m, b}});
+                }
+                acc->launches += 2;
+                uint32_t slot = (uint32_t)(wave % RING);
+                VG_CHECK(cudaMemcpyAsync(&ring[slot], (uint32_t*)acc->counts.p + ((wave + 1) & 1u), 4,
+                                         cudaMemcpyDeviceToHost, s),
+                         "count readback");
+                VG_CHECK(cudaEventRecord(ring_ev[slot], s), "event");
+                if (wave >= LAG) {
+                    uint32_t old = (uint32_t)((wave - LAG) % RING);
+                    if ((st = wait_event(ring_ev[old])) != VG_OK)
+                        return st;
+                    done = ring[old] == 0;
+                }
+            }
+            acc->last_waves = (uint32_t)wave;
+            if (!done) {
+                VG_CHECK(cudaStreamSynchronize(s), "waves");
+                if (ring[(wave - 1) % RING] != 0)
+                    return fail(VG_ERR_KERNEL, "streaming wavefront did not drain within its wave bound");
+            }
+        }
+        for (uint32_t k = 0; k < (streaming ? 0u : samples); k++) {
             c.p[P_SAMPLE] = acc->samples + k;
             VG_CHECK(vgx::launch_wf_begin(s, c, w), "wf_begin launch");
             acc->launches++;
@@ -879,7 +965,7 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
     if (st != VG_OK)
         return st;
     if (wavefront && samples > 0)
-        acc->last_depth = r->max_depth;
+        acc->last_depth = streamed ? 0 : r->max_depth;
     acc->samples += samples;
     return VG_OK;
 }
