@@ -7,6 +7,7 @@ There is no CPU fallback: without the library or a GB300 every entry point raise
 from __future__ import annotations
 
 import ctypes as C
+import os
 from enum import IntEnum
 from pathlib import Path
 from typing import Optional
@@ -17,7 +18,7 @@ from . import readback as rb
 from .pack import Packed, View, pack
 from .readback import Adaptive, Restir
 
-LIB_PATH = Path(__file__).resolve().parent / "_build" / "libvgcuda.so"
+LIB_PATH = Path(os.environ.get("VGCUDA_LIB", Path(__file__).resolve().parent / "_build" / "libvgcuda.so"))
 
 VG_OK, VG_ERR_NO_DEVICE, VG_ERR_UNSUPPORTED, VG_ERR_OOM, VG_ERR_RESOURCE, VG_ERR_KERNEL, VG_ERR_SCENE, \
     VG_ERR_TIMEOUT, VG_ERR_INVALID = range(9)

@@ -55,9 +55,13 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError(f"build step failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
-    """Compiles the library if any source is newer than it; returns its path."""
-    BUILD.mkdir(exist_ok=True)
+def build(force: bool = False, verbose: bool = False, defines=(), build_dir: Path = None) -> Path:
+    """Compiles the library if any source is newer than it; returns its path. `defines` adds
+    preprocessor definitions (e.g. "VG_SHADE_MIN_BLOCKS=4") for a variant built in `build_dir`."""
+    BUILD = Path(build_dir) if build_dir else globals()["BUILD"]
+    LIB = BUILD / "libvgcuda.so"
+    extra = [f"-D{d}" for d in defines]
+    BUILD.mkdir(parents=True, exist_ok=True)
     nvcc = _nvcc()
     cxx = shutil.which("g++") or "g++"
     jobs = []
@@ -66,7 +70,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         o = BUILD / (Path(s).stem + ".o")
         objs.append(o)
         if force or _stale(o, CSRC / s):
-            jobs.append([nvcc] + NVCC_FLAGS + ["-c", str(CSRC / s), "-o", str(o)])
+            jobs.append([nvcc] + NVCC_FLAGS + extra + ["-c", str(CSRC / s), "-o", str(o)])
     for s in CXX_SOURCES:
         o = BUILD / (Path(s).stem + ".o")
         objs.append(o)

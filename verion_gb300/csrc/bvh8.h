@@ -38,9 +38,6 @@ constexpr uint32_t STACK_SIZE = 32;      // traversal stack entries (node groups
 constexpr uint32_t MAX_WIDE_DEPTH = 30;  // the builder rejects trees deeper than this
 constexpr uint32_t ERR_STACK = 1u;       // error-status bit: a traversal stack overflowed
 
-// Robust slab test factor for the far distance: 1 + 2 gamma(3) rounded up (Ize, "Robust BVH Ray
-// Traversal", JCGT 2013; Pharr, Jakob and Humphreys, PBRT 3rd ed., section 3.9.2).
-constexpr float ROBUST_FAR = 1.00000048f;
 // Direction components smaller than this are replaced by it (sign kept) for the slab test only.
 constexpr float MIN_DIR = 1.0e-20f;
 

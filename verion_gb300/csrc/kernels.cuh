@@ -22,6 +22,11 @@ using namespace vgd;
 
 constexpr uint32_t FULL = 0xffffffffu;
 
+// Minimum resident 128-thread blocks per SM requested for the shade kernels (a register cap).
+#ifndef VG_SHADE_MIN_BLOCKS
+#define VG_SHADE_MIN_BLOCKS 3
+#endif
+
 // State planes (16 bytes each, plane k of path p at state[k * N + p]):
 //   0 (org.xyz, rng)  1 (dir.xyz, flags)  2 (thr.xyz, pathLen)  3 (total.xyz, qPrev)
 //   with the lighting split: 4 (directDiffuse.xyz, visLit) 5 (indirectDiffuse.xyz, visTotal)
@@ -172,7 +177,7 @@ static __device__ __forceinline__ void warp_count(unsigned long long* dst, uint3
 // wf_extend.slang:6-30: closest hit for every live path of depth d. STATS also counts rays,
 // BVH nodes visited and triangles tested into w.tstats[0..2] (rays at depth > 0 into [3]).
 template <bool STATS>
-__global__ void __launch_bounds__(128) wf_extend(const __grid_constant__ Ctx c, Wave w, uint32_t d)
+__global__ void __launch_bounds__(128, 8) wf_extend(const __grid_constant__ Ctx c, Wave w, uint32_t d)
 {
     uint32_t count = w.counts[d];
     const uint32_t* qin = w.queue[d & 1u];
@@ -218,7 +223,7 @@ __global__ void __launch_bounds__(128) wf_extend(const __grid_constant__ Ctx c, 
 
 // wf_shade.slang:7-29: shade each live path of depth d, then queue it for d + 1 or finish it.
 template <bool LIGHT, bool RESTIR, typename A>
-__global__ void __launch_bounds__(128) wf_shade(const __grid_constant__ Ctx c, Wave w, uint32_t d)
+__global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_shade(const __grid_constant__ Ctx c, Wave w, uint32_t d)
 {
     uint32_t count = w.counts[d];
     const uint32_t* qin = w.queue[d & 1u];
@@ -318,7 +323,7 @@ __global__ void __launch_bounds__(256) wf_stream_start(const __grid_constant__ C
 }
 
 template <bool STATS>
-__global__ void __launch_bounds__(128) wf_stream_extend(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
+__global__ void __launch_bounds__(128, 8) wf_stream_extend(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
 {
     uint32_t in = wave & 1u, out = in ^ 1u;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -359,7 +364,7 @@ __global__ void __launch_bounds__(128) wf_stream_extend(const __grid_constant__ 
 }
 
 template <bool LIGHT, typename A>
-__global__ void __launch_bounds__(128) wf_stream_shade(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
+__global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
 {
     uint32_t in = wave & 1u, out = in ^ 1u;
     if (blockIdx.x == 0 && threadIdx.x == 0)

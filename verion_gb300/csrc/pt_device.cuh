@@ -162,7 +162,7 @@ static __device__ __forceinline__ uint32_t emitMask(const Ctx& c, uint32_t inst)
 }
 
 // pt_core.slang:199-216
-static __device__ float iesFactor(const Ctx& c, uint32_t po, V3 d)
+static __device__ __noinline__ float iesFactor(const Ctx& c, uint32_t po, V3 d)
 {
     V3 l = v3(dot(d, v3(lw(c, po), lw(c, po + 1), lw(c, po + 2))), dot(d, v3(lw(c, po + 3), lw(c, po + 4), lw(c, po + 5))),
               dot(d, v3(lw(c, po + 6), lw(c, po + 7), lw(c, po + 8))));
@@ -236,7 +236,7 @@ static __device__ __forceinline__ float envPdf(const Ctx& c, V3 d)
 }
 
 // pt_core.slang:274-306
-static __device__ V3 envSample(const Ctx& c, float u1, float u2, float u3, float u4, float& pdf, V3& le)
+static __device__ __noinline__ V3 envSample(const Ctx& c, float u1, float u2, float u3, float u4, float& pdf, V3& le)
 {
     uint32_t w = c.p[P_ENV_W];
     uint32_t h = c.p[P_ENV_H];
@@ -291,7 +291,7 @@ static __device__ V3 bilinear(const Ctx& c, uint32_t base, uint32_t w, uint32_t 
 }
 
 // pt_core.slang:331-356
-static __device__ V3 sampleTexture(const Ctx& c, uint32_t tex, float ux, float uy, float footprint)
+static __device__ __noinline__ V3 sampleTexture(const Ctx& c, uint32_t tex, float ux, float uy, float footprint)
 {
     uint32_t ti = tex * 4;
     uint32_t base = uget(c.s.tex_info, ti);
@@ -329,7 +329,7 @@ struct Lobes {
 };
 
 // pt_core.slang:384-395
-static __device__ float ggxAlbedo(const Ctx& c, float cosO, float alpha)
+static __device__ __noinline__ float ggxAlbedo(const Ctx& c, float cosO, float alpha)
 {
     const uint32_t N = GGX_ALBEDO_N;
     float x = saturatef(cosO) * (float)(N - 1);
@@ -352,7 +352,7 @@ static __device__ __forceinline__ V3 multiscatterFactor(const Ctx& c, const Surf
 }
 
 // pt_core.slang:410-431
-static __device__ float dielectricAlbedo(const Ctx& c, float cosO, float rough, float ior, bool outside)
+static __device__ __noinline__ float dielectricAlbedo(const Ctx& c, float cosO, float rough, float ior, bool outside)
 {
     const uint32_t N = DIEL_ALBEDO_N;
     float x = saturatef(cosO) * (float)(N - 1);
@@ -377,7 +377,7 @@ static __device__ float dielectricAlbedo(const Ctx& c, float cosO, float rough, 
 }
 
 // pt_core.slang:434-445
-static __device__ float sheenAlbedo(const Ctx& c, float cosO, float r)
+static __device__ __noinline__ float sheenAlbedo(const Ctx& c, float cosO, float r)
 {
     const uint32_t N = SHEEN_ALBEDO_N;
     float x = saturatef(cosO) * (float)(N - 1);
@@ -401,7 +401,7 @@ static __device__ __forceinline__ float sheenCore(float woz, float wiz, float hz
 }
 
 // pt_core.slang:459-486
-static __device__ Lobes evalLobes(const Ctx& c, const Surface& s, V3 woL, V3 wiL)
+static __device__ __noinline__ Lobes evalLobes(const Ctx& c, const Surface& s, V3 woL, V3 wiL)
 {
     V3 hh = normalize(woL + wiL);
     float woh = fmaxf(dot(woL, hh), 0.0f);
@@ -470,7 +470,7 @@ struct Parts {
 };
 
 // pt_core.slang:540-557
-static __device__ float reflectivePdf(const Surface& s, V3 woL, V3 wiL)
+static __device__ __noinline__ float reflectivePdf(const Surface& s, V3 woL, V3 wiL)
 {
     V3 hh = normalize(woL + wiL);
     float woh = fmaxf(dot(woL, hh), 0.0f);
@@ -489,7 +489,7 @@ static __device__ float reflectivePdf(const Surface& s, V3 woL, V3 wiL)
 }
 
 // pt_core.slang:561-576
-static __device__ float opacityAt(const Ctx& c, uint32_t instIdx, uint32_t prim, float b1, float b2)
+static __device__ __noinline__ float opacityAt(const Ctx& c, uint32_t instIdx, uint32_t prim, float b1, float b2)
 {
     uint32_t mi = uget(c.s.instances, instIdx * 16 + 2) * 24;
     float op = fget(c.s.materials, mi + 22);
@@ -518,7 +518,7 @@ static __device__ __forceinline__ vgt::TraceHit traceShadow(const Ctx& c, V3 o, 
 
 // pt_core.slang:580-613. A scene with translucent surfaces takes the closest occluder of each
 // layer (the reference leaves "which hit" to the driver); a fully opaque one stops at any hit.
-static __device__ bool occluded(const Ctx& c, V3 o, V3 d, float tmax)
+static __device__ __noinline__ bool occluded(const Ctx& c, V3 o, V3 d, float tmax)
 {
     for (uint32_t layer = 0; layer < 8; layer++) {
         vgt::TraceHit q = traceShadow(c, o, d, tmax);
@@ -662,7 +662,7 @@ struct RestirPick {
 };
 
 // pt_core.slang:759-882
-static __device__ RestirPick restirDI(const Ctx& c, uint32_t pixel, uint32_t recv, V3 p, V3 n, float pHitT, const Surface& surf,
+static __device__ __noinline__ RestirPick restirDI(const Ctx& c, uint32_t pixel, uint32_t recv, V3 p, V3 n, float pHitT, const Surface& surf,
                                V3 T, V3 B, V3 woL, Rng& rng)
 {
     uint32_t w = c.p[P_WIDTH];

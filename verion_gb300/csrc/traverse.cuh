@@ -8,8 +8,9 @@
 // 0 < t < tmax. The closest hit is the smallest t; equal distances go to the lower global triangle
 // index, so the answer does not depend on the order the tree is walked in.
 //
-// Child boxes are tested with the robust slab test (far distance scaled by 1 + 2 gamma(3), Ize
-// 2013), which never rejects a box the ray touches, so the culling cannot change the answer.
+// Child boxes are tested in the node-local form of Ylitie, Karras and Laine (HPG 2017), one FMA per
+// plane, with an explicit bound on its rounding error added outwards, so a box the ray touches is
+// never rejected and the culling cannot change the answer.
 #pragma once
 #include "bvh8.h"
 #include "vec3.h"
@@ -157,18 +158,29 @@ __device__ __forceinline__ TraceHit trace_bvh(const uint4* __restrict__ nodes, c
         uint32_t fyl = py_pos ? w4.x : w2.z, fyh = py_pos ? w4.y : w2.w;
         uint32_t nzl = pz_pos ? w3.x : w4.z, nzh = pz_pos ? w3.y : w4.w;
         uint32_t fzl = pz_pos ? w4.z : w3.x, fzh = pz_pos ? w4.w : w3.y;
+        // Node-local ray (Ylitie et al. 2017): t(q) = A + q S per axis with A = (p - o) / d and
+        // S = 2^e / d, one FMA per plane. The plane p + q 2^e is exact; A and S carry at most a few
+        // roundings, so every t is moved outwards by err = 2^-21 (|A| + 255 |S|), a bound on that
+        // error: the test never rejects a box the ray enters, and the hits stay those of brute force.
+        float ax = (px - r.o.x) * r.ix, sx = scx * r.ix;
+        float ay = (py - r.o.y) * r.iy, sy = scy * r.iy;
+        float az = (pz - r.o.z) * r.iz, sz = scz * r.iz;
+        float ex = 4.76837158e-7f * (fabsf(ax) + 255.0f * fabsf(sx));
+        float ey = 4.76837158e-7f * (fabsf(ay) + 255.0f * fabsf(sy));
+        float ez = 4.76837158e-7f * (fabsf(az) + 255.0f * fabsf(sz));
+        float anx = ax - ex, afx = ax + ex, any_ = ay - ey, afy = ay + ey, anz = az - ez, afz = az + ez;
         uint32_t inner_hits = 0;
         uint32_t tri_bits = 0;
 #pragma unroll
         for (int i = 0; i < 8; i++) {
-            float tnx = (fmaf((float)byte_of(nxl, nxh, i), scx, px) - r.o.x) * r.ix;
-            float tny = (fmaf((float)byte_of(nyl, nyh, i), scy, py) - r.o.y) * r.iy;
-            float tnz = (fmaf((float)byte_of(nzl, nzh, i), scz, pz) - r.o.z) * r.iz;
-            float tfx = (fmaf((float)byte_of(fxl, fxh, i), scx, px) - r.o.x) * r.ix;
-            float tfy = (fmaf((float)byte_of(fyl, fyh, i), scy, py) - r.o.y) * r.iy;
-            float tfz = (fmaf((float)byte_of(fzl, fzh, i), scz, pz) - r.o.z) * r.iz;
+            float tnx = fmaf((float)byte_of(nxl, nxh, i), sx, anx);
+            float tny = fmaf((float)byte_of(nyl, nyh, i), sy, any_);
+            float tnz = fmaf((float)byte_of(nzl, nzh, i), sz, anz);
+            float tfx = fmaf((float)byte_of(fxl, fxh, i), sx, afx);
+            float tfy = fmaf((float)byte_of(fyl, fyh, i), sy, afy);
+            float tfz = fmaf((float)byte_of(fzl, fzh, i), sz, afz);
             float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
-            float tf = fminf(fminf(fminf(tfx, tfy), tfz) * bvh8::ROBUST_FAR, best_t);
+            float tf = fminf(fminf(tfx, tfy), fminf(tfz, best_t));
             if (tn <= tf) {
                 if ((imask >> i) & 1u) {
                     inner_hits |= 1u << (i ^ r.oct);
