@@ -162,6 +162,10 @@ typedef enum VgWavefrontMode { VG_WAVEFRONT_PER_SAMPLE = 0, VG_WAVEFRONT_STREAMI
 int vg_set_wavefront_mode(VgRenderer* r, int mode);
 /* Streaming mode: waves (extend + shade pairs) issued by the last vg_accumulate. */
 uint32_t vg_accum_last_waves(const VgAccum* acc);
+/* Streaming mode, last vg_accumulate: per wave, the live slots after it and (with stage timing)
+ * the extend and shade milliseconds, 3 floats per wave for up to `waves` waves. Returns the
+ * number of waves recorded. */
+size_t vg_accum_wave_profile(const VgAccum* acc, float* out, size_t waves);
 /* Wavefront only: count rays, BVH nodes visited and triangles tested in the extend stage of
  * later accumulate calls (read with vg_accum_traversal_stats). */
 int vg_set_traversal_stats(VgRenderer* r, int on);

@@ -131,3 +131,74 @@ def center_mean(img: np.ndarray, w: int, size: int) -> float:
     lo = (w - size) // 2
     im = img.reshape(-1, w, 3)
     return float(im[lo:lo + size, lo:lo + size, 0].mean())
+
+
+def textured_plane(half: float, z: float, repeat: float = 1.0) -> sc.Mesh:
+    """A square with uvs spanning [0, repeat] and +z vertex normals."""
+    h = half
+    pos = np.array([[-h, -h, z], [h, -h, z], [h, h, z], [-h, h, z]], np.float32)
+    uv = np.array([[0, 0], [repeat, 0], [repeat, repeat], [0, repeat]], np.float32)
+    nrm = np.tile(np.array([[0.0, 0.0, 1.0]], np.float32), (4, 1))
+    return sc.Mesh(pos, np.array([0, 1, 2, 0, 2, 3]), normals=nrm, uvs=uv)
+
+
+def _rot_y(a, s=1.0, t=(0.0, 0.0, 0.0)):
+    c, n = math.cos(a) * s, math.sin(a) * s
+    return ((c, 0.0, n, t[0]), (0.0, s, 0.0, t[1]), (-n, 0.0, c, t[2]))
+
+
+def feature_zoo(transparent_background: bool = False) -> sc.Scene:
+    """Every shading feature of pt_core.slang in one small scene: textures with mip chains (base
+    colour, metallic-roughness, emission, normal map, opacity cut-out), sheen, clearcoat, dispersive
+    glass, rough dielectric, IES, spot, point and directional lights, light linking, a uniform sky,
+    and rotated / scaled instances with interpolated normals."""
+    rng = np.random.default_rng(5)
+    s = sc.Scene()
+    checker = np.array([[0.9, 0.2, 0.1] if (i // 4 + j // 4) % 2 else [0.1, 0.6, 0.9]
+                        for j in range(16) for i in range(16)], np.float32)
+    t_base = s.add_image(sc.Image(16, 16, checker))
+    t_mr = s.add_image(sc.Image(8, 8, rng.uniform(0.1, 1.0, (64, 3)).astype(np.float32)))
+    nm = np.zeros((32 * 32, 3), np.float32)
+    for j in range(32):
+        for i in range(32):
+            nx, ny = 0.4 * math.sin(i * 0.6), 0.4 * math.cos(j * 0.5)
+            nm[j * 32 + i] = [0.5 + 0.5 * nx, 0.5 + 0.5 * ny, 0.5 + 0.5 * math.sqrt(max(0.0, 1 - nx * nx - ny * ny))]
+    t_nrm = s.add_image(sc.Image(32, 32, nm))
+    t_em = s.add_image(sc.Image(4, 4, rng.uniform(0.5, 3.0, (16, 3)).astype(np.float32)))
+    t_op = s.add_image(sc.Image(4, 4, np.array([[1.0] * 3, [0.0] * 3, [0.5] * 3, [1.0] * 3] * 4, np.float32)))
+
+    floor = s.add_mesh(textured_plane(4.0, 0.0, repeat=3.0))
+    m_floor = s.add_material(sc.BaseBsdf(base_color=(1.0, 1.0, 1.0), roughness=0.6, metallic=0.3,
+                                         base_color_texture=t_base, metallic_roughness_texture=t_mr,
+                                         normal_texture=t_nrm, normal_scale=0.8))
+    s.add_instance(sc.Instance(floor, m_floor, ((1, 0, 0, 0), (0, 0, -1, -0.5), (0, 1, 0, 0))))  # floor at y = -0.5
+    sp, sn, si = scenes.octasphere(6)
+    ball = s.add_mesh(sc.Mesh(sp, si, normals=sn))
+    m_velvet = s.add_material(sc.BaseBsdf(base_color=(0.6, 0.1, 0.3), roughness=0.7, sheen_color=(0.9, 0.8, 0.7),
+                                          sheen_roughness=0.4, clearcoat=0.7, clearcoat_roughness=0.2))
+    m_prism = s.add_material(sc.BaseBsdf(base_color=(1.0, 1.0, 1.0), transmission=1.0, roughness=0.0, dispersion=3.0))
+    m_frost = s.add_material(sc.BaseBsdf(base_color=(0.9, 1.0, 0.9), transmission=1.0, roughness=0.35, ior=1.4))
+    m_gold = s.add_material(sc.BaseBsdf(base_color=(1.0, 0.8, 0.4), metallic=1.0, roughness=0.25))
+    s.add_instance(sc.Instance(ball, m_velvet, _rot_y(0.4, 0.35, (-0.6, -0.15, 0.2))))
+    s.add_instance(sc.Instance(ball, m_prism, _rot_y(1.1, 0.3, (0.3, -0.2, 0.5))))
+    s.add_instance(sc.Instance(ball, m_frost, ((0.3, 0.0, 0.0, 0.8), (0.0, 0.2, 0.0, -0.3), (0.0, 0.0, 0.35, -0.3))))
+    gold = s.add_instance(sc.Instance(ball, m_gold, _rot_y(-0.3, 0.25, (-0.1, -0.25, -0.6))))
+    lamp = s.add_mesh(textured_plane(0.3, 0.0))
+    m_lamp = s.add_material(sc.BaseBsdf(base_color=(0.0, 0.0, 0.0), emission=(2.0, 2.0, 2.0), emission_texture=t_em))
+    s.add_instance(sc.Instance(lamp, m_lamp, ((1, 0, 0, -1.2), (0, 1, 0, 0.6), (0, 0, 1, -1.5))))
+    m_glow = s.add_material(scenes.material((0.2, 0.2, 0.2), (6.0, 5.0, 4.0)))
+    s.add_instance(sc.Instance(lamp, m_glow, ((0.5, 0, 0, 0.9), (0, 0, -0.5, 1.4), (0, 0.5, 0, 0.0))))
+    cut = s.add_mesh(textured_plane(0.4, 0.0, repeat=2.0))
+    m_cut = s.add_material(sc.BaseBsdf(base_color=(0.2, 0.7, 0.2), opacity=0.9, opacity_texture=t_op))
+    s.add_instance(sc.Instance(cut, m_cut, _rot_y(0.7, 1.0, (0.2, 0.3, 0.9))))
+    ies = sc.IesProfile(np.array([[1.0 + 0.5 * math.cos(math.radians(v)) * (1 + 0.3 * math.sin(math.radians(h)))
+                                   for v in range(181)] for h in range(361)], np.float32))
+    s.add_light(sc.Point((0.5, 1.2, 0.8), (1.0, 0.9, 0.8), 3.0),
+                sc.LightExtra(ies=(ies, ((1.0, 0.0, 0.0), (0.0, 0.0, 1.0), (0.0, -1.0, 0.0)))))
+    s.add_light(sc.Spot((-0.8, 1.5, 0.5), (0.5, -1.0, -0.3), (0.6, 0.7, 1.0), 4.0, 0.2, 0.5))
+    s.add_light(sc.Directional((0.3, -1.0, -0.5), (1.0, 1.0, 0.9), 1.5), sc.LightExtra(link_mask=0b10))
+    s.instance_masks[gold] = 0b01  # the directional light does not reach the gold ball
+    s.add_light(sc.Environment((0.1, 0.12, 0.15)))
+    s.camera = scenes.look_at((0.0, 0.8, 3.2), (0.0, -0.1, 0.0), fov=0.8)
+    s.transparent_background = transparent_background
+    return s

@@ -247,3 +247,27 @@ def test_streaming_lighting_split_bit_exact(gpu_ctx):
     ref = oracle_render(p, 40, 30, 6, lighting=True)
     assert_same(acc.sums(), ref.sums, "sums")
     assert_same(acc.raw_lighting(), ref.lighting, "lighting split")
+
+
+@pytest.mark.parametrize("integrator", [Integrator.MEGAKERNEL, Integrator.WAVEFRONT])
+@pytest.mark.parametrize("lighting", [False, True])
+def test_feature_zoo_bit_exact(gpu_ctx, integrator, lighting):
+    # Textures with mip chains, normal and opacity maps, IES, spot / point / directional lights with
+    # light linking, sheen, clearcoat, dispersive and rough glass, textured emitters, instancing.
+    from . import analytic as an
+
+    p = pack.pack(an.feature_zoo())
+    _, acc = gpu_render(gpu_ctx, p, 64, 48, 6, integrator=integrator, lighting=lighting, chunks=[2, 4])
+    ref = oracle_render(p, 64, 48, 6, lighting=lighting)
+    assert_same(acc.sums(), ref.sums, "feature zoo sums")
+    if lighting:
+        assert_same(acc.raw_lighting(), ref.lighting, "feature zoo lighting split")
+
+
+def test_transparent_background_bit_exact(gpu_ctx):
+    from . import analytic as an
+
+    p = pack.pack(an.feature_zoo(transparent_background=True))
+    _, acc = gpu_render(gpu_ctx, p, 48, 36, 4, integrator=Integrator.WAVEFRONT)
+    ref = oracle_render(p, 48, 36, 4)
+    assert_same(acc.sums(), ref.sums, "transparent background sums")

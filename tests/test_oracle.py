@@ -212,3 +212,73 @@ def test_edge_rays_hit_exactly_one_of_two_adjacent_triangles(oracle_lib):
     rays = np.stack([u, u, np.full_like(u, 1.0), np.zeros_like(u), np.zeros_like(u), -np.ones_like(u)], axis=1)
     h = o.trace_closest(rays, brute=True)
     assert h[:, 0].all()
+
+
+def test_clearcoat_adds_a_second_fresnel_layer(oracle_lib):
+    # pathtrace.rs:600-617: coat F0 0.04 plus 0.04 of the 0.96 it lets through.
+    m = sc.BaseBsdf(base_color=(0.0, 0.0, 0.0), roughness=0.0, clearcoat=1.0)
+    img = image(render(an.sky_scene(scenes.plane(5.0, 0.0), m, 3.0), 32, 32, 128))
+    assert abs(an.center_mean(img, 32, 16) - 0.0784) < 0.004
+
+
+def test_clearcoat_and_sheen_furnaces_conserve_energy(oracle_lib):
+    # pathtrace.rs:619-640, 662-683
+    for m in (sc.BaseBsdf(base_color=(1.0,) * 3, roughness=0.5, clearcoat=1.0, clearcoat_roughness=0.0),
+              sc.BaseBsdf(base_color=(1.0,) * 3, roughness=0.5, clearcoat=1.0, clearcoat_roughness=0.3)):
+        got = an.center_mean(image(render(an.sky_scene(scenes.cube(0.5), m, 3.0), 32, 32, 64)), 32, 16)
+        assert 0.95 < got < 1.01
+    for r in (0.3, 1.0):
+        m = sc.BaseBsdf(base_color=(1.0,) * 3, roughness=0.5, sheen_color=(1.0,) * 3, sheen_roughness=r)
+        got = an.center_mean(image(render(an.sky_scene(scenes.cube(0.5), m, 3.0), 32, 32, 64)), 32, 16)
+        assert 0.95 < got < 1.02
+
+
+def test_sheen_adds_its_directional_albedo_to_a_black_base(oracle_lib):
+    # pathtrace.rs:642-660
+    m = sc.BaseBsdf(base_color=(0.0,) * 3, roughness=0.0, sheen_color=(1.0,) * 3, sheen_roughness=1.0)
+    got = an.center_mean(image(render(an.sky_scene(scenes.plane(5.0, 0.0), m, 3.0), 32, 32, 128)), 32, 16)
+    assert abs(got - (0.137 + (1.0 - 0.137) * 0.04)) < 0.01
+
+
+def test_dispersion_gives_each_channel_its_own_fresnel_reflection(oracle_lib):
+    # pathtrace.rs:700-738
+    s = sc.Scene()
+    glass = s.add_material(sc.BaseBsdf(base_color=(1.0,) * 3, roughness=0.0, transmission=1.0, dispersion=4.0))
+    floor = s.add_material(sc.BaseBsdf(base_color=(0.0,) * 3, metallic=1.0, roughness=1.0))
+    for mesh, mat in ((scenes.plane(5.0, 0.0), glass), (scenes.plane(5.0, -1.0), floor)):
+        s.add_instance(sc.Instance(s.add_mesh(mesh), mat))
+    s.add_light(sc.Environment((1.0, 1.0, 1.0)))
+    s.camera = scenes.camera_at_z(3.0)
+    img = image(render(s, 32, 32, 512)).reshape(32, 32, 3)[8:24, 8:24].reshape(-1, 3).mean(axis=0)
+    for c, want in enumerate((0.0293, 0.04, 0.0465)):
+        assert abs(img[c] - want) < 0.006
+    assert img[0] < img[1] < img[2]
+
+
+def test_metal_tints_by_base_color(oracle_lib):
+    # pathtrace.rs:760-774
+    m = sc.BaseBsdf(base_color=(0.5,) * 3, metallic=1.0, roughness=0.0)
+    got = an.center_mean(image(render(an.sky_scene(scenes.plane(5.0, 0.0), m, 3.0), 32, 32, 16)), 32, 16)
+    assert abs(got - 0.5) < 0.01
+
+
+def test_glass_furnace_conserves_energy(oracle_lib):
+    # pathtrace.rs:776-797 (a subdivided octahedron stands in for the icosphere)
+    sp, _, si = scenes.octasphere(8)
+    for roughness, lo in ((0.0, 0.98), (0.3, 0.9)):
+        m = sc.BaseBsdf(base_color=(1.0,) * 3, roughness=roughness, transmission=1.0)
+        got = image(render(an.sky_scene(sc.Mesh(sp, si), m, 4.0), 48, 48, 64))[:, 0].mean()
+        assert lo < got < 1.01, (roughness, got)
+
+
+def test_opacity_lets_rays_and_shadows_through(oracle_lib):
+    # pathtrace.rs:1651-1672
+    def lit(opacity):
+        s = an.floor_scene(an.point_light(), True)
+        s.materials[1] = sc.BaseBsdf(base_color=(0.0,) * 3, ior=1.0, opacity=opacity)
+        return image(render(s, 65, 65, 64))[32 * 65 + 32, 0]
+
+    full = image(render(an.floor_scene(an.point_light(), False), 65, 65, 64))[32 * 65 + 32, 0]
+    assert abs(lit(0.0) - full) < 0.02 * full
+    assert lit(1.0) < 0.02 * full
+    assert abs(lit(0.5) - 0.5 * full) < 0.08 * full

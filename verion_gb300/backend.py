@@ -124,6 +124,7 @@ def lib() -> C.CDLL:
             "vg_set_traversal_stats": (i32, [vp, i32]),
             "vg_set_wavefront_mode": (i32, [vp, i32]),
             "vg_accum_last_waves": (u32, [vp]),
+            "vg_accum_wave_profile": (_S, [vp, vp, _S]),
             "vg_accum_traversal_stats": (i32, [vp, C.POINTER(C.c_uint64)]),
             "vg_set_accum_precision": (i32, [vp, i32]),
             "vg_accum_create": (i32, [vp, u32, u32, i32, C.POINTER(vp)]),
@@ -245,6 +246,13 @@ class Accumulation:
 
     def last_waves(self) -> int:
         return lib().vg_accum_last_waves(self._h)
+
+    def wave_profile(self) -> np.ndarray:
+        """(waves, 3): live slots after each wave, extend ms, shade ms (last streaming call)."""
+        n = lib().vg_accum_wave_profile(self._h, None, 0)
+        out = np.zeros(3 * n, np.float32)
+        lib().vg_accum_wave_profile(self._h, _ptr(out), n)
+        return out.reshape(-1, 3)
 
     def traversal_stats(self) -> dict:
         out = (C.c_uint64 * 4)()

@@ -168,6 +168,8 @@ struct VgAccum {
     DevBuf state, hits, queue[2], counts, fetch, tstats, meta;
     uint32_t* host_counts = nullptr; // pinned ring of wave output counts (streaming wavefront)
     uint32_t last_waves = 0;
+    std::vector<uint32_t> wave_live; // last streaming accumulate: live slots after each wave
+    std::vector<float> wave_ms;      // with stage timing: extend, shade milliseconds per wave
     ~VgAccum()
     {
         if (host_counts)
@@ -666,6 +668,19 @@ int vg_set_wavefront_mode(VgRenderer* r, int mode)
 
 uint32_t vg_accum_last_waves(const VgAccum* acc) { return acc ? acc->last_waves : 0; }
 
+size_t vg_accum_wave_profile(const VgAccum* acc, float* out, size_t waves)
+{
+    if (!acc)
+        return 0;
+    size_t n = std::min(waves, acc->wave_live.size());
+    for (size_t k = 0; out && k < n; k++) {
+        out[3 * k] = (float)acc->wave_live[k];
+        out[3 * k + 1] = 2 * k + 1 < acc->wave_ms.size() ? acc->wave_ms[2 * k] : 0.0f;
+        out[3 * k + 2] = 2 * k + 1 < acc->wave_ms.size() ? acc->wave_ms[2 * k + 1] : 0.0f;
+    }
+    return acc->wave_live.size();
+}
+
 int vg_set_traversal_stats(VgRenderer* r, int on)
 {
     if (!r)
@@ -857,6 +872,8 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
         bool streaming = r->wavefront_mode == VG_WAVEFRONT_STREAMING && !acc->restir.on;
         if (streaming && samples > 0) {
             streamed = true;
+            acc->wave_live.clear();
+            acc->wave_ms.clear();
             int svi = v.index() & 5;
             if (r->stream_shade_blocks[svi] == 0)
                 r->stream_shade_blocks[svi] = vgx::stream_shade_blocks_per_sm(v);
@@ -905,9 +922,13 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
                     if ((st = wait_event(ring_ev[old])) != VG_OK)
                         return st;
                     done = ring[old] == 0;
+                    acc->wave_live.push_back(ring[old]);
                 }
             }
             acc->last_waves = (uint32_t)wave;
+            VG_CHECK(cudaStreamSynchronize(s), "waves");
+            for (uint64_t k = wave > LAG ? wave - LAG + 1 : 0; k < wave; k++)
+                acc->wave_live.push_back(ring[k % RING]);
             if (!done) {
                 VG_CHECK(cudaStreamSynchronize(s), "waves");
                 if (ring[(wave - 1) % RING] != 0)
@@ -957,6 +978,8 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
             float sm = 0.0f;
             VG_CHECK(cudaEventElapsedTime(&sm, sp.second.first, sp.second.second), "event");
             acc->stage_seconds[sp.first] += sm * 1e-3;
+            if (streamed)
+                acc->wave_ms.push_back(sm);
             if (sp.first == 0)
                 acc->extend_launches_timed++;
         }
