@@ -160,11 +160,20 @@ int vg_set_max_depth(VgRenderer* r, uint32_t depth);
  * still added in order, and the sums are identical. ReSTIR always runs per sample. */
 typedef enum VgWavefrontMode { VG_WAVEFRONT_PER_SAMPLE = 0, VG_WAVEFRONT_STREAMING = 1 } VgWavefrontMode;
 int vg_set_wavefront_mode(VgRenderer* r, int mode);
+/* Streaming mode: when at most `threshold` slots are live after a wave, the rest of the batch
+ * (those paths and their remaining samples) runs in one launch, trace and shade in a loop per slot,
+ * instead of one wave per bounce. 0 disables it. Default 32768. */
+int vg_set_stream_tail(VgRenderer* r, uint32_t threshold);
+/* Streaming mode without the lighting split: trace the bounce's emitter / environment shadow ray
+ * in a separate stage after shade (default on) or inline in shade (off). Same sums either way. */
+int vg_set_deferred_shadows(VgRenderer* r, int on);
+/* With stage timing: seconds of the last call's tail launch (0 if none ran). */
+double vg_accum_tail_seconds(const VgAccum* acc);
 /* Streaming mode: waves (extend + shade pairs) issued by the last vg_accumulate. */
 uint32_t vg_accum_last_waves(const VgAccum* acc);
 /* Streaming mode, last vg_accumulate: per wave, the live slots after it and (with stage timing)
- * the extend and shade milliseconds, 3 floats per wave for up to `waves` waves. Returns the
- * number of waves recorded. */
+ * the extend, shade and shadow-stage milliseconds (shadow 0 when shade traced inline), 4 floats
+ * per wave for up to `waves` waves. Returns the number of waves recorded. */
 size_t vg_accum_wave_profile(const VgAccum* acc, float* out, size_t waves);
 /* Wavefront only: count rays, BVH nodes visited and triangles tested in the extend stage of
  * later accumulate calls (read with vg_accum_traversal_stats). */

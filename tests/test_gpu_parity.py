@@ -223,20 +223,49 @@ def test_many_spheres_depth16_env_bit_exact(gpu_ctx):
     assert_same(acc.sums(), ref.sums, "1M-triangle scene, depth 16, environment map")
 
 
-@pytest.mark.parametrize("mode", [WavefrontMode.PER_SAMPLE, WavefrontMode.STREAMING])
+@pytest.mark.parametrize("mode,tail", [(WavefrontMode.PER_SAMPLE, 0), (WavefrontMode.STREAMING, 0),
+                                       (WavefrontMode.STREAMING, 400), (WavefrontMode.STREAMING, 1 << 30)])
 @pytest.mark.parametrize("adaptive", [None, Adaptive(threshold=0.05, min_spp=4)])
-def test_wavefront_modes_match_the_oracle(gpu_ctx, mode, adaptive):
+def test_wavefront_modes_match_the_oracle(gpu_ctx, mode, tail, adaptive):
+    # Streaming with the tail off (waves only), on at a few hundred live slots, and on at once.
     s = scenes.many_spheres(hdri=(256, 128))
     p = pack.pack(s)
     w, h = 48, 27
-    _, acc = gpu_render(gpu_ctx, p, w, h, 12, integrator=Integrator.WAVEFRONT, depth=16, adaptive=adaptive,
-                        mode=mode, chunks=[5, 7])
+    r = Renderer(gpu_ctx, p)
+    r.set_accum_precision(32)
+    r.set_integrator(Integrator.WAVEFRONT)
+    r.set_wavefront_mode(mode)
+    r.set_stream_tail(tail)
+    r.set_max_depth(16)
+    r.set_adaptive(adaptive)
+    acc = r.new_accumulation(w, h)
+    for n in (5, 7):
+        r.accumulate(acc, n)
     ref = oracle_render(p, w, h, 12, depth=16, adaptive=adaptive)
-    assert_same(acc.sums(), ref.sums, f"{mode.name} wavefront sums")
+    assert_same(acc.sums(), ref.sums, f"{mode.name} wavefront sums (tail {tail})")
     if adaptive is not None:
         assert_same(acc.raw_stats(), ref.stats, "adaptive statistics")
     if mode == WavefrontMode.STREAMING:
         assert 0 < acc.last_waves() <= 7 * 16 + 3
+
+
+@pytest.mark.parametrize("deferred", [False, True])
+def test_streaming_shadow_stage_matches_the_oracle(gpu_ctx, deferred):
+    # The emitter / environment shadow ray traced inline in shade, or in the separate shadow stage.
+    from . import analytic as an
+
+    for s, depth in ((scenes.many_spheres(hdri=(256, 128)), 16), (an.feature_zoo(), 8)):
+        p = pack.pack(s)
+        r = Renderer(gpu_ctx, p)
+        r.set_accum_precision(32)
+        r.set_integrator(Integrator.WAVEFRONT)
+        r.set_deferred_shadows(deferred)
+        r.set_stream_tail(0)
+        r.set_max_depth(depth)
+        acc = r.new_accumulation(40, 30)
+        r.accumulate(acc, 6)
+        ref = oracle_render(p, 40, 30, 6, depth=depth)
+        assert_same(acc.sums(), ref.sums, f"shadow stage {'deferred' if deferred else 'inline'}")
 
 
 def test_streaming_lighting_split_bit_exact(gpu_ctx):

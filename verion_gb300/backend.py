@@ -125,6 +125,9 @@ def lib() -> C.CDLL:
             "vg_set_wavefront_mode": (i32, [vp, i32]),
             "vg_accum_last_waves": (u32, [vp]),
             "vg_accum_wave_profile": (_S, [vp, vp, _S]),
+            "vg_set_stream_tail": (i32, [vp, u32]),
+            "vg_accum_tail_seconds": (f64, [vp]),
+            "vg_set_deferred_shadows": (i32, [vp, i32]),
             "vg_accum_traversal_stats": (i32, [vp, C.POINTER(C.c_uint64)]),
             "vg_set_accum_precision": (i32, [vp, i32]),
             "vg_accum_create": (i32, [vp, u32, u32, i32, C.POINTER(vp)]),
@@ -247,12 +250,15 @@ class Accumulation:
     def last_waves(self) -> int:
         return lib().vg_accum_last_waves(self._h)
 
+    def tail_seconds(self) -> float:
+        return lib().vg_accum_tail_seconds(self._h)
+
     def wave_profile(self) -> np.ndarray:
-        """(waves, 3): live slots after each wave, extend ms, shade ms (last streaming call)."""
+        """(waves, 4): live slots after each wave, extend, shade and shadow ms (last streaming call)."""
         n = lib().vg_accum_wave_profile(self._h, None, 0)
-        out = np.zeros(3 * n, np.float32)
+        out = np.zeros(4 * n, np.float32)
         lib().vg_accum_wave_profile(self._h, _ptr(out), n)
-        return out.reshape(-1, 3)
+        return out.reshape(-1, 4)
 
     def traversal_stats(self) -> dict:
         out = (C.c_uint64 * 4)()
@@ -399,6 +405,12 @@ class Renderer:
 
     def set_wavefront_mode(self, mode: "WavefrontMode") -> None:
         _check(lib().vg_set_wavefront_mode(self._h, int(mode)))
+
+    def set_deferred_shadows(self, on: bool) -> None:
+        _check(lib().vg_set_deferred_shadows(self._h, int(on)))
+
+    def set_stream_tail(self, threshold: int) -> None:
+        _check(lib().vg_set_stream_tail(self._h, threshold))
 
     def set_traversal_stats(self, on: bool) -> None:
         _check(lib().vg_set_traversal_stats(self._h, int(on)))

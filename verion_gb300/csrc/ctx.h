@@ -67,6 +67,7 @@ struct Wave {
     uint32_t* counts;  // live paths per depth, max depth + 1 entries
     uint32_t* fetch;   // work counters: extend of depth d at [d], shade at [(D + 1) + d]
     unsigned long long* tstats; // traversal counters: rays, nodes, triangle tests, rays past depth 0
+    float4* sreq;      // streaming mode, deferred shadow requests: 3 planes of float4 per slot
     uint32_t* meta;    // streaming mode: per path slot, depth (bits 0-7) and sample within the batch (8+)
     uint32_t n;        // paths: one per pixel
     uint32_t depth;    // max depth

@@ -160,3 +160,62 @@ int stream_shade_blocks_per_sm(Variant v)
 }
 
 } // namespace vgx
+
+namespace vgx {
+
+cudaError_t launch_stream_tail(Variant v, uint32_t max_slots, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                               uint32_t wave)
+{
+    unsigned blocks = (max_slots + 127) / 128;
+    if (blocks == 0)
+        return cudaSuccess;
+    if (v.light && v.f64)
+        vgk::wf_stream_tail<true, double><<<blocks, 128, 0, s>>>(c, w, wave);
+    else if (v.light)
+        vgk::wf_stream_tail<true, float><<<blocks, 128, 0, s>>>(c, w, wave);
+    else if (v.f64)
+        vgk::wf_stream_tail<false, double><<<blocks, 128, 0, s>>>(c, w, wave);
+    else
+        vgk::wf_stream_tail<false, float><<<blocks, 128, 0, s>>>(c, w, wave);
+    return cudaGetLastError();
+}
+
+} // namespace vgx
+
+namespace vgx {
+
+cudaError_t launch_stream_shade_deferred(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                                         uint32_t wave)
+{
+    if (f64)
+        vgk::wf_stream_shade_deferred<double><<<blocks, 128, 0, s>>>(c, w, wave);
+    else
+        vgk::wf_stream_shade_deferred<float><<<blocks, 128, 0, s>>>(c, w, wave);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_shadow(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                                 uint32_t wave)
+{
+    if (f64)
+        vgk::wf_stream_shadow<double><<<blocks, 128, 0, s>>>(c, w, wave);
+    else
+        vgk::wf_stream_shadow<float><<<blocks, 128, 0, s>>>(c, w, wave);
+    return cudaGetLastError();
+}
+
+int stream_deferred_blocks_per_sm(bool f64, int* shadow)
+{
+    int n = 0, m = 0;
+    if (f64) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, vgk::wf_stream_shade_deferred<double>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, vgk::wf_stream_shadow<double>, 128, 0);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, vgk::wf_stream_shade_deferred<float>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, vgk::wf_stream_shadow<float>, 128, 0);
+    }
+    *shadow = m > 0 ? m : 1;
+    return n > 0 ? n : 1;
+}
+
+} // namespace vgx

@@ -329,6 +329,7 @@ __global__ void __launch_bounds__(128, 8) wf_stream_extend(const __grid_constant
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         w.counts[out] = 0;
         w.fetch[2 + in] = 0;
+        w.fetch[4 + in] = 0;
     }
     uint32_t count = w.counts[in];
     const uint32_t* qin = w.queue[in];
@@ -408,6 +409,139 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade(cons
         }
         __syncwarp();
         warp_append(&w.counts[out], qout, live, p);
+    }
+}
+
+// Streaming wave in three stages (lighting split off): extend, then shade without any traversal,
+// then shadow. Shade leaves its emitter / environment light sample as a request per slot
+// (w.sreq planes: origin + tmax, direction + flags, contribution); the shadow stage traces it,
+// adds the contribution when unoccluded, and only then finishes, restarts or queues the slot.
+// flags: bit 0 a request is present, bit 1 the path goes on to the next depth.
+template <typename A>
+__global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade_deferred(const __grid_constant__ Ctx c,
+                                                                                    Wave w, uint32_t wave)
+{
+    uint32_t in = wave & 1u;
+    uint32_t count = w.counts[in];
+    const uint32_t* qin = w.queue[in];
+    uint32_t n = w.n;
+    for (;;) {
+        uint32_t base = warp_fetch(&w.fetch[2 + in]);
+        if (base >= count)
+            break;
+        uint32_t i = base + lane_id();
+        if (i < count) {
+            uint32_t p = qin[i];
+            uint32_t depth = w.meta[p] & 0xffu;
+            PathState<false> st = loadState<false>(w, p);
+            uint4 hr = w.hits[p];
+            Hit h;
+            h.hit = hr.x != 0;
+            h.inst = hr.y;
+            h.prim = hr.z;
+            h.t = __uint_as_float(hr.w);
+            ShadowReq req;
+            bool alive = shadePath<false, false, true>(c, st, h, depth, p, &req) && depth + 1 < w.depth;
+            if (alive)
+                storePath<false>(w, st, p);
+            else
+                w.state[3 * n + p] = make_float4(st.parts.total.x, st.parts.total.y, st.parts.total.z, st.qPrev);
+            uint32_t flags = (req.valid ? 1u : 0u) | (alive ? 2u : 0u);
+            w.sreq[n + p] = make_float4(req.d.x, req.d.y, req.d.z, __uint_as_float(flags));
+            if (req.valid) {
+                w.sreq[p] = make_float4(req.o.x, req.o.y, req.o.z, req.tmax);
+                w.sreq[2 * n + p] = make_float4(req.c.x, req.c.y, req.c.z, 0.0f);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+template <typename A>
+__global__ void __launch_bounds__(128, 8) wf_stream_shadow(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
+{
+    uint32_t in = wave & 1u, out = in ^ 1u;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        w.fetch[out] = 0;
+    uint32_t count = w.counts[in];
+    const uint32_t* qin = w.queue[in];
+    uint32_t* qout = w.queue[out];
+    uint32_t n = w.n;
+    uint32_t batch = c.p[P_SAMPLES_PER_DISPATCH];
+    for (;;) {
+        uint32_t base = warp_fetch(&w.fetch[4 + in]);
+        if (base >= count)
+            break;
+        uint32_t i = base + lane_id();
+        bool live = false;
+        uint32_t p = 0;
+        if (i < count) {
+            p = qin[i];
+            uint32_t meta = w.meta[p];
+            uint32_t depth = meta & 0xffu, k = meta >> 8;
+            uint32_t flags = __float_as_uint(w.sreq[n + p].w);
+            float4 tot = w.state[3 * n + p];
+            V3 total = v3(tot.x, tot.y, tot.z);
+            if (flags & 1u) {
+                float4 r0 = w.sreq[p], r1 = w.sreq[n + p], r2 = w.sreq[2 * n + p];
+                if (!occluded(c, v3(r0.x, r0.y, r0.z), v3(r1.x, r1.y, r1.z), r0.w)) {
+                    total += v3(r2.x, r2.y, r2.z);
+                    if (flags & 2u)
+                        w.state[3 * n + p] = make_float4(total.x, total.y, total.z, tot.w);
+                }
+            }
+            if (flags & 2u) {
+                w.meta[p] = (depth + 1) | (k << 8);
+                live = true;
+            } else {
+                PathState<false> st;
+                st.parts.zero();
+                st.parts.total = total;
+                st.visLit = st.visTotal = 0.0f;
+                finishPath<false, A>(c, st, p);
+                if (k + 1 < batch && (c.p[P_ADAPTIVE] == 0 || pixelActive<A>(c, p))) {
+                    PathState<false> nx =
+                        generatePathFor<false>(c, p % c.p[P_WIDTH], p / c.p[P_WIDTH], c.p[P_SAMPLE] + k + 1);
+                    storePath<false>(w, nx, p);
+                    w.meta[p] = (k + 1) << 8;
+                    live = true;
+                }
+            }
+        }
+        __syncwarp();
+        warp_append(&w.counts[out], qout, live, p);
+    }
+}
+
+// The tail of a streaming batch: once few slots are live, one thread per remaining slot runs its
+// path and the rest of its samples to the end, trace and shade in a loop as the megakernel does,
+// instead of one half-empty wave per bounce. Same functions, same order per pixel, same sums.
+template <bool LIGHT, typename A>
+__global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_tail(const __grid_constant__ Ctx c, Wave w,
+                                                                          uint32_t wave)
+{
+    uint32_t in = wave & 1u;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.counts[in])
+        return;
+    uint32_t p = w.queue[in][i];
+    uint32_t meta = w.meta[p];
+    uint32_t depth = meta & 0xffu, k = meta >> 8;
+    uint32_t batch = c.p[P_SAMPLES_PER_DISPATCH];
+    PathState<LIGHT> st = loadState<LIGHT>(w, p);
+    for (;;) {
+        if (shadePath<LIGHT, false>(c, st, traceClosest(c, st.org, st.dir), depth, p) && depth + 1 < w.depth) {
+            depth++;
+            continue;
+        }
+        finishPath<LIGHT, A>(c, st, p);
+        if (k + 1 < batch && (c.p[P_ADAPTIVE] == 0 || pixelActive<A>(c, p))) {
+            k++;
+            depth = 0;
+            st = generatePathFor<LIGHT>(c, p % c.p[P_WIDTH], p / c.p[P_WIDTH], c.p[P_SAMPLE] + k);
+            continue;
+        }
+        break;
     }
 }
 

@@ -31,6 +31,15 @@ cudaError_t launch_stream_extend(bool stats, int blocks, cudaStream_t s, const v
 cudaError_t launch_stream_shade(Variant v, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
                                 uint32_t wave);
 int stream_shade_blocks_per_sm(Variant v);
+// Three-stage wave (lighting split off): shade without traversal, then the shadow stage.
+cudaError_t launch_stream_shade_deferred(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                                         uint32_t wave);
+cudaError_t launch_stream_shadow(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                                 uint32_t wave);
+int stream_deferred_blocks_per_sm(bool f64, int* shadow);
+// Finishes every slot still live after `wave` (at most max_slots of them) in one launch.
+cudaError_t launch_stream_tail(Variant v, uint32_t max_slots, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                               uint32_t wave);
 cudaError_t launch_trace_rays(int blocks, cudaStream_t s, const vgd::Ctx& c, const float* rays, uint4* out, uint32_t n,
                               uint32_t* fetch);
 cudaError_t launch_occlusion_rays(cudaStream_t s, const vgd::Ctx& c, const float* rays, uint32_t* out, uint32_t n);

@@ -797,10 +797,26 @@ static __device__ __forceinline__ void restirClear(const Ctx& c, uint32_t pixel)
 
 // ---------------------------------------------------------------------------------------------
 
+// The emitter / environment light sample of one bounce, whose visibility a later shadow stage
+// tests: if the segment from o along d up to tmax is unoccluded, c is added to the path's radiance.
+struct ShadowReq {
+    bool valid;
+    V3 o, d;
+    float tmax;
+    V3 c;
+};
+
 // pt_core.slang:992-1543: one bounce at `depth`. Returns false when the path ends here.
-template <bool LIGHT, bool RESTIR>
-__device__ bool shadePath(const Ctx& c, PathState<LIGHT>& st, Hit hq, uint32_t depth, uint32_t pixel)
+// DEFER (lighting split off only): the emitter / environment sample is not traced here but
+// returned in *req; it is the last contribution of the bounce, so adding it afterwards keeps the
+// order of the sums.
+template <bool LIGHT, bool RESTIR, bool DEFER = false>
+__device__ bool shadePath(const Ctx& c, PathState<LIGHT>& st, Hit hq, uint32_t depth, uint32_t pixel,
+                          ShadowReq* req = nullptr)
 {
+    static_assert(!(DEFER && LIGHT), "deferred shadow rays need the lighting split off");
+    if (DEFER)
+        req->valid = false;
     V3 sky = v3(pf(c, P_SKY), pf(c, P_SKY + 1), pf(c, P_SKY + 2));
     bool lightingOn = LIGHT && c.p[P_LIGHTING] != 0;
     uint32_t lightCount = c.p[P_LIGHT_COUNT];
@@ -1102,7 +1118,20 @@ __device__ bool shadePath(const Ctx& c, PathState<LIGHT>& st, Hit hq, uint32_t d
             V3 wi = toL / dist;
             float cosl = fabsf(dot(normalize(cross(b - a, cc - a)), wi));
             float cosi = dot(n, wi);
-            if (cosi > 0.0f && cosl > 1.0e-5f && (__float_as_uint(fget(E, e + 14)) & recvHere) != 0) {
+            if (DEFER && cosi > 0.0f && cosl > 1.0e-5f && (__float_as_uint(fget(E, e + 14)) & recvHere) != 0) {
+                // Deferred: the shadow stage tests visibility and adds c, as the last add of this bounce.
+                float pl = (1.0f - pEnv) * fget(E, e + 13) * d2 / (fget(E, e + 12) * cosl);
+                V3 wiL = v3(dot(wi, T), dot(wi, B), cosi);
+                float qb = reflectivePdf(surf, woL, wiL);
+                float wl = pl * pl / (pl * pl + qb * qb);
+                V3 lE = v3(fget(E, e + 9), fget(E, e + 10), fget(E, e + 11));
+                Lobes l = evalLobes(c, surf, woL, wiL);
+                req->valid = true;
+                req->o = p;
+                req->d = wi;
+                req->tmax = dist * (1.0f - 1.0e-3f);
+                req->c = thr * (l.specular + l.diffuse) * lE / pl * wl;
+            } else if (cosi > 0.0f && cosl > 1.0e-5f && (__float_as_uint(fget(E, e + 14)) & recvHere) != 0) {
                 bool occ = occluded(c, p, wi, dist * (1.0f - 1.0e-3f));
                 bool track = lightingOn && depth == 0;
                 if (!occ || track) {
@@ -1136,7 +1165,18 @@ __device__ bool shadePath(const Ctx& c, PathState<LIGHT>& st, Hit hq, uint32_t d
             V3 leE;
             V3 wi = envSample(c, u1e, u2e, u3e, u4e, pdfE, leE);
             float cosi = dot(n, wi);
-            if (pdfE > 0.0f && cosi > 0.0f) {
+            if (DEFER && pdfE > 0.0f && cosi > 0.0f) {
+                float pl = pEnvHere * pdfE;
+                V3 wiL = v3(dot(wi, T), dot(wi, B), cosi);
+                float qb = reflectivePdf(surf, woL, wiL);
+                float wl = pl * pl / (pl * pl + qb * qb);
+                Lobes l = evalLobes(c, surf, woL, wiL);
+                req->valid = true;
+                req->o = p;
+                req->d = wi;
+                req->tmax = 1.0e30f;
+                req->c = thr * (l.specular + l.diffuse) * leE / pl * wl;
+            } else if (pdfE > 0.0f && cosi > 0.0f) {
                 bool occ = occluded(c, p, wi, 1.0e30f);
                 bool track = lightingOn && depth == 0;
                 if (!occ || track) {

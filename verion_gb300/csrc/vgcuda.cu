@@ -138,6 +138,7 @@ struct VgRenderer {
     bool stage_timing = false;
     bool traversal_stats = false;
     int wavefront_mode = VG_WAVEFRONT_STREAMING;
+    uint32_t tail_threshold = 32768; // live slots at or below which the streaming tail runs in one launch
     bool adaptive = false;
     float adaptive_threshold = 0.02f;
     uint32_t adaptive_min_spp = 16;
@@ -147,6 +148,9 @@ struct VgRenderer {
     int extend_blocks = 0;
     int shade_blocks[8] = {};
     int stream_shade_blocks[8] = {};
+    int deferred_blocks[2] = {};
+    int shadow_blocks[2] = {};
+    bool defer_shadows = true; // streaming: shadow rays of the light sample in their own stage
 };
 
 struct VgAccum {
@@ -165,11 +169,13 @@ struct VgAccum {
     bool adaptive = false;
     Restir restir;               // captured at the first sample
     DevBuf re_g[2], re_n[2], re_x[2], re_m[2];
-    DevBuf state, hits, queue[2], counts, fetch, tstats, meta;
+    DevBuf state, hits, queue[2], counts, fetch, tstats, meta, sreq;
     uint32_t* host_counts = nullptr; // pinned ring of wave output counts (streaming wavefront)
     uint32_t last_waves = 0;
     std::vector<uint32_t> wave_live; // last streaming accumulate: live slots after each wave
     std::vector<float> wave_ms;      // with stage timing: extend, shade milliseconds per wave
+    float tail_ms = 0.0f;            // with stage timing: the tail launch of the last call
+    size_t wave_stages = 2;          // kernels per wave in wave_ms (2, or 3 with deferred shadows)
     ~VgAccum()
     {
         if (host_counts)
@@ -668,15 +674,34 @@ int vg_set_wavefront_mode(VgRenderer* r, int mode)
 
 uint32_t vg_accum_last_waves(const VgAccum* acc) { return acc ? acc->last_waves : 0; }
 
+int vg_set_stream_tail(VgRenderer* r, uint32_t threshold)
+{
+    if (!r)
+        return fail(VG_ERR_INVALID, "null renderer");
+    r->tail_threshold = threshold;
+    return VG_OK;
+}
+
+double vg_accum_tail_seconds(const VgAccum* acc) { return acc ? acc->tail_ms * 1e-3 : 0.0; }
+
+int vg_set_deferred_shadows(VgRenderer* r, int on)
+{
+    if (!r)
+        return fail(VG_ERR_INVALID, "null renderer");
+    r->defer_shadows = on != 0;
+    return VG_OK;
+}
+
 size_t vg_accum_wave_profile(const VgAccum* acc, float* out, size_t waves)
 {
     if (!acc)
         return 0;
     size_t n = std::min(waves, acc->wave_live.size());
+    size_t per = acc->wave_stages;
     for (size_t k = 0; out && k < n; k++) {
-        out[3 * k] = (float)acc->wave_live[k];
-        out[3 * k + 1] = 2 * k + 1 < acc->wave_ms.size() ? acc->wave_ms[2 * k] : 0.0f;
-        out[3 * k + 2] = 2 * k + 1 < acc->wave_ms.size() ? acc->wave_ms[2 * k + 1] : 0.0f;
+        out[4 * k] = (float)acc->wave_live[k];
+        for (size_t j = 0; j < 3; j++)
+            out[4 * k + 1 + j] = j < per && per * k + j < acc->wave_ms.size() ? acc->wave_ms[per * k + j] : 0.0f;
     }
     return acc->wave_live.size();
 }
@@ -821,7 +846,8 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
             (st = alloc(acc->counts, (max_depth_alloc + 1) * 4, s, true)) != VG_OK ||
             (st = alloc(acc->fetch, 2 * (max_depth_alloc + 1) * 4, s, true)) != VG_OK ||
             (st = alloc(acc->tstats, 4 * 8, s, true)) != VG_OK ||
-            (st = alloc(acc->meta, px * 4, s, false)) != VG_OK)
+            (st = alloc(acc->meta, px * 4, s, false)) != VG_OK ||
+            (st = alloc(acc->sreq, acc->lighting ? 16 : px * 3 * 16, s, false)) != VG_OK)
             return st;
         if (!acc->host_counts && cudaHostAlloc((void**)&acc->host_counts, 64 * 4, cudaHostAllocDefault) != cudaSuccess) {
             acc->host_counts = nullptr;
@@ -874,10 +900,20 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
             streamed = true;
             acc->wave_live.clear();
             acc->wave_ms.clear();
+            acc->tail_ms = 0.0f;
             int svi = v.index() & 5;
             if (r->stream_shade_blocks[svi] == 0)
                 r->stream_shade_blocks[svi] = vgx::stream_shade_blocks_per_sm(v);
             int ssb = blocks_for(r, r->stream_shade_blocks[svi]);
+            // Lighting split off: three-stage waves with the shadow rays in their own kernel.
+            bool deferred = !acc->lighting && r->defer_shadows;
+            if (deferred && r->deferred_blocks[v.f64 ? 1 : 0] == 0)
+                r->deferred_blocks[v.f64 ? 1 : 0] =
+                    vgx::stream_deferred_blocks_per_sm(v.f64, &r->shadow_blocks[v.f64 ? 1 : 0]);
+            int dsb = blocks_for(r, r->deferred_blocks[v.f64 ? 1 : 0]);
+            int shb = blocks_for(r, r->shadow_blocks[v.f64 ? 1 : 0]);
+            w.sreq = (float4*)acc->sreq.p;
+            acc->wave_stages = deferred ? 3 : 2;
             c.p[P_SAMPLE] = acc->samples;
             c.p[P_SAMPLES_PER_DISPATCH] = samples;
             VG_CHECK(cudaMemsetAsync(acc->counts.p, 0, 2 * 4, s), "counters");
@@ -905,13 +941,30 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
                 VG_CHECK(vgx::launch_stream_extend(r->traversal_stats, eb, s, c, w, (uint32_t)wave), "extend launch");
                 if (timed)
                     VG_CHECK(cudaEventRecord(m, s), "event");
-                VG_CHECK(vgx::launch_stream_shade(v, ssb, s, c, w, (uint32_t)wave), "shade launch");
-                if (timed) {
-                    VG_CHECK(cudaEventRecord(b, s), "event");
-                    stages.push_back({0, {a, m}});
-                    stages.push_back({1, {m, b}});
+                if (deferred) {
+                    VG_CHECK(vgx::launch_stream_shade_deferred(v.f64, dsb, s, c, w, (uint32_t)wave), "shade launch");
+                    cudaEvent_t q = nullptr;
+                    if (timed) {
+                        q = pool.get();
+                        VG_CHECK(cudaEventRecord(q, s), "event");
+                    }
+                    VG_CHECK(vgx::launch_stream_shadow(v.f64, shb, s, c, w, (uint32_t)wave), "shadow launch");
+                    if (timed) {
+                        VG_CHECK(cudaEventRecord(b, s), "event");
+                        stages.push_back({0, {a, m}});
+                        stages.push_back({1, {m, q}});
+                        stages.push_back({3, {q, b}});
+                    }
+                    acc->launches += 3;
+                } else {
+                    VG_CHECK(vgx::launch_stream_shade(v, ssb, s, c, w, (uint32_t)wave), "shade launch");
+                    if (timed) {
+                        VG_CHECK(cudaEventRecord(b, s), "event");
+                        stages.push_back({0, {a, m}});
+                        stages.push_back({1, {m, b}});
+                    }
+                    acc->launches += 2;
                 }
-                acc->launches += 2;
                 uint32_t slot = (uint32_t)(wave % RING);
                 VG_CHECK(cudaMemcpyAsync(&ring[slot], (uint32_t*)acc->counts.p + ((wave + 1) & 1u), 4,
                                          cudaMemcpyDeviceToHost, s),
@@ -921,8 +974,25 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
                     uint32_t old = (uint32_t)((wave - LAG) % RING);
                     if ((st = wait_event(ring_ev[old])) != VG_OK)
                         return st;
-                    done = ring[old] == 0;
-                    acc->wave_live.push_back(ring[old]);
+                    uint32_t live = ring[old];
+                    done = live == 0;
+                    acc->wave_live.push_back(live);
+                    if (!done && live <= r->tail_threshold) {
+                        // Few slots left: finish them in one launch (the queue after this wave).
+                        cudaEvent_t a = nullptr, b = nullptr;
+                        if (timed) {
+                            a = pool.get();
+                            b = pool.get();
+                            VG_CHECK(cudaEventRecord(a, s), "event");
+                        }
+                        VG_CHECK(vgx::launch_stream_tail(v, live, s, c, w, (uint32_t)(wave + 1)), "tail launch");
+                        if (timed) {
+                            VG_CHECK(cudaEventRecord(b, s), "event");
+                            stages.push_back({2, {a, b}});
+                        }
+                        acc->launches++;
+                        done = true;
+                    }
                 }
             }
             acc->last_waves = (uint32_t)wave;
@@ -977,8 +1047,10 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
         for (auto& sp : stages) {
             float sm = 0.0f;
             VG_CHECK(cudaEventElapsedTime(&sm, sp.second.first, sp.second.second), "event");
-            acc->stage_seconds[sp.first] += sm * 1e-3;
-            if (streamed)
+            acc->stage_seconds[sp.first >= 2 ? 1 : sp.first] += sm * 1e-3;
+            if (sp.first == 2)
+                acc->tail_ms = sm;
+            else if (streamed)
                 acc->wave_ms.push_back(sm);
             if (sp.first == 0)
                 acc->extend_launches_timed++;
