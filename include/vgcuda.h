@@ -218,6 +218,15 @@ uint64_t vg_accum_launches(const VgAccum* acc);
 /* Average duration in seconds of one extend-kernel launch, from stage timing (0 if none). */
 double vg_accum_extend_launch_seconds(const VgAccum* acc);
 
+/* RayTracingBackend::render_normals (lib.rs:55): world-space normal of the first hit through each
+ * pixel centre, facing the viewer, 3 floats per pixel into host memory; misses are zero. */
+int vg_render_normals(VgRenderer* r, uint32_t width, uint32_t height, float* out);
+/* RayTracingBackend::render_aovs (lib.rs:57, Aovs lib.rs:165-181), host arrays of width * height:
+ * albedo (3 floats) and depth along the camera's forward axis (1 float) per pixel, instance + 1,
+ * material + 1 (0 on a miss), and coverage of 16 stratified rays through translucent surfaces. */
+int vg_render_aovs(VgRenderer* r, uint32_t width, uint32_t height, float* albedo_depth, uint32_t* object_id,
+                   uint32_t* material_id, float* coverage);
+
 /* Traversal entry points (no reference counterpart; the reference's traversal is the driver's).
  * Closest hits of n rays (6 floats each: origin xyz, direction xyz, host memory) into 4 words per
  * ray (hit flag, instance, primitive, t bits) as the wavefront's hit record (wf_extend.slang:26-29). */

@@ -87,6 +87,8 @@ def lib() -> C.CDLL:
         for name in ("or_atan2f", "or_powf"):
             getattr(L, name).restype = C.c_float
             getattr(L, name).argtypes = [C.c_float, C.c_float]
+        L.or_render_normals.argtypes = [vp, vp, vp, C.c_int]
+        L.or_render_aovs.argtypes = [vp, vp, vp, vp, vp, vp, C.c_int]
         L.or_pcg.restype = C.c_uint32
         L.or_pcg.argtypes = [C.c_uint32]
         _lib = L
@@ -144,6 +146,25 @@ class OracleScene:
         out = np.zeros(len(r), np.uint32)
         lib().or_trace_occluded(self._h, _ptr(r), len(r), _ptr(out), threads or default_threads())
         return out
+
+    def render_normals(self, camera18: np.ndarray, threads: int = 0) -> np.ndarray:
+        """shaders/normals.slang: (pixels, 3) first-hit normals facing the viewer."""
+        cam = np.ascontiguousarray(camera18, np.float32)
+        n = int(cam[0]) * int(cam[1])
+        out = np.zeros(3 * n, np.float32)
+        lib().or_render_normals(self._h, _ptr(cam), _ptr(out), threads or default_threads())
+        return out.reshape(-1, 3)
+
+    def render_aovs(self, camera18: np.ndarray, threads: int = 0):
+        """shaders/aov.slang: albedo + depth (pixels, 4), object ids, material ids, coverage."""
+        cam = np.ascontiguousarray(camera18, np.float32)
+        n = int(cam[0]) * int(cam[1])
+        ad = np.zeros(4 * n, np.float32)
+        oi = np.zeros(n, np.uint32)
+        mi = np.zeros(n, np.uint32)
+        cv = np.zeros(n, np.float32)
+        lib().or_render_aovs(self._h, _ptr(cam), _ptr(ad), _ptr(oi), _ptr(mi), _ptr(cv), threads or default_threads())
+        return ad.reshape(-1, 4), oi, mi, cv
 
     def __del__(self):
         try:

@@ -1818,6 +1818,146 @@ int or_render(void* s, const uint32_t* params_in, uint32_t sample_base, uint32_t
     return 0;
 }
 
+// shaders/normals.slang:41-110: camera18 is the camera record (pack.rs:97-108).
+void or_render_normals(void* s, const float* cam, float* out, int threads)
+{
+    const Tables& T = *(const Tables*)s;
+    uint32_t params[43] = {};
+    Job<float> J{&T, params, nullptr, nullptr, nullptr, nullptr, false, false};
+    PT<float> pt{T, params, J};
+    uint32_t w = (uint32_t)cam[0], h = (uint32_t)cam[1];
+    parallel_for(w * h, threads, [&](uint32_t pix) {
+        uint32_t x = pix % w, y = pix / w;
+        float t = cam[2];
+        float aspect = cam[0] / cam[1];
+        float u = (2.0f * ((float)x + 0.5f) / (float)w - 1.0f + cam[16]) * aspect * t;
+        float v = (1.0f - 2.0f * ((float)y + 0.5f) / (float)h + cam[17]) * t;
+        V<float> d = normalize(V<float>(u, v, -1.0f));
+        float dr[3], orr[3];
+        for (int r = 0; r < 3; r++) {
+            dr[r] = cam[4 + 4 * r] * d.x + cam[5 + 4 * r] * d.y + cam[6 + 4 * r] * d.z;
+            orr[r] = cam[7 + 4 * r];
+        }
+        V<float> org(orr[0], orr[1], orr[2]);
+        V<float> dir = normalize(V<float>(dr[0], dr[1], dr[2]));
+        HitRec<float> q = pt.traceClosest(org, dir);
+        V<float> n;
+        if (q.hit) {
+            uint32_t inst = q.inst * 16;
+            uint32_t tri = T.instances[inst + 1] + 3 * q.prim;
+            uint32_t vo = T.instances[inst];
+            uint32_t i0 = T.indices[tri] + vo, i1 = T.indices[tri + 1] + vo, i2 = T.indices[tri + 2] + vo;
+            V<float> p0 = pt.transformPoint(inst + 4, pt.vertexPos(i0));
+            V<float> p1 = pt.transformPoint(inst + 4, pt.vertexPos(i1));
+            V<float> p2 = pt.transformPoint(inst + 4, pt.vertexPos(i2));
+            V<float> ng = normalize(cross(p1 - p0, p2 - p0));
+            n = ng;
+            V<float> e1 = p1 - p0, e2 = p2 - p0, e3 = org + dir * q.t - p0;
+            float d11 = dot(e1, e1), d12 = dot(e1, e2), d22 = dot(e2, e2);
+            float den = std::fmax(d11 * d22 - d12 * d12, 1.0e-20f);
+            float b1 = (d22 * dot(e3, e1) - d12 * dot(e3, e2)) / den;
+            float b2 = (d11 * dot(e3, e2) - d12 * dot(e3, e1)) / den;
+            V<float> nsObj = (1.0f - b1 - b2) * pt.vertexNormal(i0) + b1 * pt.vertexNormal(i1) + b2 * pt.vertexNormal(i2);
+            if (dot(nsObj, nsObj) > 1.0e-12f) {
+                n = normalize(pt.transformNormal(inst + 4, nsObj));
+                if (dot(n, ng) < 0.0f)
+                    n = -n;
+            }
+            if (dot(ng, dir) > 0.0f)
+                n = -n;
+        }
+        out[3 * pix] = n.x;
+        out[3 * pix + 1] = n.y;
+        out[3 * pix + 2] = n.z;
+    });
+}
+
+// shaders/aov.slang:86-188
+void or_render_aovs(void* s, const float* cam, float* albedo_depth, uint32_t* object_ids, uint32_t* material_ids,
+                    float* coverage, int threads)
+{
+    const Tables& T = *(const Tables*)s;
+    uint32_t params[43] = {};
+    Job<float> J{&T, params, nullptr, nullptr, nullptr, nullptr, false, false};
+    PT<float> pt{T, params, J};
+    uint32_t w = (uint32_t)cam[0], h = (uint32_t)cam[1];
+    float t = cam[2];
+    float aspect = cam[0] / cam[1];
+    auto pixelDir = [&](float px, float py, V<float>& dir) {
+        float u = (2.0f * px / (float)w - 1.0f + cam[16]) * aspect * t;
+        float v = (1.0f - 2.0f * py / (float)h + cam[17]) * t;
+        V<float> d = normalize(V<float>(u, v, -1.0f));
+        float r[3];
+        for (int k = 0; k < 3; k++)
+            r[k] = cam[4 + 4 * k] * d.x + cam[5 + 4 * k] * d.y + cam[6 + 4 * k] * d.z;
+        dir = V<float>(r[0], r[1], r[2]);
+        return d;
+    };
+    parallel_for(w * h, threads, [&](uint32_t pix) {
+        uint32_t x = pix % w, y = pix / w;
+        V<float> org(cam[7], cam[11], cam[15]);
+        V<float> dir;
+        V<float> d = pixelDir((float)x + 0.5f, (float)y + 0.5f, dir);
+        dir = normalize(dir);
+        HitRec<float> q = pt.traceClosest(org, dir);
+        V<float> albedo;
+        float depth = 0.0f;
+        uint32_t id = 0, matId = 0;
+        if (q.hit) {
+            uint32_t inst = q.inst * 16;
+            uint32_t tri = T.instances[inst + 1] + 3 * q.prim;
+            uint32_t vo = T.instances[inst];
+            id = q.inst + 1;
+            matId = T.instances[inst + 2] + 1;
+            depth = q.t * -d.z;
+            uint32_t mi = T.instances[inst + 2] * 24;
+            albedo = V<float>(T.materials[mi], T.materials[mi + 1], T.materials[mi + 2]);
+            uint32_t texBase = (uint32_t)T.materials[mi + 10];
+            if (texBase > 0) {
+                uint32_t i0 = T.indices[tri] + vo, i1 = T.indices[tri + 1] + vo, i2 = T.indices[tri + 2] + vo;
+                V<float> p0 = pt.transformPoint(inst + 4, pt.vertexPos(i0));
+                V<float> p1 = pt.transformPoint(inst + 4, pt.vertexPos(i1));
+                V<float> p2 = pt.transformPoint(inst + 4, pt.vertexPos(i2));
+                V<float> e1 = p1 - p0, e2 = p2 - p0, e3 = org + dir * q.t - p0;
+                float d11 = dot(e1, e1), d12 = dot(e1, e2), d22 = dot(e2, e2);
+                float den = std::fmax(d11 * d22 - d12 * d12, 1.0e-20f);
+                float b1 = (d22 * dot(e3, e1) - d12 * dot(e3, e2)) / den;
+                float b2 = (d11 * dot(e3, e2) - d12 * dot(e3, e1)) / den;
+                float u0x = T.uvs[2 * i0], u0y = T.uvs[2 * i0 + 1], u1x = T.uvs[2 * i1], u1y = T.uvs[2 * i1 + 1];
+                float u2x = T.uvs[2 * i2], u2y = T.uvs[2 * i2 + 1];
+                float ux = u0x + b1 * (u1x - u0x) + b2 * (u2x - u0x);
+                float uy = u0y + b1 * (u1y - u0y) + b2 * (u2y - u0y);
+                uint32_t ti = (texBase - 1) * 4;
+                albedo = albedo * pt.bilinear(T.tex_info[ti], T.tex_info[ti + 1], T.tex_info[ti + 2], ux, uy);
+            }
+        }
+        float cover = 0.0f;
+        for (uint32_t k = 0; k < 16; k++) {
+            V<float> sdir;
+            pixelDir((float)x + ((float)(k % 4) + 0.5f) / 4.0f, (float)y + ((float)(k / 4) + 0.5f) / 4.0f, sdir);
+            V<float> so = org, sd = normalize(sdir);
+            float seen = 0.0f, through = 1.0f;
+            for (uint32_t layer = 0; layer < 8 && through > 0.0f; layer++) {
+                QHit<float> sq = trace<float>(T, so, sd, 1.0e30f, false, false);
+                if (!sq.hit)
+                    break;
+                float op = pt.opacityAt(sq.inst, sq.prim, sq.b1, sq.b2);
+                seen += through * op;
+                through *= 1.0f - op;
+                so = so + sd * (sq.t + 1.0e-4f);
+            }
+            cover += seen;
+        }
+        coverage[pix] = cover / 16.0f;
+        albedo_depth[4 * pix] = albedo.x;
+        albedo_depth[4 * pix + 1] = albedo.y;
+        albedo_depth[4 * pix + 2] = albedo.z;
+        albedo_depth[4 * pix + 3] = depth;
+        object_ids[pix] = id;
+        material_ids[pix] = matId;
+    });
+}
+
 // Elementary functions, exported so the tests can bound their error against double precision.
 float or_sinf(float x) { return vgm::sinf_(x); }
 float or_cosf(float x) { return vgm::cosf_(x); }

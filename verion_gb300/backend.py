@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+from dataclasses import dataclass
 from enum import IntEnum
 from pathlib import Path
 from typing import Optional
@@ -146,6 +147,8 @@ def lib() -> C.CDLL:
             "vg_accum_launches": (C.c_uint64, [vp]),
             "vg_accum_read_queue_counts": (i32, [vp, vp, _S]),
             "vg_accum_extend_launch_seconds": (f64, [vp]),
+            "vg_render_normals": (i32, [vp, u32, u32, vp]),
+            "vg_render_aovs": (i32, [vp, u32, u32, vp, vp, vp, vp]),
             "vg_trace_closest": (i32, [vp, vp, _S, vp]),
             "vg_trace_occluded": (i32, [vp, vp, _S, vp]),
             "vg_trace_closest_device": (i32, [vp, vp, _S, vp, C.POINTER(f64)]),
@@ -180,6 +183,16 @@ def _view(v: View) -> _View:
     out.focus = v.focus
     out.shift[:] = [float(v.shift[0]), float(v.shift[1])]
     return out
+
+
+@dataclass
+class Aovs:
+    """lib.rs:165-181: primary-ray AOVs, row-major from the top-left; misses are zero."""
+    albedo: np.ndarray       # (pixels, 3)
+    depth: np.ndarray        # (pixels,) distance along the camera's forward axis
+    object_id: np.ndarray    # instance index + 1
+    material_id: np.ndarray  # material index + 1
+    coverage: np.ndarray     # fraction of 16 stratified rays that hit
 
 
 class Context:
@@ -439,6 +452,24 @@ class Renderer:
         acc = self.new_accumulation(width, height, False)
         self.accumulate(acc, samples)
         return acc.mean()
+
+    def render_normals(self, width: int, height: int) -> np.ndarray:
+        """RayTracingBackend::render_normals: (pixels, 3) first-hit normals, misses zero."""
+        out = np.empty(3 * width * height, np.float32)
+        _check(lib().vg_render_normals(self._h, width, height, out.ctypes.data))
+        return out.reshape(-1, 3)
+
+    def render_aovs(self, width: int, height: int) -> "Aovs":
+        """RayTracingBackend::render_aovs (lib.rs:165-181)."""
+        n = width * height
+        ad = np.empty(4 * n, np.float32)
+        oi = np.empty(n, np.uint32)
+        mi = np.empty(n, np.uint32)
+        cv = np.empty(n, np.float32)
+        _check(lib().vg_render_aovs(self._h, width, height, ad.ctypes.data, oi.ctypes.data, mi.ctypes.data,
+                                    cv.ctypes.data))
+        ad = ad.reshape(-1, 4)
+        return Aovs(ad[:, :3].copy(), ad[:, 3].copy(), oi, mi, cv)
 
     # Traversal entry points
     def trace_closest(self, rays: np.ndarray) -> np.ndarray:

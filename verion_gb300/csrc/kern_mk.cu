@@ -26,3 +26,32 @@ cudaError_t launch_megakernel(Variant v, dim3 grid, cudaStream_t s, const vgd::C
 }
 
 } // namespace vgx
+
+#include "aov.cuh"
+
+namespace vgx {
+
+cudaError_t launch_aov_normals(cudaStream_t s, const vgd::Ctx& c, const float* camera18, float* out)
+{
+    vga::CameraRecord cam;
+    for (int i = 0; i < 18; i++)
+        cam.v[i] = camera18[i];
+    uint32_t w = (uint32_t)cam.v[0], h = (uint32_t)cam.v[1];
+    dim3 grid((w + 15) / 16, (h + 7) / 8);
+    vga::aov_normals<<<grid, 128, 0, s>>>(c, cam, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_aov_main(cudaStream_t s, const vgd::Ctx& c, const float* camera18, float* albedo_depth,
+                            uint32_t* object_ids, uint32_t* material_ids, float* coverage)
+{
+    vga::CameraRecord cam;
+    for (int i = 0; i < 18; i++)
+        cam.v[i] = camera18[i];
+    uint32_t w = (uint32_t)cam.v[0], h = (uint32_t)cam.v[1];
+    dim3 grid((w + 15) / 16, (h + 7) / 8);
+    vga::aov_main<<<grid, 128, 0, s>>>(c, cam, albedo_depth, object_ids, material_ids, coverage);
+    return cudaGetLastError();
+}
+
+} // namespace vgx

@@ -40,6 +40,10 @@ int stream_deferred_blocks_per_sm(bool f64, int* shadow);
 // Finishes every slot still live after `wave` (at most max_slots of them) in one launch.
 cudaError_t launch_stream_tail(Variant v, uint32_t max_slots, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
                                uint32_t wave);
+// Primary-hit AOVs (normals.slang, aov.slang); camera18 is the reference's camera record.
+cudaError_t launch_aov_normals(cudaStream_t s, const vgd::Ctx& c, const float* camera18, float* out);
+cudaError_t launch_aov_main(cudaStream_t s, const vgd::Ctx& c, const float* camera18, float* albedo_depth,
+                            uint32_t* object_ids, uint32_t* material_ids, float* coverage);
 cudaError_t launch_trace_rays(int blocks, cudaStream_t s, const vgd::Ctx& c, const float* rays, uint4* out, uint32_t n,
                               uint32_t* fetch);
 cudaError_t launch_occlusion_rays(cudaStream_t s, const vgd::Ctx& c, const float* rays, uint32_t* out, uint32_t n);

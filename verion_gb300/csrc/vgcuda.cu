@@ -1185,6 +1185,67 @@ int vg_accum_read_queue_counts(const VgAccum* acc, uint32_t* out, size_t len)
     return read_dev(acc, acc->counts, out, (acc->last_depth + 1) * 4);
 }
 
+// pack.rs:97-108 View::camera_record
+static void camera_record(const VgRenderer* r, uint32_t w, uint32_t h, float* rec)
+{
+    for (int i = 0; i < 16; i++)
+        rec[i] = r->view.camera[i];
+    rec[0] = (float)w;
+    rec[1] = (float)h;
+    rec[16] = r->view.shift[0];
+    rec[17] = r->view.shift[1];
+}
+
+int vg_render_normals(VgRenderer* r, uint32_t width, uint32_t height, float* out)
+{
+    if (!r || !out)
+        return fail(VG_ERR_INVALID, "null argument");
+    if (width == 0 || height == 0)
+        return fail(VG_ERR_SCENE, "image size must be non-zero");
+    size_t px = (size_t)width * height;
+    cudaStream_t s = r->ctx->stream;
+    DevBuf d;
+    int st;
+    if ((st = alloc(d, px * 12, s, false)) != VG_OK)
+        return st;
+    float rec[18];
+    camera_record(r, width, height, rec);
+    vgd::Ctx c = make_ctx(r, nullptr);
+    VG_CHECK(cudaMemsetAsync(r->err.p, 0, 4, s), "error flag");
+    VG_CHECK(vgx::launch_aov_normals(s, c, rec, (float*)d.p), "normals launch");
+    VG_CHECK(cudaMemcpyAsync(out, d.p, px * 12, cudaMemcpyDeviceToHost, s), "readback");
+    VG_CHECK(cudaStreamSynchronize(s), "normals");
+    return read_err(r);
+}
+
+int vg_render_aovs(VgRenderer* r, uint32_t width, uint32_t height, float* albedo_depth, uint32_t* object_id,
+                   uint32_t* material_id, float* coverage)
+{
+    if (!r || !albedo_depth || !object_id || !material_id || !coverage)
+        return fail(VG_ERR_INVALID, "null argument");
+    if (width == 0 || height == 0)
+        return fail(VG_ERR_SCENE, "image size must be non-zero");
+    size_t px = (size_t)width * height;
+    cudaStream_t s = r->ctx->stream;
+    DevBuf ad, oi, mi, cv;
+    int st;
+    if ((st = alloc(ad, px * 16, s, false)) != VG_OK || (st = alloc(oi, px * 4, s, false)) != VG_OK ||
+        (st = alloc(mi, px * 4, s, false)) != VG_OK || (st = alloc(cv, px * 4, s, false)) != VG_OK)
+        return st;
+    float rec[18];
+    camera_record(r, width, height, rec);
+    vgd::Ctx c = make_ctx(r, nullptr);
+    VG_CHECK(cudaMemsetAsync(r->err.p, 0, 4, s), "error flag");
+    VG_CHECK(vgx::launch_aov_main(s, c, rec, (float*)ad.p, (uint32_t*)oi.p, (uint32_t*)mi.p, (float*)cv.p),
+             "aov launch");
+    VG_CHECK(cudaMemcpyAsync(albedo_depth, ad.p, px * 16, cudaMemcpyDeviceToHost, s), "readback");
+    VG_CHECK(cudaMemcpyAsync(object_id, oi.p, px * 4, cudaMemcpyDeviceToHost, s), "readback");
+    VG_CHECK(cudaMemcpyAsync(material_id, mi.p, px * 4, cudaMemcpyDeviceToHost, s), "readback");
+    VG_CHECK(cudaMemcpyAsync(coverage, cv.p, px * 4, cudaMemcpyDeviceToHost, s), "readback");
+    VG_CHECK(cudaStreamSynchronize(s), "aovs");
+    return read_err(r);
+}
+
 int vg_trace_closest_device(VgRenderer* r, const float* d_rays, size_t n, uint32_t* d_hits, double* seconds)
 {
     if (!r || (n > 0 && (!d_rays || !d_hits)))

@@ -77,6 +77,15 @@ class View:
         return View(c, float(cam.aperture_radius), float(cam.focus_distance), tuple(cam.shift))
 
 
+def camera_record(view: "View", width: int, height: int) -> np.ndarray:
+    """pack.rs:97-108: the camera record of the normal and AOV kernels."""
+    rec = np.zeros(18, np.float32)
+    rec[:16] = view.camera
+    rec[0], rec[1] = width, height
+    rec[16:] = view.shift
+    return rec
+
+
 @dataclass
 class Packed:
     positions: np.ndarray
