@@ -360,7 +360,7 @@ def run_cuda(args):
         rays1 = s1["rays_after_depth0"] - s0["rays_after_depth0"]
         node_b, tri_b = 80, 48
         alg_bytes = 20 * rays + 24 * rays1 + node_b * nodes + tri_b * tests
-        extend_launches = args.steps * SPP_STEP * DEPTH
+        extend_launches = max(1, int(round(stage[0] / extend_launch_s)))  # launches in the timed steps
         per_launch_bytes = alg_bytes / extend_launches
         achieved = per_launch_bytes / extend_launch_s / 1e9
         tpr, tsrc = traffic_per_ray()

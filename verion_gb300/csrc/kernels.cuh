@@ -24,7 +24,7 @@ constexpr uint32_t FULL = 0xffffffffu;
 
 // Minimum resident 128-thread blocks per SM requested for the shade kernels (a register cap).
 #ifndef VG_SHADE_MIN_BLOCKS
-#define VG_SHADE_MIN_BLOCKS 3
+#define VG_SHADE_MIN_BLOCKS 4
 #endif
 
 // State planes (16 bytes each, plane k of path p at state[k * N + p]):
