@@ -167,6 +167,9 @@ int vg_set_stream_tail(VgRenderer* r, uint32_t threshold);
 /* Streaming mode without the lighting split: trace the bounce's emitter / environment shadow ray
  * in a separate stage after shade (default on) or inline in shade (off). Same sums either way. */
 int vg_set_deferred_shadows(VgRenderer* r, int on);
+/* Streaming mode: the extend and shadow stages refill a warp's idle lanes with queued rays
+ * (default on) or give each warp 32 rays at a time (off). Same results either way. */
+int vg_set_dynamic_fetch(VgRenderer* r, int on);
 /* With stage timing: seconds of the last call's tail launch (0 if none ran). */
 double vg_accum_tail_seconds(const VgAccum* acc);
 /* Streaming mode: waves (extend + shade pairs) issued by the last vg_accumulate. */

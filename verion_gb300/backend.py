@@ -129,6 +129,7 @@ def lib() -> C.CDLL:
             "vg_set_stream_tail": (i32, [vp, u32]),
             "vg_accum_tail_seconds": (f64, [vp]),
             "vg_set_deferred_shadows": (i32, [vp, i32]),
+            "vg_set_dynamic_fetch": (i32, [vp, i32]),
             "vg_accum_traversal_stats": (i32, [vp, C.POINTER(C.c_uint64)]),
             "vg_set_accum_precision": (i32, [vp, i32]),
             "vg_accum_create": (i32, [vp, u32, u32, i32, C.POINTER(vp)]),
@@ -418,6 +419,9 @@ class Renderer:
 
     def set_wavefront_mode(self, mode: "WavefrontMode") -> None:
         _check(lib().vg_set_wavefront_mode(self._h, int(mode)))
+
+    def set_dynamic_fetch(self, on: bool) -> None:
+        _check(lib().vg_set_dynamic_fetch(self._h, int(on)))
 
     def set_deferred_shadows(self, on: bool) -> None:
         _check(lib().vg_set_deferred_shadows(self._h, int(on)))

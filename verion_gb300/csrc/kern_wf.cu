@@ -219,3 +219,33 @@ int stream_deferred_blocks_per_sm(bool f64, int* shadow)
 }
 
 } // namespace vgx
+
+namespace vgx {
+
+cudaError_t launch_stream_extend_dyn(bool stats, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                                     uint32_t wave)
+{
+    if (stats)
+        vgk::wf_stream_extend_dyn<true><<<blocks, 128, 0, s>>>(c, w, wave);
+    else
+        vgk::wf_stream_extend_dyn<false><<<blocks, 128, 0, s>>>(c, w, wave);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_shadow_trace(int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w, uint32_t wave)
+{
+    vgk::wf_stream_shadow_trace<<<blocks, 128, 0, s>>>(c, w, wave);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_finish(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                                 uint32_t wave)
+{
+    if (f64)
+        vgk::wf_stream_finish<double><<<blocks, 128, 0, s>>>(c, w, wave);
+    else
+        vgk::wf_stream_finish<float><<<blocks, 128, 0, s>>>(c, w, wave);
+    return cudaGetLastError();
+}
+
+} // namespace vgx

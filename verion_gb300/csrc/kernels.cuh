@@ -513,6 +513,140 @@ __global__ void __launch_bounds__(128, 8) wf_stream_shadow(const __grid_constant
     }
 }
 
+// Dynamic-fetch forms of the streaming extend and shadow stages (vgt::trace_queue). Refill when
+// at least VG_REFILL lanes of a warp are idle; at most VG_STEPS node visits between refills.
+#ifndef VG_REFILL
+#define VG_REFILL 16
+#endif
+#ifndef VG_STEPS
+#define VG_STEPS 4
+#endif
+
+template <bool STATS>
+__global__ void __launch_bounds__(128, 8) wf_stream_extend_dyn(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
+{
+    uint32_t in = wave & 1u, out = in ^ 1u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        w.counts[out] = 0;
+        w.fetch[2 + in] = 0;
+        w.fetch[4 + in] = 0;
+        w.fetch[6 + in] = 0;
+    }
+    uint32_t count = w.counts[in];
+    const uint32_t* qin = w.queue[in];
+    uint32_t n_rays = 0, n_nodes = 0, n_tests = 0, n_later = 0;
+    vgt::trace_queue<false, VG_REFILL, VG_STEPS>(
+        c.s.nodes, c.s.tris, &w.fetch[in], count, c.err,
+        [&](uint32_t i, V3& o, V3& d, float& tmax) {
+            uint32_t p = qin[i];
+            float4 a = w.state[p];
+            float4 b = w.state[w.n + p];
+            o = v3(a.x, a.y, a.z);
+            d = v3(b.x, b.y, b.z);
+            tmax = 1.0e30f;
+            return true;
+        },
+        [&](uint32_t i, const vgt::TraceHit& q) {
+            uint32_t p = qin[i];
+            w.hits[p] = make_uint4(q.hit ? 1u : 0u, q.hit ? q.inst : 0u, q.hit ? q.prim : 0u,
+                                   __float_as_uint(q.hit ? q.t : 0.0f));
+            if (STATS) {
+                n_rays++;
+                n_nodes += q.nodes;
+                n_tests += q.tests;
+                n_later += (w.meta[p] & 0xffu) != 0 ? 1u : 0u;
+            }
+        });
+    if (STATS) {
+        warp_count(&w.tstats[0], n_rays);
+        warp_count(&w.tstats[1], n_nodes);
+        warp_count(&w.tstats[2], n_tests);
+        warp_count(&w.tstats[3], n_later);
+    }
+}
+
+// Shadow rays of the deferred light samples, any hit (opaque scenes: one layer, no opacity roll).
+// The result goes to hits[p].x (1 occluded), which the finish stage reads.
+__global__ void __launch_bounds__(128, 8) wf_stream_shadow_trace(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
+{
+    uint32_t in = wave & 1u;
+    uint32_t count = w.counts[in];
+    const uint32_t* qin = w.queue[in];
+    uint32_t n = w.n;
+    vgt::trace_queue<true, VG_REFILL, VG_STEPS>(
+        c.s.nodes, c.s.tris, &w.fetch[4 + in], count, c.err,
+        [&](uint32_t i, V3& o, V3& d, float& tmax) {
+            uint32_t p = qin[i];
+            float4 r1 = w.sreq[n + p];
+            if (!(__float_as_uint(r1.w) & 1u)) {
+                tmax = 0.0f;
+                return false;
+            }
+            float4 r0 = w.sreq[p];
+            o = v3(r0.x, r0.y, r0.z);
+            d = v3(r1.x, r1.y, r1.z);
+            tmax = r0.w;
+            return true;
+        },
+        [&](uint32_t i, const vgt::TraceHit& q) { ((uint32_t*)w.hits)[4 * (size_t)qin[i]] = q.hit ? 1u : 0u; });
+}
+
+// After the shadow trace: add the unoccluded light sample, then queue, finish or restart each slot
+// (the second half of wf_stream_shadow).
+template <typename A>
+__global__ void __launch_bounds__(128, 8) wf_stream_finish(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
+{
+    uint32_t in = wave & 1u, out = in ^ 1u;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        w.fetch[out] = 0;
+    uint32_t count = w.counts[in];
+    const uint32_t* qin = w.queue[in];
+    uint32_t* qout = w.queue[out];
+    uint32_t n = w.n;
+    uint32_t batch = c.p[P_SAMPLES_PER_DISPATCH];
+    for (;;) {
+        uint32_t base = warp_fetch(&w.fetch[6 + in]);
+        if (base >= count)
+            break;
+        uint32_t i = base + lane_id();
+        bool live = false;
+        uint32_t p = 0;
+        if (i < count) {
+            p = qin[i];
+            uint32_t meta = w.meta[p];
+            uint32_t depth = meta & 0xffu, k = meta >> 8;
+            uint32_t flags = __float_as_uint(w.sreq[n + p].w);
+            float4 tot = w.state[3 * n + p];
+            V3 total = v3(tot.x, tot.y, tot.z);
+            if ((flags & 1u) && ((const uint32_t*)w.hits)[4 * (size_t)p] == 0u) {
+                float4 r2 = w.sreq[2 * n + p];
+                total += v3(r2.x, r2.y, r2.z);
+                if (flags & 2u)
+                    w.state[3 * n + p] = make_float4(total.x, total.y, total.z, tot.w);
+            }
+            if (flags & 2u) {
+                w.meta[p] = (depth + 1) | (k << 8);
+                live = true;
+            } else {
+                PathState<false> st;
+                st.parts.zero();
+                st.parts.total = total;
+                st.visLit = st.visTotal = 0.0f;
+                finishPath<false, A>(c, st, p);
+                if (k + 1 < batch && (c.p[P_ADAPTIVE] == 0 || pixelActive<A>(c, p))) {
+                    PathState<false> nx =
+                        generatePathFor<false>(c, p % c.p[P_WIDTH], p / c.p[P_WIDTH], c.p[P_SAMPLE] + k + 1);
+                    storePath<false>(w, nx, p);
+                    w.meta[p] = (k + 1) << 8;
+                    live = true;
+                }
+            }
+        }
+        __syncwarp();
+        warp_append(&w.counts[out], qout, live, p);
+    }
+}
+
 // The tail of a streaming batch: once few slots are live, one thread per remaining slot runs its
 // path and the rest of its samples to the end, trace and shade in a loop as the megakernel does,
 // instead of one half-empty wave per bounce. Same functions, same order per pixel, same sums.

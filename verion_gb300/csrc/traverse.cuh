@@ -242,4 +242,183 @@ __device__ __forceinline__ TraceHit trace_bvh(const uint4* __restrict__ nodes, c
     return h;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Queue traversal with dynamic ray fetch: a warp keeps one ray per lane and, whenever at least
+// REFILL lanes have finished theirs, hands those lanes the next rays of the queue (one atomic per
+// refill), so the warp does not idle on its longest ray (Aila and Laine, "Understanding the
+// Efficiency of Ray Traversal on GPUs", HPG 2009). Each lane runs at most STEPS node visits between
+// refills. Results are those of trace_bvh: the hit rule does not depend on the visiting order.
+//
+// get(i, r, tmax) loads queue item i into a ray and returns false when it has no ray (it then
+// completes at once with a miss); put(i, hit) stores the result of item i.
+
+struct Walk {
+    TRay r;
+    float tmax;
+    uint32_t item;
+    uint32_t node;
+    int sp;
+    TraceHit h;
+};
+
+// One node visit: box tests, the node's triangles, then the next node. Returns true when the walk
+// has finished (stack empty, or any-hit found).
+template <bool ANY>
+__device__ __forceinline__ bool walk_step(const uint4* __restrict__ nodes, const float4* __restrict__ tris, Walk& w,
+                                          uint2* stack, uint32_t* err)
+{
+    const TRay& r = w.r;
+    const uint4* np = nodes + (size_t)w.node * bvh8::NODE_VEC4;
+    uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+    w.h.nodes++;
+    float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
+    uint32_t em = w0.w;
+    float scx = __uint_as_float((em & 0xffu) << 23);
+    float scy = __uint_as_float(((em >> 8) & 0xffu) << 23);
+    float scz = __uint_as_float(((em >> 16) & 0xffu) << 23);
+    uint32_t imask = em >> 24;
+    uint32_t child_base = w1.x, tri_base = w1.y, meta_lo = w1.z, meta_hi = w1.w;
+    bool px_pos = r.ix >= 0.0f, py_pos = r.iy >= 0.0f, pz_pos = r.iz >= 0.0f;
+    uint32_t nxl = px_pos ? w2.x : w3.z, nxh = px_pos ? w2.y : w3.w;
+    uint32_t fxl = px_pos ? w3.z : w2.x, fxh = px_pos ? w3.w : w2.y;
+    uint32_t nyl = py_pos ? w2.z : w4.x, nyh = py_pos ? w2.w : w4.y;
+    uint32_t fyl = py_pos ? w4.x : w2.z, fyh = py_pos ? w4.y : w2.w;
+    uint32_t nzl = pz_pos ? w3.x : w4.z, nzh = pz_pos ? w3.y : w4.w;
+    uint32_t fzl = pz_pos ? w4.z : w3.x, fzh = pz_pos ? w4.w : w3.y;
+    float ax = (px - r.o.x) * r.ix, sx = scx * r.ix;
+    float ay = (py - r.o.y) * r.iy, sy = scy * r.iy;
+    float az = (pz - r.o.z) * r.iz, sz = scz * r.iz;
+    float ex = 4.76837158e-7f * (fabsf(ax) + 255.0f * fabsf(sx));
+    float ey = 4.76837158e-7f * (fabsf(ay) + 255.0f * fabsf(sy));
+    float ez = 4.76837158e-7f * (fabsf(az) + 255.0f * fabsf(sz));
+    float anx = ax - ex, afx = ax + ex, any_ = ay - ey, afy = ay + ey, anz = az - ez, afz = az + ez;
+    float best_t = w.tmax;
+    uint32_t inner_hits = 0, tri_bits = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        float tnx = fmaf((float)byte_of(nxl, nxh, i), sx, anx);
+        float tny = fmaf((float)byte_of(nyl, nyh, i), sy, any_);
+        float tnz = fmaf((float)byte_of(nzl, nzh, i), sz, anz);
+        float tfx = fmaf((float)byte_of(fxl, fxh, i), sx, afx);
+        float tfy = fmaf((float)byte_of(fyl, fyh, i), sy, afy);
+        float tfz = fmaf((float)byte_of(fzl, fzh, i), sz, afz);
+        float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
+        float tf = fminf(fminf(tfx, tfy), fminf(tfz, best_t));
+        if (tn <= tf) {
+            if ((imask >> i) & 1u) {
+                inner_hits |= 1u << (i ^ r.oct);
+            } else {
+                uint32_t m = byte_of(meta_lo, meta_hi, i);
+                tri_bits |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+            }
+        }
+    }
+    while (tri_bits) {
+        uint32_t j = __ffs(tri_bits) - 1;
+        tri_bits &= tri_bits - 1;
+        const float4* tp = tris + (size_t)(tri_base + j) * bvh8::TRI_VEC4;
+        float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+        float t, U, V, W, det;
+        w.h.tests++;
+        if (tri_test(r, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), t, U, V, W, det)) {
+            uint32_t gid = __float_as_uint(c.w);
+            bool take = ANY ? t < w.tmax : (t < w.tmax || (w.h.hit && t == w.tmax && gid < w.h.gid));
+            if (take) {
+                w.h.hit = true;
+                w.h.t = t;
+                w.tmax = ANY ? w.tmax : t;
+                w.h.gid = gid;
+                w.h.inst = __float_as_uint(a.w);
+                w.h.prim = __float_as_uint(b.w);
+                w.h.b1 = V / det;
+                w.h.b2 = W / det;
+                if (ANY)
+                    return true;
+            }
+        }
+    }
+    uint32_t hits = inner_hits, gbase = child_base, gmask = imask;
+    if (hits == 0) {
+        if (w.sp == 0)
+            return true;
+        --w.sp;
+        gbase = stack[w.sp].x;
+        gmask = stack[w.sp].y & 0xffu;
+        hits = stack[w.sp].y >> 8;
+    }
+    uint32_t b = __ffs(hits) - 1;
+    hits &= hits - 1;
+    w.node = gbase + __popc(gmask & ((1u << (b ^ r.oct)) - 1u));
+    if (hits) {
+        if (w.sp >= (int)bvh8::STACK_SIZE) {
+            atomicOr(err, bvh8::ERR_STACK);
+            return true;
+        }
+        stack[w.sp++] = make_uint2(gbase, gmask | (hits << 8));
+    }
+    return false;
+}
+
+template <bool ANY, int REFILL, int STEPS, typename GetRay, typename PutHit>
+__device__ __forceinline__ void trace_queue(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
+                                            uint32_t* fetch, uint32_t count, uint32_t* err, GetRay get, PutHit put)
+{
+    const uint32_t FULLM = 0xffffffffu;
+    uint32_t lane = threadIdx.x & 31u;
+    uint32_t lt = (1u << lane) - 1u;
+    uint2 stack[bvh8::STACK_SIZE];
+    Walk w;
+    bool active = false, exhausted = false;
+    for (;;) {
+        uint32_t need = __ballot_sync(FULLM, !active);
+        if (!exhausted && (need == FULLM || __popc(need) >= REFILL)) {
+            uint32_t n = __popc(need);
+            uint32_t base = 0;
+            if (lane == 0)
+                base = atomicAdd(fetch, n);
+            base = __shfl_sync(FULLM, base, 0);
+            exhausted = base + n >= count;
+            if (!active) {
+                uint32_t idx = base + __popc(need & lt);
+                if (idx < count) {
+                    V3 o, d;
+                    float tmax;
+                    w.item = idx;
+                    w.h.hit = false;
+                    w.h.inst = w.h.prim = 0;
+                    w.h.gid = 0xffffffffu;
+                    w.h.b1 = w.h.b2 = 0.0f;
+                    w.h.nodes = w.h.tests = 0;
+                    if (get(idx, o, d, tmax)) {
+                        w.r = make_ray(o, d);
+                        w.tmax = tmax;
+                        w.h.t = tmax;
+                        w.node = 0;
+                        w.sp = 0;
+                        active = true;
+                    } else {
+                        w.h.t = tmax;
+                        put(idx, w.h);
+                    }
+                }
+            }
+        }
+        if (__ballot_sync(FULLM, active) == 0) {
+            if (exhausted)
+                break;
+            continue;
+        }
+        if (active) {
+#pragma unroll 1
+            for (int s = 0; s < STEPS; s++) {
+                if (walk_step<ANY>(nodes, tris, w, stack, err)) {
+                    put(w.item, w.h);
+                    active = false;
+                    break;
+                }
+            }
+        }
+    }
+}
+
 } // namespace vgt

@@ -151,6 +151,7 @@ struct VgRenderer {
     int deferred_blocks[2] = {};
     int shadow_blocks[2] = {};
     bool defer_shadows = true; // streaming: shadow rays of the light sample in their own stage
+    bool dynamic_fetch = true; // streaming: traversal stages refill idle lanes from the queue
 };
 
 struct VgAccum {
@@ -684,6 +685,14 @@ int vg_set_stream_tail(VgRenderer* r, uint32_t threshold)
 
 double vg_accum_tail_seconds(const VgAccum* acc) { return acc ? acc->tail_ms * 1e-3 : 0.0; }
 
+int vg_set_dynamic_fetch(VgRenderer* r, int on)
+{
+    if (!r)
+        return fail(VG_ERR_INVALID, "null renderer");
+    r->dynamic_fetch = on != 0;
+    return VG_OK;
+}
+
 int vg_set_deferred_shadows(VgRenderer* r, int on)
 {
     if (!r)
@@ -938,7 +947,12 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
                     b = pool.get();
                     VG_CHECK(cudaEventRecord(a, s), "event");
                 }
-                VG_CHECK(vgx::launch_stream_extend(r->traversal_stats, eb, s, c, w, (uint32_t)wave), "extend launch");
+                if (r->dynamic_fetch)
+                    VG_CHECK(vgx::launch_stream_extend_dyn(r->traversal_stats, eb, s, c, w, (uint32_t)wave),
+                             "extend launch");
+                else
+                    VG_CHECK(vgx::launch_stream_extend(r->traversal_stats, eb, s, c, w, (uint32_t)wave),
+                             "extend launch");
                 if (timed)
                     VG_CHECK(cudaEventRecord(m, s), "event");
                 if (deferred) {
@@ -948,7 +962,13 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
                         q = pool.get();
                         VG_CHECK(cudaEventRecord(q, s), "event");
                     }
-                    VG_CHECK(vgx::launch_stream_shadow(v.f64, shb, s, c, w, (uint32_t)wave), "shadow launch");
+                    if (r->dynamic_fetch && r->ds.shadow_any) {
+                        VG_CHECK(vgx::launch_stream_shadow_trace(shb, s, c, w, (uint32_t)wave), "shadow launch");
+                        VG_CHECK(vgx::launch_stream_finish(v.f64, shb, s, c, w, (uint32_t)wave), "finish launch");
+                        acc->launches++;
+                    } else {
+                        VG_CHECK(vgx::launch_stream_shadow(v.f64, shb, s, c, w, (uint32_t)wave), "shadow launch");
+                    }
                     if (timed) {
                         VG_CHECK(cudaEventRecord(b, s), "event");
                         stages.push_back({0, {a, m}});
