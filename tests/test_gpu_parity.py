@@ -249,9 +249,10 @@ def test_wavefront_modes_match_the_oracle(gpu_ctx, mode, tail, adaptive):
         assert 0 < acc.last_waves() <= 7 * 16 + 3
 
 
-@pytest.mark.parametrize("deferred", [False, True])
-def test_streaming_shadow_stage_matches_the_oracle(gpu_ctx, deferred):
-    # The emitter / environment shadow ray traced inline in shade, or in the separate shadow stage.
+@pytest.mark.parametrize("deferred,dynamic", [(False, False), (True, False), (True, True)])
+def test_streaming_shadow_stage_matches_the_oracle(gpu_ctx, deferred, dynamic):
+    # The emitter / environment shadow ray traced inline in shade, or in the separate shadow stage;
+    # with dynamic fetch the extend and shadow traversals refill idle lanes from the queue.
     from . import analytic as an
 
     for s, depth in ((scenes.many_spheres(hdri=(256, 128)), 16), (an.feature_zoo(), 8)):
@@ -260,6 +261,7 @@ def test_streaming_shadow_stage_matches_the_oracle(gpu_ctx, deferred):
         r.set_accum_precision(32)
         r.set_integrator(Integrator.WAVEFRONT)
         r.set_deferred_shadows(deferred)
+        r.set_dynamic_fetch(dynamic)
         r.set_stream_tail(0)
         r.set_max_depth(depth)
         acc = r.new_accumulation(40, 30)

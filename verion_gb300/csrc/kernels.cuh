@@ -567,7 +567,7 @@ __global__ void __launch_bounds__(128, 8) wf_stream_extend_dyn(const __grid_cons
 
 // Shadow rays of the deferred light samples, any hit (opaque scenes: one layer, no opacity roll).
 // The result goes to hits[p].x (1 occluded), which the finish stage reads.
-__global__ void __launch_bounds__(128, 8) wf_stream_shadow_trace(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
+static __global__ void __launch_bounds__(128, 8) wf_stream_shadow_trace(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
 {
     uint32_t in = wave & 1u;
     uint32_t count = w.counts[in];
