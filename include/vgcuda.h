@@ -240,6 +240,20 @@ int vg_trace_occluded(VgRenderer* r, const float* rays, size_t n, uint32_t* out)
 /* Device-resident form for timing: rays and hits are device pointers; returns the kernel time. */
 int vg_trace_closest_device(VgRenderer* r, const float* d_rays, size_t n, uint32_t* d_hits, double* seconds);
 
+/* vg_trace_closest without any device allocation (no reference counterpart). For callers that must
+ * not allocate while they query the scene: a viewer's per-frame picking or a tool's probe rays run
+ * beside other streams, and cudaMalloc / cudaFree (which vg_trace_closest does per call for its
+ * ray and hit staging) synchronise the whole device or fail once the scene has taken the memory.
+ * The staging, the fetch counter and the error flag live in one static device array of the
+ * library module instead: at most VG_TRACE_NOALLOC_MAX_RAYS rays per call (2.5 MiB); larger n is
+ * rejected with VG_ERR_INVALID. The first call on a device resolves that array's address (with
+ * cudaGetSymbolAddress, the device made current) and caches it: make that first call before any
+ * stream capture. All renderers on a device share the array, so calls that overlap on the GPU
+ * (from several threads or contexts at once) race on it; the call synchronises its stream before
+ * it returns. Results are identical to vg_trace_closest's. */
+#define VG_TRACE_NOALLOC_MAX_RAYS 65536u
+int vg_trace_closest_noalloc(VgRenderer* r, const float* rays, size_t n, uint32_t* hits);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,6 +23,7 @@ LIB_PATH = Path(os.environ.get("VGCUDA_LIB", Path(__file__).resolve().parent / "
 
 VG_OK, VG_ERR_NO_DEVICE, VG_ERR_UNSUPPORTED, VG_ERR_OOM, VG_ERR_RESOURCE, VG_ERR_KERNEL, VG_ERR_SCENE, \
     VG_ERR_TIMEOUT, VG_ERR_INVALID = range(9)
+VG_TRACE_NOALLOC_MAX_RAYS = 65536  # include/vgcuda.h
 _KIND = {VG_ERR_NO_DEVICE: "NoDevice", VG_ERR_UNSUPPORTED: "Unsupported", VG_ERR_OOM: "OutOfMemory",
          VG_ERR_RESOURCE: "Resource", VG_ERR_KERNEL: "Kernel", VG_ERR_SCENE: "Scene", VG_ERR_TIMEOUT: "Timeout",
          VG_ERR_INVALID: "Invalid"}
@@ -153,6 +154,7 @@ def lib() -> C.CDLL:
             "vg_trace_closest": (i32, [vp, vp, _S, vp]),
             "vg_trace_occluded": (i32, [vp, vp, _S, vp]),
             "vg_trace_closest_device": (i32, [vp, vp, _S, vp, C.POINTER(f64)]),
+            "vg_trace_closest_noalloc": (i32, [vp, vp, _S, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -480,6 +482,14 @@ class Renderer:
         r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
         out = np.empty((len(r), 4), np.uint32)
         _check(lib().vg_trace_closest(self._h, _ptr(r), len(r), _ptr(out)))
+        return out
+
+    def trace_closest_noalloc(self, rays: np.ndarray) -> np.ndarray:
+        """trace_closest through the library's static device scratch (no device allocation);
+        at most VG_TRACE_NOALLOC_MAX_RAYS rays per call."""
+        r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        out = np.empty((len(r), 4), np.uint32)
+        _check(lib().vg_trace_closest_noalloc(self._h, _ptr(r), len(r), _ptr(out)))
         return out
 
     def trace_occluded(self, rays: np.ndarray) -> np.ndarray:

@@ -16,6 +16,7 @@
 #include <chrono>
 #include <cstring>
 #include <string>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -1313,6 +1314,75 @@ int vg_trace_closest(VgRenderer* r, const float* rays, size_t n, uint32_t* hits)
         VG_CHECK(cudaMemcpyAsync(hits, dh.p, n * 16, cudaMemcpyDeviceToHost, s), "hit readback");
         VG_CHECK(cudaStreamSynchronize(s), "hit readback");
     }
+    return VG_OK;
+}
+
+} // extern "C"
+
+// Static scratch of vg_trace_closest_noalloc: word 0 is the ray fetch counter, word 1 the error
+// flag, then the staged rays (24 B each) and hits (16 B each) of at most VG_TRACE_NOALLOC_MAX_RAYS
+// rays: 256 + 65536 * 40 bytes = 2.5 MiB of device memory in the module image.
+namespace {
+constexpr size_t NA_RAYS_OFF = 256;
+constexpr size_t NA_HITS_OFF = NA_RAYS_OFF + (size_t)VG_TRACE_NOALLOC_MAX_RAYS * 24;
+constexpr size_t NA_BYTES = NA_HITS_OFF + (size_t)VG_TRACE_NOALLOC_MAX_RAYS * 16;
+constexpr int NA_MAX_DEVICES = 64;
+std::mutex g_na_mu;
+unsigned char* g_na_addr[NA_MAX_DEVICES] = {};
+} // namespace
+
+static __device__ __align__(256) unsigned char g_trace_noalloc_scratch[NA_BYTES];
+
+// Resolves the scratch array's address on `device` once (with that device current) and caches it.
+static int noalloc_scratch(int device, unsigned char** out)
+{
+    if (device < 0 || device >= NA_MAX_DEVICES)
+        return fail(VG_ERR_INVALID, "device ordinal out of range for the static scratch table");
+    std::lock_guard<std::mutex> lock(g_na_mu);
+    if (!g_na_addr[device]) {
+        VG_CHECK(cudaSetDevice(device), "cudaSetDevice");
+        void* p = nullptr;
+        VG_CHECK(cudaGetSymbolAddress(&p, g_trace_noalloc_scratch), "cudaGetSymbolAddress");
+        g_na_addr[device] = (unsigned char*)p;
+    }
+    *out = g_na_addr[device];
+    return VG_OK;
+}
+
+extern "C" {
+
+int vg_trace_closest_noalloc(VgRenderer* r, const float* rays, size_t n, uint32_t* hits)
+{
+    if (!r || (n > 0 && (!rays || !hits)))
+        return fail(VG_ERR_INVALID, "null argument");
+    if (n > VG_TRACE_NOALLOC_MAX_RAYS)
+        return fail(VG_ERR_INVALID, "vg_trace_closest_noalloc: " + std::to_string(n) +
+                                        " rays exceed its static scratch of " +
+                                        std::to_string(VG_TRACE_NOALLOC_MAX_RAYS) +
+                                        " rays; split the batch or call vg_trace_closest");
+    unsigned char* base = nullptr;
+    int st = noalloc_scratch(r->ctx->device, &base);
+    if (st != VG_OK)
+        return st;
+    cudaStream_t s = r->ctx->stream;
+    vgd::Ctx c = make_ctx(r, nullptr);
+    c.err = (uint32_t*)(base + 4);
+    // The fetch counter and the error flag must start at zero.
+    VG_CHECK(cudaMemsetAsync(base, 0, 8, s), "scratch clear");
+    if (n > 0) {
+        VG_CHECK(cudaMemcpyAsync(base + NA_RAYS_OFF, rays, n * 24, cudaMemcpyHostToDevice, s), "ray upload");
+        VG_CHECK(vgx::launch_trace_rays(blocks_for(r, r->extend_blocks), s, c, (const float*)(base + NA_RAYS_OFF),
+                                        (uint4*)(base + NA_HITS_OFF), (uint32_t)n, (uint32_t*)base),
+                 "trace launch");
+        VG_CHECK(cudaMemcpyAsync(hits, base + NA_HITS_OFF, n * 16, cudaMemcpyDeviceToHost, s), "hit readback");
+    }
+    uint32_t e = 0;
+    VG_CHECK(cudaMemcpyAsync(&e, base + 4, 4, cudaMemcpyDeviceToHost, s), "error flag");
+    VG_CHECK(cudaStreamSynchronize(s), "trace");
+    if (e & bvh8::ERR_STACK)
+        return fail(VG_ERR_KERNEL, "BVH traversal stack overflow");
+    if (e)
+        return fail(VG_ERR_KERNEL, "kernel reported error status " + std::to_string(e));
     return VG_OK;
 }
 
