@@ -40,6 +40,7 @@ typedef enum VgStatus {
 typedef struct VgContext VgContext;
 typedef struct VgRenderer VgRenderer;
 typedef struct VgAccum VgAccum;
+typedef struct VgCache VgCache;
 
 /* lib.rs:240-249 MemoryUsage */
 typedef struct VgMemoryUsage {
@@ -253,6 +254,73 @@ int vg_trace_closest_device(VgRenderer* r, const float* d_rays, size_t n, uint32
  * it returns. Results are identical to vg_trace_closest's. */
 #define VG_TRACE_NOALLOC_MAX_RAYS 65536u
 int vg_trace_closest_noalloc(VgRenderer* r, const float* rays, size_t n, uint32_t* hits);
+
+/* ---- Radiance cache (no reference counterpart) -----------------------------------------------
+ * A multi-resolution hash-grid encoding of the position (two fp16 features per level) feeding a
+ * 64-wide MLP with 4 hidden ReLU layers (bf16 weights and activations, f32 accumulation on the
+ * tensor cores) that predicts the radiance a surface point scatters toward a direction. Trained
+ * online with Adam on the relative L2 loss sum_k (p_k - y_k)^2 / (p_k^2 + 0.01) (denominator held
+ * constant).
+ *
+ * Records are VG_CACHE_RECORD_FLOATS floats: 0-2 world position, 3-5 direction toward the viewer
+ * of the vertex, 6-8 shading normal, 9 roughness, 10-12 base colour, 13 metallic, 14 transmission,
+ * 15 unused, 16-18 the training target (radiance), 19 unused.
+ * Parameters (f32): the MLP as 4 matrices of 64 x 64 then one of 16 x 64 (rows 0-2 used), each
+ * row-major (output, input), VG_CACHE_MLP_PARAMS floats; the grid as levels x 2^log2_entries x 2. */
+#define VG_CACHE_RECORD_FLOATS 20u
+#define VG_CACHE_MLP_PARAMS 17408u
+
+typedef struct VgCacheConfig {
+    uint32_t levels;          /* hash-grid levels, 1..16 (16) */
+    uint32_t log2_entries;    /* table entries per level, log2, 8..24 (19) */
+    uint32_t base_resolution; /* coarsest grid resolution over the box's largest side (16) */
+    uint32_t max_resolution;  /* finest grid resolution (2048) */
+    float learning_rate;      /* Adam step size (0.01) */
+    float beta1, beta2, epsilon; /* Adam (0.9, 0.99, 1e-8) */
+    uint32_t seed;            /* initialisation seed */
+    float bounds_lo[3], bounds_hi[3]; /* scene box the grid spans (vg_renderer_bounds) */
+} VgCacheConfig;
+
+/* Fills the defaults above (bounds zero). */
+void vg_cache_default_config(VgCacheConfig* out);
+/* World-space box of the renderer's triangles. */
+int vg_renderer_bounds(const VgRenderer* r, float lo[3], float hi[3]);
+int vg_cache_create(VgContext* ctx, const VgCacheConfig* cfg, VgCache** out);
+int vg_cache_destroy(VgCache* cache);
+int vg_cache_param_counts(const VgCache* cache, size_t* mlp, size_t* grid);
+/* f32 master parameters; either pointer may be null. */
+int vg_cache_read_params(VgCache* cache, float* mlp, float* grid);
+/* Replaces the parameters (either pointer may be null) and restarts the optimiser. */
+int vg_cache_write_params(VgCache* cache, const float* mlp, const float* grid);
+/* Predictions (3 floats per record) of n records. */
+int vg_cache_infer(VgCache* cache, const float* records, size_t n, float* out);
+/* Gradient sums over n records of the per-record loss, without applying them: mlp_grad has
+ * VG_CACHE_MLP_PARAMS floats, grid_grad the grid's size (either may be null); *loss = loss sum. */
+int vg_cache_gradients(VgCache* cache, const float* records, size_t n, float* mlp_grad, float* grid_grad,
+                       double* loss);
+/* Adam steps over consecutive batches of `batch` records (gradient = batch mean); *last_loss =
+ * mean loss per channel of the last batch. */
+int vg_cache_train(VgCache* cache, const float* records, size_t n, uint32_t batch, double* last_loss);
+/* Radiance-cache integrator for this renderer's accumulations (cache null: off). Each sample
+ * traces one path per pixel that ends at the first vertex past the primary one where the path
+ * spread passes `spread` times the primary spread (Mueller et al. 2021), and adds the cache's
+ * prediction there times the path throughput; about `train_paths` pixels per sample trace
+ * training paths to full depth instead, whose vertices train the cache for `train_steps` Adam
+ * steps of `train_batch` records after the sample. Megakernel paths; the lighting split,
+ * adaptive sampling and ReSTIR are not available with it (VG_ERR_UNSUPPORTED). The renderer does
+ * not own the cache: keep it alive while the renderer uses it. */
+int vg_set_cache(VgRenderer* r, VgCache* cache, float spread, uint32_t train_paths, uint32_t train_steps,
+                 uint32_t train_batch);
+/* Of the last sample of the last accumulate call with the cache: query records, training
+ * records (before the capacity clamp), and the last training step's mean loss per channel;
+ * with stage timing, seconds spent in the path kernel, inference and training over that call. */
+typedef struct VgCacheStats {
+    uint32_t queries;
+    uint32_t train_records;
+    double loss;
+    double path_seconds, infer_seconds, train_seconds;
+} VgCacheStats;
+int vg_accum_cache_stats(const VgAccum* acc, VgCacheStats* out);
 
 #ifdef __cplusplus
 }

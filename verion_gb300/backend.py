@@ -95,6 +95,22 @@ class BvhInfo(C.Structure):
                 ("triangle_bytes", C.c_uint64), ("build_seconds", C.c_double)]
 
 
+class CacheConfig(C.Structure):
+    """Radiance-cache configuration (include/vgcuda.h VgCacheConfig)."""
+    _fields_ = [("levels", C.c_uint32), ("log2_entries", C.c_uint32), ("base_resolution", C.c_uint32),
+                ("max_resolution", C.c_uint32), ("learning_rate", C.c_float), ("beta1", C.c_float),
+                ("beta2", C.c_float), ("epsilon", C.c_float), ("seed", C.c_uint32),
+                ("bounds_lo", C.c_float * 3), ("bounds_hi", C.c_float * 3)]
+
+
+class CacheStats(C.Structure):
+    _fields_ = [("queries", C.c_uint32), ("train_records", C.c_uint32), ("loss", C.c_double),
+                ("path_seconds", C.c_double), ("infer_seconds", C.c_double), ("train_seconds", C.c_double)]
+
+
+CACHE_RECORD_FLOATS = 20  # include/vgcuda.h VG_CACHE_RECORD_FLOATS
+CACHE_MLP_PARAMS = 17408  # VG_CACHE_MLP_PARAMS
+
 _lib = None
 
 
@@ -155,6 +171,18 @@ def lib() -> C.CDLL:
             "vg_trace_occluded": (i32, [vp, vp, _S, vp]),
             "vg_trace_closest_device": (i32, [vp, vp, _S, vp, C.POINTER(f64)]),
             "vg_trace_closest_noalloc": (i32, [vp, vp, _S, vp]),
+            "vg_cache_default_config": (None, [C.POINTER(CacheConfig)]),
+            "vg_renderer_bounds": (i32, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+            "vg_cache_create": (i32, [vp, C.POINTER(CacheConfig), C.POINTER(vp)]),
+            "vg_cache_destroy": (i32, [vp]),
+            "vg_cache_param_counts": (i32, [vp, C.POINTER(_S), C.POINTER(_S)]),
+            "vg_cache_read_params": (i32, [vp, vp, vp]),
+            "vg_cache_write_params": (i32, [vp, vp, vp]),
+            "vg_cache_infer": (i32, [vp, vp, _S, vp]),
+            "vg_cache_gradients": (i32, [vp, vp, _S, vp, vp, C.POINTER(f64)]),
+            "vg_cache_train": (i32, [vp, vp, _S, u32, C.POINTER(f64)]),
+            "vg_set_cache": (i32, [vp, vp, C.c_float, u32, u32, u32]),
+            "vg_accum_cache_stats": (i32, [vp, C.POINTER(CacheStats)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -329,6 +357,11 @@ class Accumulation:
     def active_pixels(self) -> int:
         return rb.active_pixels(self.raw_stats(), self.adaptive, self.pixels)
 
+    def cache_stats(self) -> CacheStats:
+        st = CacheStats()
+        _check(lib().vg_accum_cache_stats(self._h, C.byref(st)))
+        return st
+
     def close(self):
         if self._h:
             lib().vg_accum_destroy(self._h)
@@ -498,9 +531,102 @@ class Renderer:
         _check(lib().vg_trace_occluded(self._h, _ptr(r), len(r), _ptr(out)))
         return out
 
+    def bounds(self):
+        """World-space box (lo, hi) of the scene's triangles."""
+        lo, hi = (C.c_float * 3)(), (C.c_float * 3)()
+        _check(lib().vg_renderer_bounds(self._h, lo, hi))
+        return tuple(lo), tuple(hi)
+
+    def set_cache(self, cache: Optional["Cache"], spread: float = 0.01, train_paths: int = 16384,
+                  train_steps: int = 4, train_batch: int = 16384) -> None:
+        """Radiance-cache integrator (None: off); the renderer keeps a reference to the cache."""
+        _check(lib().vg_set_cache(self._h, cache._h if cache else None, spread, train_paths, train_steps,
+                                  train_batch))
+        self._cache = cache
+
     def close(self):
         if self._h:
             lib().vg_renderer_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Cache:
+    """Radiance cache: hash-grid encoding + 64-wide MLP trained on the tensor cores (include/vgcuda.h,
+    "Radiance cache"). Records are (n, CACHE_RECORD_FLOATS) float32 arrays."""
+
+    def __init__(self, ctx: Context, config: Optional[CacheConfig] = None, bounds=None, **overrides):
+        cfg = CacheConfig()
+        lib().vg_cache_default_config(C.byref(cfg))
+        if config is not None:
+            C.memmove(C.byref(cfg), C.byref(config), C.sizeof(CacheConfig))
+        for k, v in overrides.items():
+            setattr(cfg, k, v)
+        if bounds is not None:
+            lo, hi = bounds
+            for i in range(3):
+                cfg.bounds_lo[i] = lo[i]
+                cfg.bounds_hi[i] = hi[i]
+        self.config = cfg
+        self._ctx = ctx
+        h = C.c_void_p()
+        _check(lib().vg_cache_create(ctx._h, C.byref(cfg), C.byref(h)))
+        self._h = h
+
+    def param_counts(self):
+        m, g = _S(), _S()
+        _check(lib().vg_cache_param_counts(self._h, C.byref(m), C.byref(g)))
+        return m.value, g.value
+
+    def read_params(self):
+        m, g = self.param_counts()
+        mlp, grid = np.empty(m, np.float32), np.empty(g, np.float32)
+        _check(lib().vg_cache_read_params(self._h, _ptr(mlp), _ptr(grid)))
+        return mlp, grid
+
+    def write_params(self, mlp: Optional[np.ndarray] = None, grid: Optional[np.ndarray] = None) -> None:
+        m, g = self.param_counts()
+        mp = np.ascontiguousarray(mlp, np.float32) if mlp is not None else None
+        gp = np.ascontiguousarray(grid, np.float32) if grid is not None else None
+        if mp is not None and mp.size != m or gp is not None and gp.size != g:
+            raise ValueError("parameter vector of the wrong size")
+        _check(lib().vg_cache_write_params(self._h, _ptr(mp) if mp is not None else None,
+                                           _ptr(gp) if gp is not None else None))
+
+    @staticmethod
+    def _records(records: np.ndarray) -> np.ndarray:
+        return np.ascontiguousarray(records, np.float32).reshape(-1, CACHE_RECORD_FLOATS)
+
+    def infer(self, records: np.ndarray) -> np.ndarray:
+        r = self._records(records)
+        out = np.empty((len(r), 3), np.float32)
+        _check(lib().vg_cache_infer(self._h, _ptr(r), len(r), _ptr(out)))
+        return out
+
+    def gradients(self, records: np.ndarray):
+        """(mlp gradient sums, grid gradient sums, loss sum) over the records, not applied."""
+        r = self._records(records)
+        m, g = self.param_counts()
+        gm, gg = np.empty(m, np.float32), np.empty(g, np.float32)
+        loss = C.c_double()
+        _check(lib().vg_cache_gradients(self._h, _ptr(r), len(r), _ptr(gm), _ptr(gg), C.byref(loss)))
+        return gm, gg, loss.value
+
+    def train(self, records: np.ndarray, batch: int) -> float:
+        """Adam steps over consecutive batches; returns the last batch's mean loss per channel."""
+        r = self._records(records)
+        loss = C.c_double()
+        _check(lib().vg_cache_train(self._h, _ptr(r), len(r), batch, C.byref(loss)))
+        return loss.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().vg_cache_destroy(self._h)
             self._h = None
 
     def __del__(self):

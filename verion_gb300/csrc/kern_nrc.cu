@@ -1,0 +1,677 @@
+// Radiance-cache kernels (no reference counterpart; see nrc.cuh for the record and network
+// layout): the hash-grid encoding, inference and training on the fifth-generation tensor cores
+// (tcgen05 MMA, operands in shared memory, accumulators in tensor memory), Adam, the bf16 weight
+// image, and the path kernel that ends paths at the cache.
+#include <cuda_fp16.h>
+
+#include <algorithm>
+
+#include "launch_nrc.h"
+#include "nrc.cuh"
+#include "pt_device.cuh"
+#include "tc.cuh"
+
+namespace vgnk {
+
+using namespace vgd;
+using namespace vgn;
+using namespace vgtc;
+
+constexpr uint32_t FULLM = 0xffffffffu;
+constexpr unsigned long long WAIT_NS = 2000000000ull; // an MMA completion wait gives up after 2 s
+
+static __device__ __forceinline__ uint8_t* align1024(uint8_t* p)
+{
+    uint32_t a = smem_u32(p);
+    return p + (((a + 1023u) & ~1023u) - a);
+}
+
+static __device__ __forceinline__ unsigned long long now_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits for the MMA phase; false once WAIT_NS have passed (the caller stops issuing work).
+static __device__ __forceinline__ bool wait_mma(uint64_t* bar, uint32_t parity)
+{
+    unsigned long long t0 = now_ns();
+    for (;;) {
+        if (bar_wait(bar, parity, 64))
+            return true;
+        if (now_ns() - t0 > WAIT_NS)
+            return false;
+    }
+}
+
+// ---- encoding ---------------------------------------------------------------------------------
+
+// Trilinear hash-grid features of a world position, 2 per level (levels past cd.levels are 0).
+// The corner weights are ((wx * wy) * wz) and the corners are summed in the order 0..7
+// (bit 0 = x, bit 1 = y, bit 2 = z), in single precision.
+static __device__ __forceinline__ void grid_features(const CacheDev& cd, const float* rec, float* f)
+{
+    float x = fminf(fmaxf((rec[0] - cd.lo[0]) * cd.inv_extent, 0.0f), 1.0f);
+    float y = fminf(fmaxf((rec[1] - cd.lo[1]) * cd.inv_extent, 0.0f), 1.0f);
+    float z = fminf(fmaxf((rec[2] - cd.lo[2]) * cd.inv_extent, 0.0f), 1.0f);
+    uint32_t mask = (1u << cd.log2_t) - 1u;
+#pragma unroll
+    for (uint32_t l = 0; l < MAX_LEVELS; l++) {
+        float a0 = 0.0f, a1 = 0.0f;
+        if (l < cd.levels) {
+            uint32_t res = cd.res[l];
+            float sx = x * (float)res, sy = y * (float)res, sz = z * (float)res;
+            uint32_t ix = min((uint32_t)sx, res - 1u), iy = min((uint32_t)sy, res - 1u), iz = min((uint32_t)sz, res - 1u);
+            float fx = sx - (float)ix, fy = sy - (float)iy, fz = sz - (float)iz;
+            bool dense = (cd.dense_mask >> l) & 1u;
+            const uint32_t* g = cd.grid + ((size_t)l << cd.log2_t);
+#pragma unroll
+            for (uint32_t k = 0; k < 8; k++) {
+                float w = ((k & 1u) ? fx : 1.0f - fx) * ((k & 2u) ? fy : 1.0f - fy);
+                w = w * ((k & 4u) ? fz : 1.0f - fz);
+                uint32_t e = __ldg(g + grid_index(ix + (k & 1u), iy + ((k >> 1) & 1u), iz + ((k >> 2) & 1u), res, dense, mask));
+                __half2 h = *reinterpret_cast<__half2*>(&e);
+                float2 v = __half22float2(h);
+                a0 = a0 + w * v.x;
+                a1 = a1 + w * v.y;
+            }
+        }
+        f[2 * l] = a0;
+        f[2 * l + 1] = a1;
+    }
+}
+
+// Gradient of the grid features scattered to the table entries (f32 atomics).
+static __device__ __forceinline__ void grid_backward(const CacheDev& cd, const float* rec, const float* g)
+{
+    float x = fminf(fmaxf((rec[0] - cd.lo[0]) * cd.inv_extent, 0.0f), 1.0f);
+    float y = fminf(fmaxf((rec[1] - cd.lo[1]) * cd.inv_extent, 0.0f), 1.0f);
+    float z = fminf(fmaxf((rec[2] - cd.lo[2]) * cd.inv_extent, 0.0f), 1.0f);
+    uint32_t mask = (1u << cd.log2_t) - 1u;
+    for (uint32_t l = 0; l < cd.levels; l++) {
+        float g0 = g[2 * l], g1 = g[2 * l + 1];
+        if (g0 == 0.0f && g1 == 0.0f)
+            continue;
+        uint32_t res = cd.res[l];
+        float sx = x * (float)res, sy = y * (float)res, sz = z * (float)res;
+        uint32_t ix = min((uint32_t)sx, res - 1u), iy = min((uint32_t)sy, res - 1u), iz = min((uint32_t)sz, res - 1u);
+        float fx = sx - (float)ix, fy = sy - (float)iy, fz = sz - (float)iz;
+        bool dense = (cd.dense_mask >> l) & 1u;
+        float* gg = cd.grid_grad + ((size_t)l << cd.log2_t) * 2;
+        for (uint32_t k = 0; k < 8; k++) {
+            float w = ((k & 1u) ? fx : 1.0f - fx) * ((k & 2u) ? fy : 1.0f - fy);
+            w = w * ((k & 4u) ? fz : 1.0f - fz);
+            uint32_t e = grid_index(ix + (k & 1u), iy + ((k >> 1) & 1u), iz + ((k >> 2) & 1u), res, dense, mask);
+            atomicAdd(gg + 2 * (size_t)e, w * g0);
+            atomicAdd(gg + 2 * (size_t)e + 1, w * g1);
+        }
+    }
+}
+
+// The 64 network inputs of a record.
+static __device__ __forceinline__ void input_row(const CacheDev& cd, const float* rec, float* v)
+{
+    grid_features(cd, rec, v);
+#pragma unroll
+    for (int k = 0; k < 6; k++)
+        v[32 + k] = rec[3 + k] * 0.5f + 0.5f;
+#pragma unroll
+    for (int k = 0; k < 6; k++)
+        v[38 + k] = rec[9 + k];
+    v[44] = 1.0f;
+#pragma unroll
+    for (int k = 45; k < 64; k++)
+        v[k] = 0.0f;
+}
+
+// Row m of a [rows x 64] swizzled bf16 tile.
+static __device__ __forceinline__ void store_row(uint8_t* tile, uint32_t m, const float* v)
+{
+#pragma unroll
+    for (uint32_t j = 0; j < 8; j++) {
+        uint4 q;
+        q.x = pack_bf16(v[8 * j], v[8 * j + 1]);
+        q.y = pack_bf16(v[8 * j + 2], v[8 * j + 3]);
+        q.z = pack_bf16(v[8 * j + 4], v[8 * j + 5]);
+        q.w = pack_bf16(v[8 * j + 6], v[8 * j + 7]);
+        *reinterpret_cast<uint4*>(tile + m * 128u + (((j ^ m) & 7u) << 4)) = q;
+    }
+}
+
+// Column m (0..127) of a transposed tile: rows 0..63 of K-regions of `region` bytes each.
+static __device__ __forceinline__ void store_col(uint8_t* tile, uint32_t region, uint32_t m, const float* v)
+{
+    uint8_t* base = tile + (m >> 6) * region;
+    uint32_t c = m & 63u;
+#pragma unroll
+    for (uint32_t j = 0; j < 64; j++)
+        *reinterpret_cast<__nv_bfloat16*>(base + sw128(j, c)) = __float2bfloat16_rn(v[j]);
+}
+
+// 64 (or 16) accumulator columns of this thread's row.
+static __device__ __forceinline__ void load_acc(uint32_t taddr, float* v, int cols)
+{
+    tmem_ld16(taddr, v);
+    if (cols > 16) {
+        tmem_ld16(taddr + 16, v + 16);
+        tmem_ld16(taddr + 32, v + 32);
+        tmem_ld16(taddr + 48, v + 48);
+    }
+}
+
+// Makes the tile writes visible to the tensor core, then thread 0 issues `steps` MMAs of one layer.
+static __device__ __forceinline__ void issue_layer(uint32_t d, const uint8_t* A, uint32_t a_region, const uint8_t* B,
+                                                   uint32_t b_region, uint32_t n, uint32_t steps, bool accumulate)
+{
+    uint32_t id = idesc_bf16(128, n);
+    uint32_t a = smem_u32(A), b = smem_u32(B);
+    for (uint32_t s = 0; s < steps; s++) {
+        uint32_t ao = (s >> 2) * a_region + (s & 3u) * 32u;
+        uint32_t bo = (s >> 2) * b_region + (s & 3u) * 32u;
+        mma_bf16(d, sdesc(a + ao), sdesc(b + bo), id, (accumulate || s > 0) ? 1u : 0u);
+    }
+}
+
+// ---- inference ----------------------------------------------------------------------------------
+
+// MODE 0: out[3 i + k] = prediction k of record i. MODE 1: the prediction, clamped at zero and
+// times the record's throughput, is added to the record's pixel in `accum`.
+template <int MODE, typename A>
+__global__ void __launch_bounds__(128) nrc_infer(CacheDev cd, const float* __restrict__ rec, const uint32_t* count,
+                                                 uint32_t cap, float* out, A* accum)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* sm = align1024(smem_raw);
+    uint8_t* W = sm;
+    uint8_t* H = sm + IMG_FWD_BYTES;
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tslot;
+    uint32_t tid = threadIdx.x, warp = tid >> 5;
+    for (uint32_t i = tid; i < IMG_FWD_BYTES / 16; i += blockDim.x)
+        reinterpret_cast<uint4*>(W)[i] = __ldg(reinterpret_cast<const uint4*>(cd.img) + i);
+    if (tid == 0) {
+        bar_init(&bar, 1);
+        fence_bar_init();
+    }
+    if (warp == 0)
+        tmem_alloc(&tslot, 64);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    uint32_t tmem = tslot;
+    uint32_t lane_addr = tmem + ((warp * 32u) << 16);
+    uint32_t n = min(*count, cap);
+    uint32_t tiles = (n + TILE - 1) / TILE;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (uint32_t t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+        uint32_t i = t * TILE + tid;
+        bool valid = i < n;
+        float v[64];
+        if (valid) {
+            input_row(cd, rec + (size_t)i * REC_WORDS, v);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 64; k++)
+                v[k] = 0.0f;
+        }
+        store_row(H, tid, v);
+        for (uint32_t l = 0; l < 5 && ok; l++) {
+            fence_async_smem();
+            __syncthreads();
+            tc_fence_after();
+            if (tid == 0) {
+                const uint8_t* B = W + (l < 4 ? IMG_W + l * 8192u : IMG_W4);
+                issue_layer(tmem, H, 0, B, 0, l < 4 ? 64u : 16u, 4, false);
+                mma_commit(&bar);
+            }
+            bool done = wait_mma(&bar, phase);
+            phase ^= 1u;
+            ok = __syncthreads_and(done) != 0;
+            if (!ok)
+                break;
+            tc_fence_after();
+            load_acc(lane_addr, v, l < 4 ? 64 : 16);
+            tc_fence_before();
+            if (l < 4) {
+#pragma unroll
+                for (int k = 0; k < 64; k++)
+                    v[k] = fmaxf(v[k], 0.0f);
+                store_row(H, tid, v);
+            }
+        }
+        if (!ok)
+            break;
+        if (valid) {
+            if (MODE == 0) {
+                out[3 * (size_t)i] = v[0];
+                out[3 * (size_t)i + 1] = v[1];
+                out[3 * (size_t)i + 2] = v[2];
+            } else {
+                const float* r = rec + (size_t)i * REC_WORDS;
+                uint32_t px = __float_as_uint(r[19]);
+                A* a = accum + 3 * (size_t)px;
+                a[0] += (A)(r[16] * fmaxf(v[0], 0.0f));
+                a[1] += (A)(r[17] * fmaxf(v[1], 0.0f));
+                a[2] += (A)(r[18] * fmaxf(v[2], 0.0f));
+            }
+        }
+    }
+    if (!ok && tid == 0)
+        atomicOr(cd.err, ERR_MMA_TIMEOUT);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0)
+        tmem_free(tmem, 64);
+}
+
+// ---- training -----------------------------------------------------------------------------------
+
+// Shared-memory plan of the training kernel (bytes from a 1024-aligned base).
+constexpr uint32_t T_H = IMG_BYTES;            // 128 x 64 activations (forward A operand)
+constexpr uint32_t T_HT = T_H + 16384;         // 5 transposed activations, 64 x 128 each
+constexpr uint32_t T_G = T_HT + 5 * 16384;     // 128 x 64 gradients (backward A operand)
+constexpr uint32_t T_GT = T_G + 16384;         // 128 x 128 transposed gradients, rows 64..127 zero
+constexpr uint32_t T_END = T_GT + 32768;       // 223,232
+constexpr uint32_t TRAIN_SMEM = T_END + 1024;  // with the alignment slack
+constexpr uint32_t INFER_SMEM = IMG_FWD_BYTES + 16384 + 1024;
+
+// One training pass over records [offset, offset + batch) of the first min(*count, cap): the
+// relative L2 loss sum_k (p_k - y_k)^2 / (p_k^2 + 0.01) (denominator held constant) is summed
+// into cd.loss, its parameter gradients into cd.mlp_grad and cd.grid_grad. Per 128-record tile:
+// forward (5 MMA layers), then for each layer from the last, the weight gradient
+// dW_l += G^T H_l (accumulated in tensor memory over the tiles of this CTA) and the data
+// gradient G W_l, masked by the ReLU of the layer below.
+__global__ void __launch_bounds__(128, 1) nrc_train(CacheDev cd, const float* __restrict__ rec, const uint32_t* count,
+                                                    uint32_t cap, uint32_t offset, uint32_t batch)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* sm = align1024(smem_raw);
+    uint8_t* W = sm;
+    uint8_t* H = sm + T_H;
+    uint8_t* HT = sm + T_HT;
+    uint8_t* G = sm + T_G;
+    uint8_t* GT = sm + T_GT;
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tslot;
+    __shared__ float red[4];
+    uint32_t tid = threadIdx.x, warp = tid >> 5;
+    for (uint32_t i = tid; i < IMG_BYTES / 16; i += blockDim.x)
+        reinterpret_cast<uint4*>(W)[i] = __ldg(reinterpret_cast<const uint4*>(cd.img) + i);
+    for (uint32_t i = tid; i < 32768 / 16; i += blockDim.x)
+        reinterpret_cast<uint4*>(GT)[i] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+        bar_init(&bar, 1);
+        fence_bar_init();
+    }
+    if (warp == 0)
+        tmem_alloc(&tslot, 512);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    uint32_t tmem = tslot;
+    uint32_t lane_addr = tmem + ((warp * 32u) << 16);
+    uint32_t n = min(*count, cap);
+    uint32_t end = offset < n ? min(n, offset + batch) : offset;
+    uint32_t tiles = end > offset ? (end - offset + TILE - 1) / TILE : 0;
+    uint32_t phase = 0;
+    bool ok = true, first = true;
+    float loss = 0.0f;
+    for (uint32_t t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+        uint32_t i = offset + t * TILE + tid;
+        bool valid = i < end;
+        const float* r = rec + (size_t)i * REC_WORDS;
+        float v[64];
+        if (valid) {
+            input_row(cd, r, v);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 64; k++)
+                v[k] = 0.0f;
+        }
+        store_row(H, tid, v);
+        store_col(HT, 8192, tid, v);
+        uint32_t mask[4][2];
+        // Forward.
+#pragma unroll
+        for (uint32_t l = 0; l < 5; l++) {
+            fence_async_smem();
+            __syncthreads();
+            tc_fence_after();
+            if (tid == 0) {
+                const uint8_t* B = W + (l < 4 ? IMG_W + l * 8192u : IMG_W4);
+                issue_layer(tmem, H, 0, B, 0, l < 4 ? 64u : 16u, 4, false);
+                mma_commit(&bar);
+            }
+            bool done = wait_mma(&bar, phase);
+            phase ^= 1u;
+            ok = __syncthreads_and(done) != 0;
+            if (!ok)
+                break;
+            tc_fence_after();
+            load_acc(lane_addr, v, l < 4 ? 64 : 16);
+            tc_fence_before();
+            if (l < 4) {
+                uint32_t m0 = 0, m1 = 0;
+#pragma unroll
+                for (int k = 0; k < 64; k++) {
+                    bool on = v[k] > 0.0f;
+                    if (k < 32)
+                        m0 |= (on ? 1u : 0u) << k;
+                    else
+                        m1 |= (on ? 1u : 0u) << (k - 32);
+                    v[k] = on ? v[k] : 0.0f;
+                }
+                mask[l][0] = m0;
+                mask[l][1] = m1;
+                store_row(H, tid, v);
+                store_col(HT + (l + 1) * 16384u, 8192, tid, v);
+            }
+        }
+        if (!ok)
+            break;
+        // Loss gradient of the three outputs.
+        float g[64];
+#pragma unroll
+        for (int k = 0; k < 64; k++)
+            g[k] = 0.0f;
+        if (valid) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                float d = v[k] - r[16 + k];
+                float den = v[k] * v[k] + 0.01f;
+                loss += d * d / den;
+                g[k] = 2.0f * d / den;
+            }
+        }
+        store_row(G, tid, g);
+        store_col(GT, 16384, tid, g);
+        // Backward.
+#pragma unroll
+        for (int l = 4; l >= 0; l--) {
+            fence_async_smem();
+            __syncthreads();
+            tc_fence_after();
+            if (tid == 0) {
+                issue_layer(tmem + 64u + 64u * l, GT, 16384, HT + l * 16384u, 8192, 64, 8, !first);
+                const uint8_t* B = W + (l == 4 ? IMG_W4T : IMG_WT + l * 8192u);
+                issue_layer(tmem, G, 0, B, 0, 64, l == 4 ? 1u : 4u, false);
+                mma_commit(&bar);
+            }
+            bool done = wait_mma(&bar, phase);
+            phase ^= 1u;
+            ok = __syncthreads_and(done) != 0;
+            if (!ok)
+                break;
+            tc_fence_after();
+            load_acc(lane_addr, g, 64);
+            tc_fence_before();
+            if (l > 0) {
+#pragma unroll
+                for (int k = 0; k < 64; k++) {
+                    uint32_t bit = k < 32 ? (mask[l - 1][0] >> k) & 1u : (mask[l - 1][1] >> (k - 32)) & 1u;
+                    g[k] = bit ? g[k] : 0.0f;
+                }
+                store_row(G, tid, g);
+                store_col(GT, 16384, tid, g);
+            } else if (valid) {
+                grid_backward(cd, r, g);
+            }
+        }
+        first = false;
+    }
+    // Weight gradients: rows 0..63 of each accumulator (0..15 for the output layer) live in the
+    // lanes of warps 0 and 1.
+    if (ok && !first && warp < 2) {
+        tc_fence_after();
+        for (uint32_t l = 0; l < 5; l++) {
+            float v[64];
+            load_acc(lane_addr + 64u + 64u * l, v, 64);
+            uint32_t rows = l < 4 ? 64u : 16u;
+            if (tid < rows) {
+                float* dst = cd.mlp_grad + mlp_offset(l) + tid * WIDTH;
+#pragma unroll
+                for (int k = 0; k < 64; k++)
+                    atomicAdd(dst + k, v[k]);
+            }
+        }
+    }
+    if (!ok && tid == 0)
+        atomicOr(cd.err, ERR_MMA_TIMEOUT);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        loss += __shfl_xor_sync(FULLM, loss, o);
+    if ((tid & 31u) == 0)
+        red[warp] = loss;
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0 && cd.loss)
+        atomicAdd(cd.loss, (double)red[0] + (double)red[1] + (double)red[2] + (double)red[3]);
+    if (warp == 0)
+        tmem_free(tmem, 512);
+}
+
+// ---- optimiser and weight image ---------------------------------------------------------------
+
+// Adam (Kingma and Ba 2015) on the gradient sums of the step, scaled by 1 / (3 x records used);
+// a step without records changes nothing. The gradient sums are cleared. With `half_out` the
+// updated parameter is also written as fp16 (the grid table).
+__global__ void nrc_adam(float* p, float* g, float* m, float* v, size_t n, const uint32_t* count, uint32_t cap,
+                         uint32_t offset, uint32_t batch, NrcAdam a, __half* half_out)
+{
+    uint32_t avail = min(*count, cap);
+    uint32_t used = avail > offset ? min(batch, avail - offset) : 0u;
+    if (used == 0)
+        return;
+    float scale = 1.0f / (3.0f * (float)used);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        float gi = g[i] * scale;
+        g[i] = 0.0f;
+        float mi = a.beta1 * m[i] + (1.0f - a.beta1) * gi;
+        float vi = a.beta2 * v[i] + (1.0f - a.beta2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        float pi = p[i] - a.lr * (mi / a.bc1) / (sqrtf(vi / a.bc2) + a.eps);
+        p[i] = pi;
+        if (half_out)
+            half_out[i] = __float2half_rn(pi);
+    }
+}
+
+// fp16 copy of the f32 grid parameters.
+__global__ void nrc_to_half(const float* p, __half* out, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = __float2half_rn(p[i]);
+}
+
+// The bf16 weight image from the f32 parameters (see nrc.cuh).
+__global__ void nrc_pack(const float* w, uint8_t* img)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= MLP_PARAMS)
+        return;
+    __nv_bfloat16 b = __float2bfloat16_rn(w[i]);
+    uint32_t l = min(i / (WIDTH * WIDTH), 4u);
+    uint32_t j = i - l * WIDTH * WIDTH;
+    uint32_t o = j / WIDTH, k = j % WIDTH;
+    if (l < 4) {
+        *reinterpret_cast<__nv_bfloat16*>(img + IMG_W + l * 8192u + sw128(o, k)) = b;
+        *reinterpret_cast<__nv_bfloat16*>(img + IMG_WT + l * 8192u + sw128(k, o)) = b;
+    } else {
+        *reinterpret_cast<__nv_bfloat16*>(img + IMG_W4 + sw128(o, k)) = b;
+        *reinterpret_cast<__nv_bfloat16*>(img + IMG_W4T + sw128(k, o)) = b;
+    }
+}
+
+// ---- path kernel --------------------------------------------------------------------------------
+
+constexpr uint32_t MAX_TRAIN_VERTICES = 16;
+
+// Reserves k consecutive slots per lane with one atomic per warp; every lane of the warp calls it.
+static __device__ __forceinline__ uint32_t warp_reserve(uint32_t* ctr, uint32_t k)
+{
+    uint32_t lane = threadIdx.x & 31u;
+    uint32_t incl = k;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(FULLM, incl, o);
+        if (lane >= o)
+            incl += y;
+    }
+    uint32_t total = __shfl_sync(FULLM, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total)
+        base = atomicAdd(ctr, total);
+    base = __shfl_sync(FULLM, base, 31);
+    return base + incl - k;
+}
+
+static __device__ __forceinline__ void put_features(float* d, const CacheHook& hk)
+{
+    d[0] = hk.pos.x, d[1] = hk.pos.y, d[2] = hk.pos.z;
+    d[3] = hk.wo.x, d[4] = hk.wo.y, d[5] = hk.wo.z;
+    d[6] = hk.n.x, d[7] = hk.n.y, d[8] = hk.n.z;
+    d[9] = hk.rough;
+    d[10] = hk.albedo.x, d[11] = hk.albedo.y, d[12] = hk.albedo.z;
+    d[13] = hk.metallic;
+    d[14] = hk.transmission;
+    d[15] = 0.0f;
+}
+
+// One sample per pixel (sample index P_SAMPLE). A path ends at the first vertex where its
+// spread passes the threshold and leaves a query record (its radiance past that vertex comes
+// from the cache); one pixel in `train_stride` (offset by the frame) traces a training path
+// instead, which never ends for a query and leaves one training record per vertex with the
+// radiance the rest of the path brought, divided by the throughput reaching the vertex.
+template <typename A>
+__global__ void __launch_bounds__(128) mk_cache_paths(const __grid_constant__ Ctx c, NrcPathArgs a)
+{
+    uint32_t x = blockIdx.x * 16 + (threadIdx.x & 15u);
+    uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 4);
+    bool inside = x < c.p[P_WIDTH] && y < c.p[P_HEIGHT];
+    uint32_t pixel = y * c.p[P_WIDTH] + x;
+    CacheHook hk;
+    hk.c = a.spread;
+    hk.train = inside && (pixel + a.train_offset) % a.train_stride == 0;
+    hk.a0 = hk.a = 0.0f;
+    hk.query = false;
+    float feat[MAX_TRAIN_VERTICES][16];
+    V3 thr[MAX_TRAIN_VERTICES], Lb[MAX_TRAIN_VERTICES];
+    uint32_t nv = 0;
+    bool query = false;
+    PathState<false> st;
+    if (inside) {
+        st = generatePathFor<false>(c, x, y, c.p[P_SAMPLE]);
+        for (uint32_t depth = 0; depth < c.p[P_MAX_DEPTH]; depth++) {
+            bool alive = shadePath<false, false, false, true>(c, st, traceClosest(c, st.org, st.dir), depth, pixel,
+                                                              nullptr, &hk);
+            if (hk.vertex && hk.train && nv < MAX_TRAIN_VERTICES) {
+                put_features(feat[nv], hk);
+                thr[nv] = hk.thr;
+                Lb[nv] = hk.L;
+                nv++;
+            }
+            if (hk.query) {
+                query = true;
+                break;
+            }
+            if (!alive)
+                break;
+        }
+        finishPath<false, A>(c, st, pixel);
+    }
+    bool ok = inside && !bad3(st.parts.total);
+    uint32_t q = warp_reserve(a.qcount, (query && ok) ? 1u : 0u);
+    if (query && ok && q < a.qcap) {
+        float* d = a.qrec + (size_t)q * REC_WORDS;
+        put_features(d, hk);
+        d[16] = hk.thr.x, d[17] = hk.thr.y, d[18] = hk.thr.z;
+        d[19] = __uint_as_float(pixel);
+    }
+    uint32_t nt = (hk.train && ok) ? nv : 0u;
+    uint32_t t0 = warp_reserve(a.tcount, nt);
+    for (uint32_t k = 0; k < nt; k++) {
+        if (t0 + k >= a.tcap)
+            break;
+        float* d = a.trec + (size_t)(t0 + k) * REC_WORDS;
+        V3 rest = st.parts.total - Lb[k];
+        V3 t = thr[k];
+        for (int j = 0; j < 16; j++)
+            d[j] = feat[k][j];
+        d[16] = t.x > 0.0f ? rest.x / t.x : 0.0f;
+        d[17] = t.y > 0.0f ? rest.y / t.y : 0.0f;
+        d[18] = t.z > 0.0f ? rest.z / t.z : 0.0f;
+        d[19] = 0.0f;
+    }
+}
+
+} // namespace vgnk
+
+namespace vgx {
+
+using namespace vgnk;
+
+cudaError_t nrc_launch_infer(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const float* rec,
+                             const uint32_t* count, uint32_t cap, float* out, void* accum, int accum_bits)
+{
+    static bool init = false;
+    if (!init) {
+        cudaFuncSetAttribute(nrc_infer<0, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM);
+        cudaFuncSetAttribute(nrc_infer<1, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM);
+        cudaFuncSetAttribute(nrc_infer<1, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM);
+        init = true;
+    }
+    if (!accum)
+        nrc_infer<0, float><<<blocks, 128, INFER_SMEM, s>>>(cd, rec, count, cap, out, (float*)nullptr);
+    else if (accum_bits == 64)
+        nrc_infer<1, double><<<blocks, 128, INFER_SMEM, s>>>(cd, rec, count, cap, nullptr, (double*)accum);
+    else
+        nrc_infer<1, float><<<blocks, 128, INFER_SMEM, s>>>(cd, rec, count, cap, nullptr, (float*)accum);
+    return cudaGetLastError();
+}
+
+cudaError_t nrc_launch_train(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const float* rec,
+                             const uint32_t* count, uint32_t cap, uint32_t offset, uint32_t batch)
+{
+    static bool init = false;
+    if (!init) {
+        cudaFuncSetAttribute(nrc_train, cudaFuncAttributeMaxDynamicSharedMemorySize, TRAIN_SMEM);
+        init = true;
+    }
+    nrc_train<<<blocks, 128, TRAIN_SMEM, s>>>(cd, rec, count, cap, offset, batch);
+    return cudaGetLastError();
+}
+
+cudaError_t nrc_launch_adam(cudaStream_t s, float* p, float* g, float* m, float* v, size_t n, const uint32_t* count,
+                            uint32_t cap, uint32_t offset, uint32_t batch, const NrcAdam& a, void* half_out)
+{
+    int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
+    nrc_adam<<<blocks, 256, 0, s>>>(p, g, m, v, n, count, cap, offset, batch, a, (__half*)half_out);
+    return cudaGetLastError();
+}
+
+cudaError_t nrc_launch_to_half(cudaStream_t s, const float* p, void* out, size_t n)
+{
+    int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
+    nrc_to_half<<<blocks, 256, 0, s>>>(p, (__half*)out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t nrc_launch_pack(cudaStream_t s, const float* w, uint8_t* img)
+{
+    nrc_pack<<<(vgn::MLP_PARAMS + 255) / 256, 256, 0, s>>>(w, img);
+    return cudaGetLastError();
+}
+
+cudaError_t nrc_launch_paths(bool f64, dim3 grid, cudaStream_t s, const vgd::Ctx& c, const NrcPathArgs& a)
+{
+    if (f64)
+        mk_cache_paths<double><<<grid, 128, 0, s>>>(c, a);
+    else
+        mk_cache_paths<float><<<grid, 128, 0, s>>>(c, a);
+    return cudaGetLastError();
+}
+
+} // namespace vgx

@@ -1,0 +1,37 @@
+// Host-side launchers of the radiance-cache kernels (kern_nrc.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "ctx.h"
+#include "nrc.cuh"
+
+struct NrcAdam {
+    float lr, beta1, beta2, eps;
+    float bc1, bc2; // 1 - beta1^t, 1 - beta2^t
+};
+
+// Path-kernel outputs: query records (one per pixel at most) and training records.
+struct NrcPathArgs {
+    float spread;
+    uint32_t train_stride, train_offset;
+    float* qrec;
+    uint32_t* qcount;
+    uint32_t qcap;
+    float* trec;
+    uint32_t* tcount;
+    uint32_t tcap;
+};
+
+namespace vgx {
+
+cudaError_t nrc_launch_infer(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const float* rec,
+                             const uint32_t* count, uint32_t cap, float* out, void* accum, int accum_bits);
+cudaError_t nrc_launch_train(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const float* rec,
+                             const uint32_t* count, uint32_t cap, uint32_t offset, uint32_t batch);
+cudaError_t nrc_launch_adam(cudaStream_t s, float* p, float* g, float* m, float* v, size_t n, const uint32_t* count,
+                            uint32_t cap, uint32_t offset, uint32_t batch, const NrcAdam& a, void* half_out);
+cudaError_t nrc_launch_to_half(cudaStream_t s, const float* p, void* out, size_t n);
+cudaError_t nrc_launch_pack(cudaStream_t s, const float* w, uint8_t* img);
+cudaError_t nrc_launch_paths(bool f64, dim3 grid, cudaStream_t s, const vgd::Ctx& c, const NrcPathArgs& a);
+
+} // namespace vgx

@@ -810,13 +810,37 @@ struct ShadowReq {
 // DEFER (lighting split off only): the emitter / environment sample is not traced here but
 // returned in *req; it is the last contribution of the bounce, so adding it afterwards keeps the
 // order of the sums.
-template <bool LIGHT, bool RESTIR, bool DEFER = false>
+// Radiance-cache hook of shadePath (no reference counterpart). At every surface vertex the
+// path reaches (after that vertex's emission is added, before its light sampling) the hook
+// records the cache inputs, the throughput and the path radiance so far, and grows the path
+// spread of Mueller et al. 2021 (Real-time Neural Radiance Caching, eq. 3):
+// a = sum over vertices i >= 1 of sqrt(|x_{i-1} - x_i|^2 / (p(w_{i-1}) |cos theta_i|)), against
+// a0 = |x_0 - x_1|^2 / (4 pi cos theta_1) at the primary vertex. A path that is not a training
+// path ends at the first vertex past the primary one where a^2 > c a0 and is flagged as a query.
+// Directions sampled without a finite solid-angle density (refraction) add nothing to a.
+struct CacheHook {
+    float c;        // spread threshold
+    bool train;     // training path: never ends for a query
+    float a0, a;    // spread state, carried across bounces
+    bool vertex;    // a surface vertex was recorded at this bounce
+    bool query;     // the path ended at this vertex for a cache query
+    V3 pos, wo, n, albedo;
+    float rough, metallic, transmission;
+    V3 thr;         // throughput arriving at the vertex
+    V3 L;           // path radiance after the vertex's emission
+};
+
+template <bool LIGHT, bool RESTIR, bool DEFER = false, bool CACHE = false>
 __device__ bool shadePath(const Ctx& c, PathState<LIGHT>& st, Hit hq, uint32_t depth, uint32_t pixel,
-                          ShadowReq* req = nullptr)
+                          ShadowReq* req = nullptr, CacheHook* hk = nullptr)
 {
     static_assert(!(DEFER && LIGHT), "deferred shadow rays need the lighting split off");
     if (DEFER)
         req->valid = false;
+    if (CACHE) {
+        hk->vertex = false;
+        hk->query = false;
+    }
     V3 sky = v3(pf(c, P_SKY), pf(c, P_SKY + 1), pf(c, P_SKY + 2));
     bool lightingOn = LIGHT && c.p[P_LIGHTING] != 0;
     uint32_t lightCount = c.p[P_LIGHT_COUNT];
@@ -962,6 +986,31 @@ __device__ bool shadePath(const Ctx& c, PathState<LIGHT>& st, Hit hq, uint32_t d
         float transmission = fget(M, mi + 8);
         float ior = fget(M, mi + 9);
         float dispersion = fget(M, mi + 21);
+        if (CACHE) {
+            hk->vertex = true;
+            hk->pos = p;
+            hk->wo = wo;
+            hk->n = n;
+            hk->albedo = albedo;
+            hk->rough = rough;
+            hk->metallic = metallic;
+            hk->transmission = transmission;
+            hk->thr = thr;
+            hk->L = st.parts.total;
+            float cosT = fmaxf(fabsf(dot(nOut, dir)), 1.0e-4f);
+            if (depth == 0) {
+                hk->a0 = pHitT * pHitT / (4.0f * PI * cosT);
+                hk->a = 0.0f;
+            } else {
+                if (st.misPrev && st.qPrev > 0.0f)
+                    hk->a += sqrtf(pHitT * pHitT / (st.qPrev * cosT));
+                if (!hk->train && hk->a * hk->a > hk->c * hk->a0) {
+                    hk->query = true;
+                    alive = false;
+                    break;
+                }
+            }
+        }
         if (dispersion > 0.0f && transmission > 0.0f) {
             if (chan < 0) {
                 chan = min((int)(rng.next() * 3.0f), 2);

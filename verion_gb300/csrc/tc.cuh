@@ -1,0 +1,130 @@
+// Fifth-generation tensor-core helpers for sm_103a: tcgen05 MMA with operands in shared memory and
+// the accumulator in tensor memory (TMEM), mbarrier completion, and TMEM loads. Inline PTX only.
+//
+// Operand convention used throughout: every operand tile is K-major with the 128-byte swizzle.
+// A tile of R rows and 64 bf16 columns is R x 128 bytes, 1024-byte aligned; the 16-byte chunk j of
+// row r sits at chunk j ^ (r & 7) of that row. Longer K is stored as consecutive 64-column regions
+// of R x 128 bytes each. One MMA consumes K = 16 (32 bytes of every row); stepping K inside a region
+// advances the descriptor's start address by 32 bytes.
+#pragma once
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace vgtc {
+
+static __device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Byte offset of element (row r, column c) inside a 64-column swizzled region.
+static __device__ __forceinline__ uint32_t sw128(uint32_t r, uint32_t c)
+{
+    return r * 128u + ((((c >> 3) ^ r) & 7u) << 4) + ((c & 7u) << 1);
+}
+
+// Shared-memory matrix descriptor: start address, leading offset 16 B (unused by swizzled
+// K-major), stride 1024 B between 8-row groups, descriptor version 1, 128-byte swizzle.
+static __device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
+{
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// Instruction descriptor of kind::f16 with bf16 A and B, f32 accumulation, both K-major.
+static __host__ __device__ constexpr uint32_t idesc_bf16(uint32_t m, uint32_t n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+
+// D[tmem] (+)= A * B^T for one K = 16 step; issued by a single thread.
+static __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+// Arrives once on the mbarrier when every MMA this thread issued before has completed.
+static __device__ __forceinline__ void mma_commit(uint64_t* bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+static __device__ __forceinline__ void bar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+static __device__ __forceinline__ void fence_bar_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Waits for the phase with the given parity to complete; gives up after `limit` polls and returns
+// false (the caller records an error and stops issuing work).
+static __device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity, uint32_t limit)
+{
+    uint32_t a = smem_u32(bar);
+    for (uint32_t i = 0; i < limit; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done)
+            return true;
+    }
+    return false;
+}
+
+// Generic-proxy shared-memory writes become visible to the tensor core (async proxy).
+static __device__ __forceinline__ void fence_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+static __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+static __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// TMEM allocation by one whole warp; the base address lands in *slot (shared memory).
+static __device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+static __device__ __forceinline__ void tmem_free(uint32_t base, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(base), "r"(ncols) : "memory");
+}
+
+// 16 consecutive 32-bit columns of this thread's TMEM lane (the warp reads its 32 lanes).
+static __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++)
+        v[i] = __uint_as_float(r[i]);
+}
+
+static __device__ __forceinline__ uint32_t pack_bf16(float a, float b)
+{
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+
+static __device__ __forceinline__ float bf16_round(float a) { return __bfloat162float(__float2bfloat16_rn(a)); }
+
+} // namespace vgtc
