@@ -15,6 +15,7 @@ struct VgCache {
     DevBuf grid, grid_h, grid_grad, grid_m, grid_v;
     DevBuf mlp, mlp_grad, mlp_m, mlp_v, img;
     DevBuf loss, err, count;
+    DevBuf X, GX; // encoded input tiles, input-gradient rows (grown on demand)
     uint32_t step = 0;
 
     vgn::CacheDev dev() const
@@ -89,14 +90,47 @@ int cache_reset_optimiser(VgCache* k)
     return VG_OK;
 }
 
+// Room for `rows` encoded records and input-gradient rows.
+int ensure_work(VgCache* k, size_t rows)
+{
+    size_t xb = std::max<size_t>((rows + vgn::TILE - 1) / vgn::TILE, 1) * 16384;
+    size_t gb = std::max<size_t>(rows, 1) * 32 * 4;
+    int st;
+    if (k->X.bytes < xb && (st = alloc(k->X, xb, k->ctx->stream, false)) != VG_OK)
+        return st;
+    if (k->GX.bytes < gb && (st = alloc(k->GX, gb, k->ctx->stream, false)) != VG_OK)
+        return st;
+    return VG_OK;
+}
+
+int encode_blocks(const VgCache* k) { return 8 * k->ctx->sms; }
+
+// Gradient sums of the records [offset, offset + batch) of the first min(*count, cap) at `rec`:
+// encode, the tensor-core pass, the grid scatter (ensure_work(batch) first).
+int cache_gradient_pass(VgCache* k, const float* rec, const uint32_t* count, uint32_t cap, uint32_t offset,
+                        uint32_t batch)
+{
+    cudaStream_t s = k->ctx->stream;
+    vgn::CacheDev d = k->dev();
+    VG_CHECK(vgx::nrc_launch_encode(encode_blocks(k), s, d, rec, count, cap, offset, batch, (uint8_t*)k->X.p),
+             "encode launch");
+    VG_CHECK(vgx::nrc_launch_train(k->ctx->sms, s, d, (const uint8_t*)k->X.p, rec, count, cap, offset, batch,
+                                   (float*)k->GX.p),
+             "train launch");
+    VG_CHECK(vgx::nrc_launch_scatter(encode_blocks(k), s, d, rec, count, cap, offset, batch, (const float*)k->GX.p),
+             "scatter launch");
+    return VG_OK;
+}
+
 // One Adam step on the records [offset, offset + batch) of the first min(*count, cap) at `rec`.
 int cache_train_step(VgCache* k, const float* rec, const uint32_t* count, uint32_t cap, uint32_t offset,
                      uint32_t batch)
 {
     cudaStream_t s = k->ctx->stream;
-    vgn::CacheDev d = k->dev();
+    int st;
     VG_CHECK(cudaMemsetAsync(k->loss.p, 0, 8, s), "loss");
-    VG_CHECK(vgx::nrc_launch_train(k->ctx->sms, s, d, rec, count, cap, offset, batch), "train launch");
+    if ((st = cache_gradient_pass(k, rec, count, cap, offset, batch)) != VG_OK)
+        return st;
     k->step++;
     NrcAdam a;
     a.lr = k->cfg.learning_rate;
@@ -106,11 +140,12 @@ int cache_train_step(VgCache* k, const float* rec, const uint32_t* count, uint32
     a.bc1 = (float)(1.0 - std::pow((double)k->cfg.beta1, (double)k->step));
     a.bc2 = (float)(1.0 - std::pow((double)k->cfg.beta2, (double)k->step));
     VG_CHECK(vgx::nrc_launch_adam(s, (float*)k->mlp.p, (float*)k->mlp_grad.p, (float*)k->mlp_m.p, (float*)k->mlp_v.p,
-                                  vgn::MLP_PARAMS, count, cap, offset, batch, a, nullptr),
+                                  vgn::MLP_PARAMS, count, cap, offset, batch, a, nullptr, false),
              "adam");
     VG_CHECK(vgx::nrc_launch_pack(s, (const float*)k->mlp.p, (uint8_t*)k->img.p), "weight image");
     VG_CHECK(vgx::nrc_launch_adam(s, (float*)k->grid.p, (float*)k->grid_grad.p, (float*)k->grid_m.p,
-                                  (float*)k->grid_v.p, k->grid_params, count, cap, offset, batch, a, k->grid_h.p),
+                                  (float*)k->grid_v.p, k->grid_params, count, cap, offset, batch, a, k->grid_h.p,
+                                  true),
              "adam");
     return VG_OK;
 }
@@ -161,6 +196,8 @@ int cache_accumulate(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, uint32_t samples,
     a.trec = (float*)acc->cache_t.p;
     a.tcount = ctr + 1;
     a.tcap = tcap;
+    if ((st = ensure_work(k, std::max<size_t>(px, r->cache_batch))) != VG_OK)
+        return st;
     dim3 grid((acc->width + 15) / 16, (acc->height + 7) / 8);
     vgn::CacheDev d = k->dev();
     bool f64 = acc->precision == 64;
@@ -179,7 +216,10 @@ int cache_accumulate(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, uint32_t samples,
         VG_CHECK(vgx::nrc_launch_paths(f64, grid, s, c, a), "cache path launch");
         if (timed)
             VG_CHECK(cudaEventRecord(e1, s), "event");
-        VG_CHECK(vgx::nrc_launch_infer(4 * r->ctx->sms, s, d, a.qrec, ctr, a.qcap, nullptr, c.accum, f64 ? 64 : 32),
+        VG_CHECK(vgx::nrc_launch_encode(encode_blocks(k), s, d, a.qrec, ctr, a.qcap, 0, a.qcap, (uint8_t*)k->X.p),
+                 "cache encode launch");
+        VG_CHECK(vgx::nrc_launch_infer(3 * r->ctx->sms, s, d, (const uint8_t*)k->X.p, a.qrec, ctr, a.qcap, nullptr,
+                                       c.accum, f64 ? 64 : 32),
                  "cache inference launch");
         if (timed)
             VG_CHECK(cudaEventRecord(e2, s), "event");
@@ -187,7 +227,7 @@ int cache_accumulate(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, uint32_t samples,
         for (uint32_t t = 0; t < r->cache_steps; t++) {
             if ((st = cache_train_step(k, a.trec, ctr + 1, tcap, t * r->cache_batch, r->cache_batch)) != VG_OK)
                 return st;
-            acc->launches += 4;
+            acc->launches += 6;
         }
         if (timed) {
             VG_CHECK(cudaEventRecord(e3, s), "event");
@@ -366,11 +406,17 @@ int vg_cache_infer(VgCache* k, const float* records, size_t n, float* out)
         return VG_OK;
     DevBuf rec, o;
     int st;
-    if ((st = stage_records(k, rec, records, n)) != VG_OK || (st = alloc(o, n * 12, k->ctx->stream, false)) != VG_OK)
+    if ((st = stage_records(k, rec, records, n)) != VG_OK || (st = alloc(o, n * 12, k->ctx->stream, false)) != VG_OK ||
+        (st = ensure_work(k, n)) != VG_OK)
         return st;
     cudaStream_t s = k->ctx->stream;
+    vgn::CacheDev d = k->dev();
+    const uint32_t* cnt = (const uint32_t*)k->count.p;
     VG_CHECK(cudaMemsetAsync(k->err.p, 0, 4, s), "error flag");
-    VG_CHECK(vgx::nrc_launch_infer(4 * k->ctx->sms, s, k->dev(), (const float*)rec.p, (const uint32_t*)k->count.p,
+    VG_CHECK(vgx::nrc_launch_encode(encode_blocks(k), s, d, (const float*)rec.p, cnt, (uint32_t)n, 0, (uint32_t)n,
+                                    (uint8_t*)k->X.p),
+             "encode launch");
+    VG_CHECK(vgx::nrc_launch_infer(3 * k->ctx->sms, s, d, (const uint8_t*)k->X.p, (const float*)rec.p, cnt,
                                    (uint32_t)n, (float*)o.p, nullptr, 32),
              "inference launch");
     VG_CHECK(cudaMemcpyAsync(out, o.p, n * 12, cudaMemcpyDeviceToHost, s), "readback");
@@ -385,17 +431,16 @@ int vg_cache_gradients(VgCache* k, const float* records, size_t n, float* mlp_gr
         return fail(VG_ERR_INVALID, "too many records");
     DevBuf rec;
     int st;
-    if ((st = stage_records(k, rec, records, n)) != VG_OK)
+    if ((st = stage_records(k, rec, records, n)) != VG_OK || (st = ensure_work(k, n)) != VG_OK)
         return st;
     cudaStream_t s = k->ctx->stream;
     VG_CHECK(cudaMemsetAsync(k->err.p, 0, 4, s), "error flag");
     VG_CHECK(cudaMemsetAsync(k->mlp_grad.p, 0, k->mlp_grad.bytes, s), "clear");
     VG_CHECK(cudaMemsetAsync(k->grid_grad.p, 0, k->grid_grad.bytes, s), "clear");
     VG_CHECK(cudaMemsetAsync(k->loss.p, 0, 8, s), "clear");
-    if (n > 0)
-        VG_CHECK(vgx::nrc_launch_train(k->ctx->sms, s, k->dev(), (const float*)rec.p, (const uint32_t*)k->count.p,
-                                       (uint32_t)n, 0, (uint32_t)n),
-                 "train launch");
+    if (n > 0 && (st = cache_gradient_pass(k, (const float*)rec.p, (const uint32_t*)k->count.p, (uint32_t)n, 0,
+                                           (uint32_t)n)) != VG_OK)
+        return st;
     if (mlp_grad)
         VG_CHECK(cudaMemcpyAsync(mlp_grad, k->mlp_grad.p, vgn::MLP_PARAMS * 4, cudaMemcpyDeviceToHost, s), "readback");
     if (grid_grad)
@@ -420,7 +465,7 @@ int vg_cache_train(VgCache* k, const float* records, size_t n, uint32_t batch, d
         return fail(VG_ERR_INVALID, "batch must be non-zero");
     DevBuf rec;
     int st;
-    if ((st = stage_records(k, rec, records, n)) != VG_OK)
+    if ((st = stage_records(k, rec, records, n)) != VG_OK || (st = ensure_work(k, std::min<size_t>(n, batch))) != VG_OK)
         return st;
     cudaStream_t s = k->ctx->stream;
     VG_CHECK(cudaMemsetAsync(k->err.p, 0, 4, s), "error flag");

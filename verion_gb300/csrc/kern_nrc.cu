@@ -153,8 +153,9 @@ static __device__ __forceinline__ void store_col(uint8_t* tile, uint32_t region,
 static __device__ __forceinline__ void load_acc(uint32_t taddr, float* v, int cols)
 {
     tmem_ld16(taddr, v);
-    if (cols > 16) {
+    if (cols > 16)
         tmem_ld16(taddr + 16, v + 16);
+    if (cols > 32) {
         tmem_ld16(taddr + 32, v + 32);
         tmem_ld16(taddr + 48, v + 48);
     }
@@ -173,25 +174,81 @@ static __device__ __forceinline__ void issue_layer(uint32_t d, const uint8_t* A,
     }
 }
 
+// ---- encoding kernel ----------------------------------------------------------------------------
+
+// Rows [offset, end) of the first min(*count, cap) records, end = min(that, offset + limit),
+// encoded as the network's input tiles: tile t holds rows offset + 128 t ... in the MMA operand
+// layout (128 x 64 bf16, 128-byte swizzle), so a tile moves to shared memory in one bulk copy.
+// The padding rows of the last tile are zero.
+__global__ void __launch_bounds__(256) nrc_encode(CacheDev cd, const float* __restrict__ rec, const uint32_t* count,
+                                                  uint32_t cap, uint32_t offset, uint32_t limit, uint8_t* X)
+{
+    uint32_t n = min(*count, cap);
+    uint32_t end = offset < n ? min(n, offset + limit) : offset;
+    uint32_t rows = end - offset;
+    uint32_t padded = (rows + TILE - 1) / TILE * TILE;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < padded; r += gridDim.x * blockDim.x) {
+        float v[64];
+        if (r < rows) {
+            input_row(cd, rec + (size_t)(offset + r) * REC_WORDS, v);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 64; k++)
+                v[k] = 0.0f;
+        }
+        store_row(X + (size_t)(r / TILE) * 16384u, r % TILE, v);
+    }
+}
+
+// Scatters the input-gradient grid columns of rows [offset, end) (GX: 32 floats per row, row r of
+// the batch at GX + 32 r) to the table gradient.
+__global__ void __launch_bounds__(256) nrc_grid_scatter(CacheDev cd, const float* __restrict__ rec,
+                                                        const uint32_t* count, uint32_t cap, uint32_t offset,
+                                                        uint32_t limit, const float* __restrict__ GX)
+{
+    uint32_t n = min(*count, cap);
+    uint32_t end = offset < n ? min(n, offset + limit) : offset;
+    uint32_t rows = end - offset;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+        float g[32];
+        const float4* src = reinterpret_cast<const float4*>(GX + (size_t)r * 32);
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            float4 q = src[k];
+            g[4 * k] = q.x, g[4 * k + 1] = q.y, g[4 * k + 2] = q.z, g[4 * k + 3] = q.w;
+        }
+        grid_backward(cd, rec + (size_t)(offset + r) * REC_WORDS, g);
+    }
+}
+
 // ---- inference ----------------------------------------------------------------------------------
 
-// MODE 0: out[3 i + k] = prediction k of record i. MODE 1: the prediction, clamped at zero and
-// times the record's throughput, is added to the record's pixel in `accum`.
+// Over the encoded tiles X of the first min(*count, cap) records. MODE 0: out[3 i + k] =
+// prediction k of record i. MODE 1: the prediction, clamped at zero and times the record's
+// throughput, is added to the record's pixel in `accum`. Each CTA walks tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ... with two input buffers: the next tile's bulk copy runs while the
+// current one goes through the five layers (MMA into tensor memory, then bias-free ReLU epilogue
+// back into the same buffer as the next layer's operand).
 template <int MODE, typename A>
-__global__ void __launch_bounds__(128) nrc_infer(CacheDev cd, const float* __restrict__ rec, const uint32_t* count,
-                                                 uint32_t cap, float* out, A* accum)
+__global__ void __launch_bounds__(128) nrc_infer(CacheDev cd, const uint8_t* __restrict__ X,
+                                                 const float* __restrict__ rec, const uint32_t* count, uint32_t cap,
+                                                 float* out, A* accum)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* sm = align1024(smem_raw);
     uint8_t* W = sm;
-    uint8_t* H = sm + IMG_FWD_BYTES;
-    __shared__ uint64_t bar;
+    uint8_t* buf[2] = {sm + IMG_FWD_BYTES, sm + IMG_FWD_BYTES + 16384};
+    __shared__ uint64_t mbar, lbar[2];
     __shared__ uint32_t tslot;
     uint32_t tid = threadIdx.x, warp = tid >> 5;
+    uint32_t n = min(*count, cap);
+    uint32_t tiles = (n + TILE - 1) / TILE;
     for (uint32_t i = tid; i < IMG_FWD_BYTES / 16; i += blockDim.x)
         reinterpret_cast<uint4*>(W)[i] = __ldg(reinterpret_cast<const uint4*>(cd.img) + i);
     if (tid == 0) {
-        bar_init(&bar, 1);
+        bar_init(&mbar, 1);
+        bar_init(&lbar[0], 1);
+        bar_init(&lbar[1], 1);
         fence_bar_init();
     }
     if (warp == 0)
@@ -199,24 +256,29 @@ __global__ void __launch_bounds__(128) nrc_infer(CacheDev cd, const float* __res
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
+    uint32_t issued[2] = {0, 0}, used[2] = {0, 0}; // bulk copies per buffer (issued by thread 0)
+    if (tid == 0) {
+        for (uint32_t b = 0; b < 2; b++) {
+            uint32_t t = blockIdx.x + b * gridDim.x;
+            if (t < tiles) {
+                bar_expect_tx(&lbar[b], 16384);
+                bulk_g2s(buf[b], X + (size_t)t * 16384u, 16384, &lbar[b]);
+                issued[b]++;
+            }
+        }
+    }
     uint32_t tmem = tslot;
     uint32_t lane_addr = tmem + ((warp * 32u) << 16);
-    uint32_t n = min(*count, cap);
-    uint32_t tiles = (n + TILE - 1) / TILE;
     uint32_t phase = 0;
     bool ok = true;
-    for (uint32_t t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
-        uint32_t i = t * TILE + tid;
-        bool valid = i < n;
+    uint32_t k = 0;
+    for (uint32_t t = blockIdx.x; t < tiles && ok; t += gridDim.x, k++) {
+        uint8_t* H = buf[k & 1u];
+        ok = __syncthreads_and(wait_mma(&lbar[k & 1u], (k >> 1) & 1u)) != 0;
+        if (!ok)
+            break;
+        used[k & 1u]++;
         float v[64];
-        if (valid) {
-            input_row(cd, rec + (size_t)i * REC_WORDS, v);
-        } else {
-#pragma unroll
-            for (int k = 0; k < 64; k++)
-                v[k] = 0.0f;
-        }
-        store_row(H, tid, v);
         for (uint32_t l = 0; l < 5 && ok; l++) {
             fence_async_smem();
             __syncthreads();
@@ -224,9 +286,9 @@ __global__ void __launch_bounds__(128) nrc_infer(CacheDev cd, const float* __res
             if (tid == 0) {
                 const uint8_t* B = W + (l < 4 ? IMG_W + l * 8192u : IMG_W4);
                 issue_layer(tmem, H, 0, B, 0, l < 4 ? 64u : 16u, 4, false);
-                mma_commit(&bar);
+                mma_commit(&mbar);
             }
-            bool done = wait_mma(&bar, phase);
+            bool done = wait_mma(&mbar, phase);
             phase ^= 1u;
             ok = __syncthreads_and(done) != 0;
             if (!ok)
@@ -236,14 +298,15 @@ __global__ void __launch_bounds__(128) nrc_infer(CacheDev cd, const float* __res
             tc_fence_before();
             if (l < 4) {
 #pragma unroll
-                for (int k = 0; k < 64; k++)
-                    v[k] = fmaxf(v[k], 0.0f);
+                for (int q = 0; q < 64; q++)
+                    v[q] = fmaxf(v[q], 0.0f);
                 store_row(H, tid, v);
             }
         }
         if (!ok)
             break;
-        if (valid) {
+        uint32_t i = t * TILE + tid;
+        if (i < n) {
             if (MODE == 0) {
                 out[3 * (size_t)i] = v[0];
                 out[3 * (size_t)i + 1] = v[1];
@@ -257,9 +320,24 @@ __global__ void __launch_bounds__(128) nrc_infer(CacheDev cd, const float* __res
                 a[2] += (A)(r[18] * fmaxf(v[2], 0.0f));
             }
         }
+        // The buffer is free (its last reader, the output layer's MMA, has completed): refill it
+        // with the tile after next once the generic writes are ordered before the async copy.
+        fence_async_smem();
+        __syncthreads();
+        uint32_t nt = t + 2 * gridDim.x;
+        if (tid == 0 && nt < tiles) {
+            bar_expect_tx(&lbar[k & 1u], 16384);
+            bulk_g2s(H, X + (size_t)nt * 16384u, 16384, &lbar[k & 1u]);
+            issued[k & 1u]++;
+        }
     }
-    if (!ok && tid == 0)
+    // After an early stop, a copy still in flight must land (bounded wait) before the CTA exits.
+    if (!ok && tid == 0) {
         atomicOr(cd.err, ERR_MMA_TIMEOUT);
+        for (uint32_t b = 0; b < 2; b++)
+            if (issued[b] > used[b])
+                wait_mma(&lbar[b], used[b] & 1u);
+    }
     tc_fence_before();
     __syncthreads();
     if (warp == 0)
@@ -269,22 +347,24 @@ __global__ void __launch_bounds__(128) nrc_infer(CacheDev cd, const float* __res
 // ---- training -----------------------------------------------------------------------------------
 
 // Shared-memory plan of the training kernel (bytes from a 1024-aligned base).
-constexpr uint32_t T_H = IMG_BYTES;            // 128 x 64 activations (forward A operand)
+constexpr uint32_t T_H = IMG_BYTES;            // 128 x 64 inputs, then activations (forward A operand)
 constexpr uint32_t T_HT = T_H + 16384;         // 5 transposed activations, 64 x 128 each
 constexpr uint32_t T_G = T_HT + 5 * 16384;     // 128 x 64 gradients (backward A operand)
 constexpr uint32_t T_GT = T_G + 16384;         // 128 x 128 transposed gradients, rows 64..127 zero
 constexpr uint32_t T_END = T_GT + 32768;       // 223,232
 constexpr uint32_t TRAIN_SMEM = T_END + 1024;  // with the alignment slack
-constexpr uint32_t INFER_SMEM = IMG_FWD_BYTES + 16384 + 1024;
+constexpr uint32_t INFER_SMEM = IMG_FWD_BYTES + 2 * 16384 + 1024;
 
-// One training pass over records [offset, offset + batch) of the first min(*count, cap): the
-// relative L2 loss sum_k (p_k - y_k)^2 / (p_k^2 + 0.01) (denominator held constant) is summed
-// into cd.loss, its parameter gradients into cd.mlp_grad and cd.grid_grad. Per 128-record tile:
-// forward (5 MMA layers), then for each layer from the last, the weight gradient
-// dW_l += G^T H_l (accumulated in tensor memory over the tiles of this CTA) and the data
-// gradient G W_l, masked by the ReLU of the layer below.
-__global__ void __launch_bounds__(128, 1) nrc_train(CacheDev cd, const float* __restrict__ rec, const uint32_t* count,
-                                                    uint32_t cap, uint32_t offset, uint32_t batch)
+// One training pass over the encoded tiles X of records [offset, end) (end as in nrc_encode):
+// the relative L2 loss sum_k (p_k - y_k)^2 / (p_k^2 + 0.01) (denominator held constant) is
+// summed into cd.loss and its weight gradients into cd.mlp_grad; the gradient of the 32 grid
+// inputs of batch row r goes to GX + 32 r (nrc_grid_scatter takes it to the table). Per
+// 128-record tile: forward (5 MMA layers), then for each layer from the last, the weight
+// gradient dW_l += G^T H_l (accumulated in tensor memory over the tiles of this CTA) and the
+// data gradient G W_l, masked by the ReLU of the layer below.
+__global__ void __launch_bounds__(128, 1) nrc_train(CacheDev cd, const uint8_t* __restrict__ X,
+                                                    const float* __restrict__ rec, const uint32_t* count,
+                                                    uint32_t cap, uint32_t offset, uint32_t batch, float* GX)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* sm = align1024(smem_raw);
@@ -293,7 +373,7 @@ __global__ void __launch_bounds__(128, 1) nrc_train(CacheDev cd, const float* __
     uint8_t* HT = sm + T_HT;
     uint8_t* G = sm + T_G;
     uint8_t* GT = sm + T_GT;
-    __shared__ uint64_t bar;
+    __shared__ uint64_t mbar, lbar;
     __shared__ uint32_t tslot;
     __shared__ float red[4];
     uint32_t tid = threadIdx.x, warp = tid >> 5;
@@ -302,7 +382,8 @@ __global__ void __launch_bounds__(128, 1) nrc_train(CacheDev cd, const float* __
     for (uint32_t i = tid; i < 32768 / 16; i += blockDim.x)
         reinterpret_cast<uint4*>(GT)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
-        bar_init(&bar, 1);
+        bar_init(&mbar, 1);
+        bar_init(&lbar, 1);
         fence_bar_init();
     }
     if (warp == 0)
@@ -315,22 +396,39 @@ __global__ void __launch_bounds__(128, 1) nrc_train(CacheDev cd, const float* __
     uint32_t n = min(*count, cap);
     uint32_t end = offset < n ? min(n, offset + batch) : offset;
     uint32_t tiles = end > offset ? (end - offset + TILE - 1) / TILE : 0;
-    uint32_t phase = 0;
-    bool ok = true, first = true;
+    uint32_t phase = 0, lphase = 0;
+    bool ok = true, first = true, copy_late = false;
     float loss = 0.0f;
     for (uint32_t t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
-        uint32_t i = offset + t * TILE + tid;
+        // The previous tile is done with H: bring in this tile's inputs.
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            bar_expect_tx(&lbar, 16384);
+            bulk_g2s(H, X + (size_t)t * 16384u, 16384, &lbar);
+        }
+        ok = __syncthreads_and(wait_mma(&lbar, lphase)) != 0;
+        if (!ok) {
+            copy_late = true;
+            break;
+        }
+        lphase ^= 1u;
+        uint32_t row = t * TILE + tid;
+        uint32_t i = offset + row;
         bool valid = i < end;
         const float* r = rec + (size_t)i * REC_WORDS;
         float v[64];
-        if (valid) {
-            input_row(cd, r, v);
-        } else {
 #pragma unroll
-            for (int k = 0; k < 64; k++)
-                v[k] = 0.0f;
+        for (uint32_t j = 0; j < 8; j++) {
+            uint4 q = *reinterpret_cast<const uint4*>(H + tid * 128u + (((j ^ tid) & 7u) << 4));
+            const __nv_bfloat162* h2 = reinterpret_cast<const __nv_bfloat162*>(&q);
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                float2 f = __bfloat1622float2(h2[e]);
+                v[8 * j + 2 * e] = f.x;
+                v[8 * j + 2 * e + 1] = f.y;
+            }
         }
-        store_row(H, tid, v);
         store_col(HT, 8192, tid, v);
         uint32_t mask[4][2];
         // Forward.
@@ -342,9 +440,9 @@ __global__ void __launch_bounds__(128, 1) nrc_train(CacheDev cd, const float* __
             if (tid == 0) {
                 const uint8_t* B = W + (l < 4 ? IMG_W + l * 8192u : IMG_W4);
                 issue_layer(tmem, H, 0, B, 0, l < 4 ? 64u : 16u, 4, false);
-                mma_commit(&bar);
+                mma_commit(&mbar);
             }
-            bool done = wait_mma(&bar, phase);
+            bool done = wait_mma(&mbar, phase);
             phase ^= 1u;
             ok = __syncthreads_and(done) != 0;
             if (!ok)
@@ -355,13 +453,13 @@ __global__ void __launch_bounds__(128, 1) nrc_train(CacheDev cd, const float* __
             if (l < 4) {
                 uint32_t m0 = 0, m1 = 0;
 #pragma unroll
-                for (int k = 0; k < 64; k++) {
-                    bool on = v[k] > 0.0f;
-                    if (k < 32)
-                        m0 |= (on ? 1u : 0u) << k;
+                for (int q = 0; q < 64; q++) {
+                    bool on = v[q] > 0.0f;
+                    if (q < 32)
+                        m0 |= (on ? 1u : 0u) << q;
                     else
-                        m1 |= (on ? 1u : 0u) << (k - 32);
-                    v[k] = on ? v[k] : 0.0f;
+                        m1 |= (on ? 1u : 0u) << (q - 32);
+                    v[q] = on ? v[q] : 0.0f;
                 }
                 mask[l][0] = m0;
                 mask[l][1] = m1;
@@ -374,15 +472,15 @@ __global__ void __launch_bounds__(128, 1) nrc_train(CacheDev cd, const float* __
         // Loss gradient of the three outputs.
         float g[64];
 #pragma unroll
-        for (int k = 0; k < 64; k++)
-            g[k] = 0.0f;
+        for (int q = 0; q < 64; q++)
+            g[q] = 0.0f;
         if (valid) {
 #pragma unroll
-            for (int k = 0; k < 3; k++) {
-                float d = v[k] - r[16 + k];
-                float den = v[k] * v[k] + 0.01f;
+            for (int q = 0; q < 3; q++) {
+                float d = v[q] - r[16 + q];
+                float den = v[q] * v[q] + 0.01f;
                 loss += d * d / den;
-                g[k] = 2.0f * d / den;
+                g[q] = 2.0f * d / den;
             }
         }
         store_row(G, tid, g);
@@ -397,26 +495,29 @@ __global__ void __launch_bounds__(128, 1) nrc_train(CacheDev cd, const float* __
                 issue_layer(tmem + 64u + 64u * l, GT, 16384, HT + l * 16384u, 8192, 64, 8, !first);
                 const uint8_t* B = W + (l == 4 ? IMG_W4T : IMG_WT + l * 8192u);
                 issue_layer(tmem, G, 0, B, 0, 64, l == 4 ? 1u : 4u, false);
-                mma_commit(&bar);
+                mma_commit(&mbar);
             }
-            bool done = wait_mma(&bar, phase);
+            bool done = wait_mma(&mbar, phase);
             phase ^= 1u;
             ok = __syncthreads_and(done) != 0;
             if (!ok)
                 break;
             tc_fence_after();
-            load_acc(lane_addr, g, 64);
+            load_acc(lane_addr, g, l > 0 ? 64 : 32);
             tc_fence_before();
             if (l > 0) {
 #pragma unroll
-                for (int k = 0; k < 64; k++) {
-                    uint32_t bit = k < 32 ? (mask[l - 1][0] >> k) & 1u : (mask[l - 1][1] >> (k - 32)) & 1u;
-                    g[k] = bit ? g[k] : 0.0f;
+                for (int q = 0; q < 64; q++) {
+                    uint32_t bit = q < 32 ? (mask[l - 1][0] >> q) & 1u : (mask[l - 1][1] >> (q - 32)) & 1u;
+                    g[q] = bit ? g[q] : 0.0f;
                 }
                 store_row(G, tid, g);
                 store_col(GT, 16384, tid, g);
             } else if (valid) {
-                grid_backward(cd, r, g);
+                float4* dst = reinterpret_cast<float4*>(GX + (size_t)row * 32);
+#pragma unroll
+                for (int q = 0; q < 8; q++)
+                    dst[q] = make_float4(g[4 * q], g[4 * q + 1], g[4 * q + 2], g[4 * q + 3]);
             }
         }
         first = false;
@@ -432,13 +533,16 @@ __global__ void __launch_bounds__(128, 1) nrc_train(CacheDev cd, const float* __
             if (tid < rows) {
                 float* dst = cd.mlp_grad + mlp_offset(l) + tid * WIDTH;
 #pragma unroll
-                for (int k = 0; k < 64; k++)
-                    atomicAdd(dst + k, v[k]);
+                for (int q = 0; q < 64; q++)
+                    atomicAdd(dst + q, v[q]);
             }
         }
     }
-    if (!ok && tid == 0)
+    if (!ok && tid == 0) {
         atomicOr(cd.err, ERR_MMA_TIMEOUT);
+        if (copy_late)
+            wait_mma(&lbar, lphase); // the input copy must land before the CTA exits
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
         loss += __shfl_xor_sync(FULLM, loss, o);
@@ -457,8 +561,10 @@ __global__ void __launch_bounds__(128, 1) nrc_train(CacheDev cd, const float* __
 // Adam (Kingma and Ba 2015) on the gradient sums of the step, scaled by 1 / (3 x records used);
 // a step without records changes nothing. The gradient sums are cleared. With `half_out` the
 // updated parameter is also written as fp16 (the grid table).
+// With `lazy`, entries whose gradient sum is exactly zero are left alone (their moments do not
+// decay): the grid table, where a step touches a small fraction of the entries.
 __global__ void nrc_adam(float* p, float* g, float* m, float* v, size_t n, const uint32_t* count, uint32_t cap,
-                         uint32_t offset, uint32_t batch, NrcAdam a, __half* half_out)
+                         uint32_t offset, uint32_t batch, NrcAdam a, __half* half_out, bool lazy)
 {
     uint32_t avail = min(*count, cap);
     uint32_t used = avail > offset ? min(batch, avail - offset) : 0u;
@@ -466,7 +572,10 @@ __global__ void nrc_adam(float* p, float* g, float* m, float* v, size_t n, const
         return;
     float scale = 1.0f / (3.0f * (float)used);
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        float gi = g[i] * scale;
+        float gs = g[i];
+        if (lazy && gs == 0.0f)
+            continue;
+        float gi = gs * scale;
         g[i] = 0.0f;
         float mi = a.beta1 * m[i] + (1.0f - a.beta1) * gi;
         float vi = a.beta2 * v[i] + (1.0f - a.beta2) * gi * gi;
@@ -613,7 +722,21 @@ namespace vgx {
 
 using namespace vgnk;
 
-cudaError_t nrc_launch_infer(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const float* rec,
+cudaError_t nrc_launch_encode(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const float* rec,
+                              const uint32_t* count, uint32_t cap, uint32_t offset, uint32_t limit, uint8_t* X)
+{
+    nrc_encode<<<blocks, 256, 0, s>>>(cd, rec, count, cap, offset, limit, X);
+    return cudaGetLastError();
+}
+
+cudaError_t nrc_launch_scatter(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const float* rec,
+                               const uint32_t* count, uint32_t cap, uint32_t offset, uint32_t limit, const float* GX)
+{
+    nrc_grid_scatter<<<blocks, 256, 0, s>>>(cd, rec, count, cap, offset, limit, GX);
+    return cudaGetLastError();
+}
+
+cudaError_t nrc_launch_infer(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const uint8_t* X, const float* rec,
                              const uint32_t* count, uint32_t cap, float* out, void* accum, int accum_bits)
 {
     static bool init = false;
@@ -624,31 +747,31 @@ cudaError_t nrc_launch_infer(int blocks, cudaStream_t s, const vgn::CacheDev& cd
         init = true;
     }
     if (!accum)
-        nrc_infer<0, float><<<blocks, 128, INFER_SMEM, s>>>(cd, rec, count, cap, out, (float*)nullptr);
+        nrc_infer<0, float><<<blocks, 128, INFER_SMEM, s>>>(cd, X, rec, count, cap, out, (float*)nullptr);
     else if (accum_bits == 64)
-        nrc_infer<1, double><<<blocks, 128, INFER_SMEM, s>>>(cd, rec, count, cap, nullptr, (double*)accum);
+        nrc_infer<1, double><<<blocks, 128, INFER_SMEM, s>>>(cd, X, rec, count, cap, nullptr, (double*)accum);
     else
-        nrc_infer<1, float><<<blocks, 128, INFER_SMEM, s>>>(cd, rec, count, cap, nullptr, (float*)accum);
+        nrc_infer<1, float><<<blocks, 128, INFER_SMEM, s>>>(cd, X, rec, count, cap, nullptr, (float*)accum);
     return cudaGetLastError();
 }
 
-cudaError_t nrc_launch_train(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const float* rec,
-                             const uint32_t* count, uint32_t cap, uint32_t offset, uint32_t batch)
+cudaError_t nrc_launch_train(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const uint8_t* X, const float* rec,
+                             const uint32_t* count, uint32_t cap, uint32_t offset, uint32_t batch, float* GX)
 {
     static bool init = false;
     if (!init) {
         cudaFuncSetAttribute(nrc_train, cudaFuncAttributeMaxDynamicSharedMemorySize, TRAIN_SMEM);
         init = true;
     }
-    nrc_train<<<blocks, 128, TRAIN_SMEM, s>>>(cd, rec, count, cap, offset, batch);
+    nrc_train<<<blocks, 128, TRAIN_SMEM, s>>>(cd, X, rec, count, cap, offset, batch, GX);
     return cudaGetLastError();
 }
 
 cudaError_t nrc_launch_adam(cudaStream_t s, float* p, float* g, float* m, float* v, size_t n, const uint32_t* count,
-                            uint32_t cap, uint32_t offset, uint32_t batch, const NrcAdam& a, void* half_out)
+                            uint32_t cap, uint32_t offset, uint32_t batch, const NrcAdam& a, void* half_out, bool lazy)
 {
-    int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
-    nrc_adam<<<blocks, 256, 0, s>>>(p, g, m, v, n, count, cap, offset, batch, a, (__half*)half_out);
+    int blocks = (int)std::min<size_t>((n + 255) / 256, 8192);
+    nrc_adam<<<blocks, 256, 0, s>>>(p, g, m, v, n, count, cap, offset, batch, a, (__half*)half_out, lazy);
     return cudaGetLastError();
 }
 

@@ -24,12 +24,18 @@ struct NrcPathArgs {
 
 namespace vgx {
 
-cudaError_t nrc_launch_infer(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const float* rec,
+// Input tiles of records [offset, offset + limit) of the first min(*count, cap) (kern_nrc.cu).
+cudaError_t nrc_launch_encode(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const float* rec,
+                              const uint32_t* count, uint32_t cap, uint32_t offset, uint32_t limit, uint8_t* X);
+cudaError_t nrc_launch_scatter(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const float* rec,
+                               const uint32_t* count, uint32_t cap, uint32_t offset, uint32_t limit, const float* GX);
+cudaError_t nrc_launch_infer(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const uint8_t* X, const float* rec,
                              const uint32_t* count, uint32_t cap, float* out, void* accum, int accum_bits);
-cudaError_t nrc_launch_train(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const float* rec,
-                             const uint32_t* count, uint32_t cap, uint32_t offset, uint32_t batch);
+cudaError_t nrc_launch_train(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const uint8_t* X, const float* rec,
+                             const uint32_t* count, uint32_t cap, uint32_t offset, uint32_t batch, float* GX);
 cudaError_t nrc_launch_adam(cudaStream_t s, float* p, float* g, float* m, float* v, size_t n, const uint32_t* count,
-                            uint32_t cap, uint32_t offset, uint32_t batch, const NrcAdam& a, void* half_out);
+                            uint32_t cap, uint32_t offset, uint32_t batch, const NrcAdam& a, void* half_out,
+                            bool lazy);
 cudaError_t nrc_launch_to_half(cudaStream_t s, const float* p, void* out, size_t n);
 cudaError_t nrc_launch_pack(cudaStream_t s, const float* w, uint8_t* img);
 cudaError_t nrc_launch_paths(bool f64, dim3 grid, cudaStream_t s, const vgd::Ctx& c, const NrcPathArgs& a);

@@ -82,6 +82,22 @@ static __device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity, 
     return false;
 }
 
+// Arms the mbarrier for `bytes` of asynchronous copies (counts as the one expected arrival).
+static __device__ __forceinline__ void bar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// Bulk (TMA) copy of `bytes` (a multiple of 16, both addresses 16-byte aligned) from global to
+// shared memory, completing on the mbarrier.
+static __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
 // Generic-proxy shared-memory writes become visible to the tensor core (async proxy).
 static __device__ __forceinline__ void fence_async_smem()
 {
