@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--integrator", choices=["wavefront", "megakernel"], default="wavefront")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cache", action="store_true", help="skip the radiance-cache measurement")
     ap.add_argument("--width", type=int, default=WIDTH, help="smaller frames are for profiling runs only")
     ap.add_argument("--height", type=int, default=HEIGHT)
     a = ap.parse_args()
@@ -246,6 +247,109 @@ def run_reference(args):
     return 0
 
 
+CACHE_W = CACHE_H = 512
+CACHE_REF_SPP = 8192
+CACHE_MLP_FLOP = 2 * (4 * 64 * 64 + 64 * 3)  # per record, inference (algorithmic, 3 outputs)
+
+
+def _rmse(a, b):
+    return float(np.sqrt(np.mean((a - b) ** 2)))
+
+
+def _time_at(curve, target):
+    """First time (log-log interpolation between points) at which the curve's RMSE reaches target."""
+    for (t0, e0), (t1, e1) in zip(curve, curve[1:]):
+        if e1 <= target < e0 or (e0 <= target and t0 == curve[0][0]):
+            if e0 <= target:
+                return t0
+            f = (math.log(e0) - math.log(target)) / (math.log(e0) - math.log(e1))
+            return math.exp(math.log(t0) + f * (math.log(t1) - math.log(t0)))
+    return None
+
+
+def _rmse_at(curve, t):
+    for (t0, e0), (t1, e1) in zip(curve, curve[1:]):
+        if t0 <= t <= t1:
+            f = (math.log(t) - math.log(t0)) / (math.log(t1) - math.log(t0))
+            return math.exp(math.log(e0) + f * (math.log(e1) - math.log(e0)))
+    return None
+
+
+def cache_report(ctx, peak_tflops, peak_kind):
+    """Radiance cache on the Cornell box (512 x 512, depth 8, 32 triangles): plain megakernel path
+    tracing against the cache integrator, RMSE against an 8192-spp plain image over GPU time, and
+    the MLP kernels' device time on 2^20 synthetic records against the tensor roofline."""
+    from verion_gb300 import pack, scenes
+    from verion_gb300.backend import Cache, Renderer
+
+    p = pack.pack(scenes.cornell())
+    ref_r = Renderer(ctx, p)
+    acc = ref_r.new_accumulation(CACHE_W, CACHE_H)
+    for _ in range(CACHE_REF_SPP // 512):
+        ref_r.accumulate(acc, 512)
+    ref = acc.mean()
+    del acc
+    plain_r = Renderer(ctx, p)
+    acc = plain_r.new_accumulation(CACHE_W, CACHE_H)
+    plain, n = [], 0
+    for k in (32, 32, 64, 128, 256, 512):
+        plain_r.accumulate(acc, k)
+        n += k
+        plain.append((acc.gpu_seconds(), _rmse(acc.mean(), ref)))
+    plain_spp_ms = 1e3 * acc.gpu_seconds() / n
+    del acc
+    r = Renderer(ctx, p)
+    cache = Cache(ctx, bounds=r.bounds())
+    r.set_cache(cache, spread=0.01, train_paths=16384, train_steps=4, train_batch=16384)
+    r.set_stage_timing(True)
+    acc = r.new_accumulation(CACHE_W, CACHE_H)
+    curve, n = [], 0
+    for k in (32, 32, 64, 128, 256, 512, 1024):
+        r.accumulate(acc, k)
+        n += k
+        curve.append((acc.gpu_seconds(), _rmse(acc.mean(), ref)))
+    img = acc.mean()
+    st = acc.cache_stats()
+    frame_ms = 1e3 * acc.gpu_seconds() / n
+    target = plain[-1][1]
+    t_plain = plain[-1][0]
+    t_cache = _time_at(curve, target)
+    # MLP kernels on synthetic records (random positions in the scene box, unit directions).
+    rng = np.random.default_rng(5)
+    nrec = 1 << 20
+    lo, hi = r.bounds()
+    rec = np.zeros((nrec, 20), np.float32)
+    rec[:, 0:3] = rng.uniform(lo, hi, (nrec, 3))
+    for o in (3, 6):
+        d = rng.normal(size=(nrec, 3))
+        rec[:, o:o + 3] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rec[:, 9:15] = rng.uniform(0, 1, (nrec, 6))
+    rec[:, 16:19] = rng.uniform(0, 2, (nrec, 3))
+    kt = cache.time_kernels(rec, reps=10)
+    infer_tf = CACHE_MLP_FLOP * nrec / kt["infer"] / 1e12
+    train_tf = 3 * CACHE_MLP_FLOP * nrec / kt["train"] / 1e12
+    return {
+        "config": "Cornell box 512x512, depth 8, 1 sample per pixel per frame; cache 16 levels x 2^19 entries x 2 fp16, "
+                  "MLP 64 x 4 hidden bf16; 4 Adam steps of 16384 records per frame from ~16384 training paths; "
+                  f"reference {CACHE_REF_SPP} spp plain",
+        "plain_ms_per_spp": plain_spp_ms, "cache_ms_per_frame": frame_ms,
+        "cache_split_seconds": {"paths": st.path_seconds, "encode_and_infer": st.infer_seconds,
+                                "train": st.train_seconds},
+        "queries_per_frame": st.queries, "train_records_per_frame": st.train_records,
+        "target_rmse": target, "target": f"plain RMSE at {sum((32, 32, 64, 128, 256, 512))} spp",
+        "time_to_target_s": {"plain": t_plain, "cache": t_cache},
+        "speedup": (t_plain / t_cache) if t_cache else None,
+        "rmse_equal_time": {"seconds": t_plain, "plain": target, "cache": _rmse_at(curve, t_plain)},
+        "cache_curve": curve, "plain_curve": plain,
+        "bias_rel_mean": float((img.mean() - ref.mean()) / ref.mean()),
+        "mlp_kernels": {"records": nrec, "seconds_per_launch": kt,
+                        "infer_tflops": infer_tf, "train_tflops": train_tf,
+                        "peak_tflops": peak_tflops, "peak_kind": peak_kind,
+                        "infer_frac": infer_tf / peak_tflops, "train_frac": train_tf / peak_tflops,
+                        "flop_per_record": {"infer": CACHE_MLP_FLOP, "train": 3 * CACHE_MLP_FLOP}},
+    }
+
+
 def run_cuda(args):
     rank, world = dist_init(args)
     import torch
@@ -375,6 +479,12 @@ def run_cuda(args):
                     "formula": "20 B/ray (queue id + hit record) + 24 B/ray past depth 0 (origin, direction) "
                                "+ 80 B/node visited + 48 B/triangle tested"}
 
+    cache = None
+    if rank == 0 and not args.no_cache:
+        bf = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("bf16_tflops") \
+            if (ROOT / "MEASURED_PEAKS.json").exists() else None
+        cache = cache_report(ctx, bf or 1900.0, "measured (bf16_tflops, burst)" if bf else "fallback")
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu, _ = cpu_baseline(packed, args.cpu_seconds)
@@ -390,7 +500,7 @@ def run_cuda(args):
                 "clocks": clk.summary(),
                 "stage_seconds": {"extend": stage[0], "shade": stage[1]},
                 "paths_per_step": paths_all / args.steps,
-                "megakernel_value": mega}
+                "megakernel_value": mega, "radiance_cache": cache}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

@@ -301,6 +301,11 @@ int vg_cache_gradients(VgCache* cache, const float* records, size_t n, float* ml
 /* Adam steps over consecutive batches of `batch` records (gradient = batch mean); *last_loss =
  * mean loss per channel of the last batch. */
 int vg_cache_train(VgCache* cache, const float* records, size_t n, uint32_t batch, double* last_loss);
+/* Device time per launch of the cache kernels on n records (one untimed round, then `reps`
+ * launches of each back to back): out = {encode, inference, training pass (forward, backward and
+ * weight gradients on the tensor cores), grid-gradient scatter} in seconds. Gradients are not
+ * applied. For measurement. */
+int vg_cache_time(VgCache* cache, const float* records, size_t n, uint32_t reps, double out[4]);
 /* Radiance-cache integrator for this renderer's accumulations (cache null: off). Each sample
  * traces one path per pixel that ends at the first vertex past the primary one where the path
  * spread passes `spread` times the primary spread (Mueller et al. 2021), and adds the cache's

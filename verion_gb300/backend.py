@@ -182,6 +182,7 @@ def lib() -> C.CDLL:
             "vg_cache_gradients": (i32, [vp, vp, _S, vp, vp, C.POINTER(f64)]),
             "vg_cache_train": (i32, [vp, vp, _S, u32, C.POINTER(f64)]),
             "vg_set_cache": (i32, [vp, vp, C.c_float, u32, u32, u32]),
+            "vg_cache_time": (i32, [vp, vp, _S, u32, C.POINTER(f64)]),
             "vg_accum_cache_stats": (i32, [vp, C.POINTER(CacheStats)]),
         }
         for name, (res, args) in sig.items():
@@ -623,6 +624,13 @@ class Cache:
         loss = C.c_double()
         _check(lib().vg_cache_train(self._h, _ptr(r), len(r), batch, C.byref(loss)))
         return loss.value
+
+    def time_kernels(self, records: np.ndarray, reps: int = 10) -> dict:
+        """Device seconds per launch of the encode, inference, training-pass and scatter kernels."""
+        r = self._records(records)
+        out = (C.c_double * 4)()
+        _check(lib().vg_cache_time(self._h, _ptr(r), len(r), reps, out))
+        return dict(zip(("encode", "infer", "train", "scatter"), list(out)))
 
     def close(self):
         if getattr(self, "_h", None):

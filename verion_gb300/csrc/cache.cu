@@ -485,6 +485,69 @@ int vg_cache_train(VgCache* k, const float* records, size_t n, uint32_t batch, d
     return VG_OK;
 }
 
+int vg_cache_time(VgCache* k, const float* records, size_t n, uint32_t reps, double out[4])
+{
+    if (!k || !records || !out || n == 0 || reps == 0)
+        return fail(VG_ERR_INVALID, "null argument or empty input");
+    if (n > 0x7fffffffull)
+        return fail(VG_ERR_INVALID, "too many records");
+    DevBuf rec, o;
+    int st;
+    if ((st = stage_records(k, rec, records, n)) != VG_OK || (st = ensure_work(k, n)) != VG_OK ||
+        (st = alloc(o, n * 12, k->ctx->stream, false)) != VG_OK)
+        return st;
+    cudaStream_t s = k->ctx->stream;
+    vgn::CacheDev d = k->dev();
+    const uint32_t* cnt = (const uint32_t*)k->count.p;
+    const float* rp = (const float*)rec.p;
+    uint32_t n32 = (uint32_t)n;
+    VG_CHECK(cudaMemsetAsync(k->err.p, 0, 4, s), "error flag");
+    EventPool pool;
+    cudaEvent_t ev[5];
+    for (int i = 0; i < 5; i++)
+        ev[i] = pool.get();
+    // One untimed round, then `reps` launches of each kernel back to back.
+    for (uint32_t round = 0; round < 2; round++) {
+        uint32_t m = round == 0 ? 1 : reps;
+        if (round == 1)
+            VG_CHECK(cudaEventRecord(ev[0], s), "event");
+        for (uint32_t i = 0; i < m; i++)
+            VG_CHECK(vgx::nrc_launch_encode(encode_blocks(k), s, d, rp, cnt, n32, 0, n32, (uint8_t*)k->X.p), "encode");
+        if (round == 1)
+            VG_CHECK(cudaEventRecord(ev[1], s), "event");
+        for (uint32_t i = 0; i < m; i++)
+            VG_CHECK(vgx::nrc_launch_infer(3 * k->ctx->sms, s, d, (const uint8_t*)k->X.p, rp, cnt, n32, (float*)o.p,
+                                           nullptr, 32),
+                     "infer");
+        if (round == 1)
+            VG_CHECK(cudaEventRecord(ev[2], s), "event");
+        for (uint32_t i = 0; i < m; i++)
+            VG_CHECK(vgx::nrc_launch_train(k->ctx->sms, s, d, (const uint8_t*)k->X.p, rp, cnt, n32, 0, n32,
+                                           (float*)k->GX.p),
+                     "train");
+        if (round == 1)
+            VG_CHECK(cudaEventRecord(ev[3], s), "event");
+        for (uint32_t i = 0; i < m; i++)
+            VG_CHECK(vgx::nrc_launch_scatter(encode_blocks(k), s, d, rp, cnt, n32, 0, n32, (const float*)k->GX.p),
+                     "scatter");
+        if (round == 1)
+            VG_CHECK(cudaEventRecord(ev[4], s), "event");
+    }
+    if ((st = wait_event(ev[4])) != VG_OK)
+        return st;
+    for (int i = 0; i < 4; i++) {
+        float ms = 0.0f;
+        VG_CHECK(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]), "event");
+        out[i] = ms * 1e-3 / reps;
+    }
+    if ((st = cache_check(k)) != VG_OK)
+        return st;
+    VG_CHECK(cudaMemsetAsync(k->mlp_grad.p, 0, k->mlp_grad.bytes, s), "clear");
+    VG_CHECK(cudaMemsetAsync(k->grid_grad.p, 0, k->grid_grad.bytes, s), "clear");
+    VG_CHECK(cudaStreamSynchronize(s), "clear");
+    return VG_OK;
+}
+
 int vg_set_cache(VgRenderer* r, VgCache* cache, float spread, uint32_t train_paths, uint32_t train_steps,
                  uint32_t train_batch)
 {
