@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-cache", action="store_true", help="skip the radiance-cache measurement")
+    ap.add_argument("--profile-extend", action="store_true",
+                    help="profiling helper: one step with traversal counters inside the NVTX range 'traffic', "
+                         "then print the counters (for an ncu capture of the extend kernels' DRAM bytes)")
     ap.add_argument("--width", type=int, default=WIDTH, help="smaller frames are for profiling runs only")
     ap.add_argument("--height", type=int, default=HEIGHT)
     a = ap.parse_args()
@@ -368,6 +371,22 @@ def run_cuda(args):
     r.set_accum_precision(64)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     total = args.warmup + args.steps
+
+    if args.profile_extend:
+        acc_p = r.new_accumulation(WIDTH, HEIGHT)
+        for _ in range(args.warmup):
+            r.accumulate(acc_p, SPP_STEP)
+        r.set_traversal_stats(True)
+        s0 = acc_p.traversal_stats()
+        flush.zero_()
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("traffic")
+        r.accumulate(acc_p, SPP_STEP)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        s1 = acc_p.traversal_stats()
+        print(json.dumps({k: s1[k] - s0[k] for k in s1}), flush=True)
+        return
 
     def paths_of(acc):
         st = acc.raw_stats()
