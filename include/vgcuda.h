@@ -134,6 +134,39 @@ int vg_memory(VgContext* ctx, VgMemoryUsage* out);
  * table is VG_ERR_SCENE (pack.rs:727-729). */
 int vg_renderer_create(VgContext* ctx, const VgPacked* packed, VgRenderer** out);
 void vg_renderer_destroy(VgRenderer* r);
+
+/* pack.rs:758-784 UpdatePlan: what a batch of scene edits makes the backend redo. `blases` lists
+ * the meshes whose vertices were rewritten in place (same vertex counts). */
+typedef struct VgUpdatePlan {
+    int full;      /* meshes or instances added or re-pointed: rebuild everything */
+    int materials; /* material and texture tables */
+    int lights;    /* light table, sky, environment map */
+    int emitters;  /* emitter table and CDF */
+    int instances; /* instance table */
+    int vertices;  /* vertex tables of the meshes in `blases` */
+    const uint32_t* blases;
+    size_t blas_count;
+    int tlas;      /* instance transforms changed */
+    int camera;
+} VgUpdatePlan;
+
+/* lib.rs:63-71 UpdateReport. */
+typedef struct VgUpdateReport {
+    uint64_t blases_built;
+    int tlas_built;
+    uint64_t bytes_uploaded;
+} VgUpdateReport;
+
+/* RayTracingBackend::update (lib.rs:23-27; Metal renderer.rs:226-349): applies the edits `plan`
+ * names, taking the tables of the edited scene from `packed` (pack::pack of the edited scene) and
+ * leaving everything else as it is. This backend's acceleration structure is one BVH8 over the
+ * world-space triangles of all instances, rebuilt when instance transforms or vertices change
+ * (`tlas_built`); `blases_built` counts the meshes whose vertex tables were rewritten (all meshes
+ * on a full rebuild). `bytes_uploaded` counts table and BVH bytes written to the device. Settings
+ * (integrator, adaptive, ReSTIR, depth, precision, cache) are kept. A deformation that changes a
+ * mesh's vertex count is VG_ERR_SCENE: that is a geometry change (plan.full). Start a new
+ * accumulation afterwards: samples from before the edit no longer match the scene. */
+int vg_renderer_update(VgRenderer* r, const VgPacked* packed, const VgUpdatePlan* plan, VgUpdateReport* out);
 int vg_renderer_bvh_info(const VgRenderer* r, VgBvhInfo* out);
 
 /* RayTracingBackend::set_camera (lib.rs:31) */
@@ -254,6 +287,52 @@ int vg_trace_closest_device(VgRenderer* r, const float* d_rays, size_t n, uint32
  * it returns. Results are identical to vg_trace_closest's. */
 #define VG_TRACE_NOALLOC_MAX_RAYS 65536u
 int vg_trace_closest_noalloc(VgRenderer* r, const float* rays, size_t n, uint32_t* hits);
+
+/* ---- EXR output (crates/verion-render-io/src/exr_out.rs) -----------------------------------------
+ * Working and target colour spaces, tone map and transfer function (crates/verion-scene/src/color.rs). */
+typedef enum VgColorSpace { VG_COLOR_LINEAR_REC709 = 0, VG_COLOR_ACESCG = 1 } VgColorSpace;
+typedef enum VgToneMap { VG_TONEMAP_NONE = 0, VG_TONEMAP_REINHARD = 1 } VgToneMap;
+typedef enum VgOetf { VG_OETF_LINEAR = 0, VG_OETF_SRGB = 1 } VgOetf;
+/* color.rs:84-124 OutputTransform: {target, NONE, LINEAR} is OutputTransform::linear(target),
+ * {LINEAR_REC709, REINHARD, SRGB} is OutputTransform::display(). */
+typedef struct VgOutputTransform {
+    int target;
+    int tone_map;
+    int oetf;
+} VgOutputTransform;
+
+/* exr_out.rs:8-79 ExrFrame + ExrAovs + RenderInfo. Pixels row-major from the top-left; 3 floats per
+ * pixel for colour planes, 1 for depth and visibility. Optional planes are null when absent; the
+ * lighting split needs all five parts and the visibility. */
+typedef struct VgExrFrame {
+    uint32_t width, height;
+    int working_space;
+    const float* beauty;
+    const float* normal;
+    const float* albedo;
+    const float* depth;
+    const uint32_t* object_id;
+    const uint32_t* material_id;
+    const uint32_t* sample_count;
+    const float* lighting[5]; /* direct diffuse, indirect diffuse, specular, transmission, emission */
+    const float* visibility;
+    int physical;
+    uint32_t samples;
+    uint64_t stylization_revision;
+    int has_grade;
+    float exposure, saturation, white_balance[3];
+    const char* denoiser; /* null: none */
+    int has_adaptive_threshold;
+    float adaptive_threshold;
+    const char* restir;   /* null, "di" or "di+gi" */
+} VgExrFrame;
+
+/* write_exr (exr_out.rs:103-293): one OpenEXR file with the reference's channel names (R, G, B,
+ * N.X.., Albedo.*, DirectDiffuse.* .. Emission.*, Visibility.V, Z, and the 32-bit integer channels
+ * ObjectId, MaterialId, SampleCount), the target's chromaticities and the `verion/*` metadata.
+ * Uncompressed scanlines. VG_ERR_INVALID for a zero size or an incomplete lighting split;
+ * VG_ERR_RESOURCE when the file cannot be written. */
+int vg_write_exr(const char* path, const VgExrFrame* frame, const VgOutputTransform* transform);
 
 /* ---- Radiance cache (no reference counterpart) -----------------------------------------------
  * A multi-resolution hash-grid encoding of the position (two fp16 features per level) feeding a

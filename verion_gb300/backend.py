@@ -108,6 +108,24 @@ class CacheStats(C.Structure):
                 ("path_seconds", C.c_double), ("infer_seconds", C.c_double), ("train_seconds", C.c_double)]
 
 
+class _UpdatePlan(C.Structure):
+    _fields_ = [("full", C.c_int), ("materials", C.c_int), ("lights", C.c_int), ("emitters", C.c_int),
+                ("instances", C.c_int), ("vertices", C.c_int), ("blases", C.c_void_p), ("blas_count", C.c_size_t),
+                ("tlas", C.c_int), ("camera", C.c_int)]
+
+
+class _UpdateReport(C.Structure):
+    _fields_ = [("blases_built", C.c_uint64), ("tlas_built", C.c_int), ("bytes_uploaded", C.c_uint64)]
+
+
+@dataclass
+class UpdateReport:
+    """lib.rs:63-71"""
+    blases_built: int = 0
+    tlas_built: bool = False
+    bytes_uploaded: int = 0
+
+
 CACHE_RECORD_FLOATS = 20  # include/vgcuda.h VG_CACHE_RECORD_FLOATS
 CACHE_MLP_PARAMS = 17408  # VG_CACHE_MLP_PARAMS
 
@@ -131,6 +149,7 @@ def lib() -> C.CDLL:
             "vg_renderer_create": (i32, [vp, C.POINTER(_Packed), C.POINTER(vp)]),
             "vg_renderer_destroy": (None, [vp]),
             "vg_renderer_bvh_info": (i32, [vp, C.POINTER(BvhInfo)]),
+            "vg_renderer_update": (i32, [vp, C.POINTER(_Packed), C.POINTER(_UpdatePlan), C.POINTER(_UpdateReport)]),
             "vg_set_camera": (i32, [vp, C.POINTER(_View)]),
             "vg_set_multiscatter": (i32, [vp, i32]),
             "vg_set_integrator": (i32, [vp, i32]),
@@ -381,6 +400,31 @@ class Renderer:
     def __init__(self, ctx: Context, scene_or_packed):
         packed = scene_or_packed if isinstance(scene_or_packed, Packed) else pack(scene_or_packed)
         self.packed = packed
+        pk = self._struct(packed)
+        h = C.c_void_p()
+        _check(lib().vg_renderer_create(ctx._h, C.byref(pk), C.byref(h)))
+        self._h = h
+        self._ctx = ctx
+        self._keep = []
+        self._adaptive: Optional[Adaptive] = None
+        self._restir: Optional[Restir] = None
+
+    def update(self, scene_or_packed, plan) -> "UpdateReport":
+        """RayTracingBackend::update (lib.rs:23-27): applies `plan` (pack.UpdatePlan) from the
+        edited scene's tables; returns what was rebuilt."""
+        packed = scene_or_packed if isinstance(scene_or_packed, Packed) else pack(scene_or_packed)
+        pk = self._struct(packed)
+        blases = np.ascontiguousarray(plan.blases, np.uint32)
+        up = _UpdatePlan(int(plan.full), int(plan.materials), int(plan.lights), int(plan.emitters),
+                         int(plan.instances), int(plan.vertices), _ptr(blases) if blases.size else None,
+                         blases.size, int(plan.tlas), int(plan.camera))
+        rep = _UpdateReport()
+        _check(lib().vg_renderer_update(self._h, C.byref(pk), C.byref(up), C.byref(rep)))
+        self._keep = []
+        self.packed = packed
+        return UpdateReport(rep.blases_built, bool(rep.tlas_built), rep.bytes_uploaded)
+
+    def _struct(self, packed: Packed) -> "_Packed":
         self._keep = []
         pk = _Packed()
 
@@ -416,13 +460,7 @@ class Renderer:
         pk.info.sky[:] = list(i.sky)
         pk.info.virtual_light, pk.info.transparent_background = int(i.virtual_light), int(i.transparent_background)
         pk.view = _view(packed.view)
-        h = C.c_void_p()
-        _check(lib().vg_renderer_create(ctx._h, C.byref(pk), C.byref(h)))
-        self._h = h
-        self._ctx = ctx
-        self._keep = []
-        self._adaptive: Optional[Adaptive] = None
-        self._restir: Optional[Restir] = None
+        return pk
 
     # RayTracingBackend setters
     def set_camera(self, view_or_camera) -> None:

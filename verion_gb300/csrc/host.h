@@ -154,6 +154,7 @@ struct VgRenderer {
     bool defer_shadows = true; // streaming: shadow rays of the light sample in their own stage
     bool dynamic_fetch = true; // streaming: traversal stages refill idle lanes from the queue
     float bounds_lo[3] = {0, 0, 0}, bounds_hi[3] = {0, 0, 0}; // world box of the triangles
+    uint64_t texel_key = 0, env_key = 0; // hashes of the uploaded texture and environment tables
     VgCache* cache = nullptr;  // radiance cache integrator when set
     float cache_spread = 0.01f;
     uint32_t cache_train_paths = 16384;

@@ -26,7 +26,119 @@
 
 #include "host.h"
 
+// Sets the thread's error text for translation units compiled without the CUDA headers.
+int vg_internal_fail(int status, const char* msg) { return fail(status, msg); }
+
+namespace {
+
+// World-space triangles for the BVH: each instance's mesh through its transform, with the
+// arithmetic of transformPoint (pt_core.slang:90-99) so the kernels' vertices match. Builds the
+// BVH8 over them and records its statistics and the scene box on the renderer.
+int build_world_bvh(VgRenderer* r, const VgPacked* pk, Bvh8Host& bvh)
+{
+    std::vector<float> verts;
+    std::vector<uint32_t> tinst, tprim;
+    size_t total = 0;
+    for (size_t i = 0; i < pk->instance_count; i++)
+        total += pk->meshes[pk->tlas_mesh[i]].index_count / 3;
+    if (total > 0xffffffffu / 2)
+        return fail(VG_ERR_SCENE, "too many triangles");
+    verts.reserve(total * 9);
+    tinst.reserve(total);
+    tprim.reserve(total);
+    for (size_t i = 0; i < pk->instance_count; i++) {
+        const uint32_t* rec = &pk->instances[i * INSTANCE_WORDS];
+        const VgMeshRange& mr = pk->meshes[pk->tlas_mesh[i]];
+        float m[12];
+        for (int k = 0; k < 12; k++)
+            m[k] = u2f(rec[4 + k]);
+        for (uint32_t t = 0; t < mr.index_count / 3; t++) {
+            for (int v = 0; v < 3; v++) {
+                uint32_t vi = pk->indices[mr.index_offset + 3 * t + v] + rec[0];
+                float x = pk->positions[3 * vi], y = pk->positions[3 * vi + 1], z = pk->positions[3 * vi + 2];
+                for (int row = 0; row < 3; row++)
+                    verts.push_back(m[4 * row] * x + m[4 * row + 1] * y + m[4 * row + 2] * z + m[4 * row + 3]);
+            }
+            tinst.push_back((uint32_t)i);
+            tprim.push_back(t);
+        }
+    }
+    float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+    for (size_t i = 0; i < verts.size(); i++) {
+        lo[i % 3] = std::min(lo[i % 3], verts[i]);
+        hi[i % 3] = std::max(hi[i % 3], verts[i]);
+    }
+    std::string err;
+    if (!build_bvh8(verts.data(), tinst.data(), tprim.data(), (uint32_t)total, bvh, err))
+        return fail(VG_ERR_SCENE, err);
+    for (int k = 0; k < 3; k++) {
+        r->bounds_lo[k] = lo[k];
+        r->bounds_hi[k] = hi[k];
+    }
+    r->bvh.triangles = bvh.triangles;
+    r->bvh.wide_nodes = bvh.wide_nodes;
+    r->bvh.wide_depth = bvh.wide_depth;
+    r->bvh.binary_nodes = bvh.binary_nodes;
+    r->bvh.binary_depth = bvh.binary_depth;
+    r->bvh.node_bytes = bvh.nodes.size() * 4;
+    r->bvh.triangle_bytes = bvh.tris.size() * 4;
+    r->bvh.build_seconds = bvh.build_seconds;
+    return VG_OK;
+}
+
+// Any translucent material (opacity below 1 or transmission): shadow rays then look past hits.
+bool translucent_materials(const VgPacked* pk)
+{
+    for (size_t m = 0; m < pk->materials_len / MATERIAL_WORDS; m++)
+        if (pk->materials[m * MATERIAL_WORDS + 22] < 1.0f || pk->materials[m * MATERIAL_WORDS + 23] > 0.0f)
+            return true;
+    return false;
+}
+
+// FNV-1a over two tables: whether a re-packed table differs from the uploaded one.
+uint64_t table_key(const void* a, size_t a_len, const void* b, size_t b_len)
+{
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](const void* p, size_t words) {
+        const uint32_t* w = (const uint32_t*)p;
+        for (size_t i = 0; i < words; i++) {
+            h ^= w[i];
+            h *= 1099511628211ull;
+        }
+        h ^= words;
+        h *= 1099511628211ull;
+    };
+    if (a)
+        mix(a, a_len);
+    if (b)
+        mix(b, b_len);
+    return h;
+}
+
+void bind_tables(VgRenderer* r)
+{
+    r->ds.positions = (const float*)r->positions.p;
+    r->ds.indices = (const uint32_t*)r->indices.p;
+    r->ds.instances = (const uint32_t*)r->instances.p;
+    r->ds.materials = (const float*)r->materials.p;
+    r->ds.lights = (const uint32_t*)r->lights.p;
+    r->ds.emitters = (const float*)r->emitters.p;
+    r->ds.emit_cdf = (const float*)r->emit_cdf.p;
+    r->ds.env_pixels = (const float*)r->env_pixels.p;
+    r->ds.env_marginal = (const float*)r->env_marginal.p;
+    r->ds.env_cond = (const float*)r->env_cond.p;
+    r->ds.uvs = (const float*)r->uvs.p;
+    r->ds.texels = (const float*)r->texels.p;
+    r->ds.tex_info = (const uint32_t*)r->tex_info.p;
+    r->ds.vnormals = (const float*)r->vnormals.p;
+    r->ds.nodes = (const uint4*)r->nodes.p;
+    r->ds.tris = (const float4*)r->tris.p;
+}
+
+} // namespace
+
 extern "C" {
+
 
 size_t vg_last_error(char* buf, size_t len)
 {
@@ -107,64 +219,12 @@ int vg_renderer_create(VgContext* ctx, const VgPacked* pk, VgRenderer** out)
     r->info = pk->info;
     r->view = pk->view;
     r->instance_count = (uint32_t)pk->instance_count;
-    // World-space triangles for the BVH: each instance's mesh through its transform, with the
-    // arithmetic of transformPoint (pt_core.slang:90-99) so the kernels' vertices match.
-    std::vector<float> verts;
-    std::vector<uint32_t> tinst, tprim;
-    size_t total = 0;
-    for (size_t i = 0; i < pk->instance_count; i++)
-        total += pk->meshes[pk->tlas_mesh[i]].index_count / 3;
-    if (total > 0xffffffffu / 2) {
-        delete r;
-        return fail(VG_ERR_SCENE, "too many triangles");
-    }
-    verts.reserve(total * 9);
-    tinst.reserve(total);
-    tprim.reserve(total);
-    for (size_t i = 0; i < pk->instance_count; i++) {
-        const uint32_t* rec = &pk->instances[i * INSTANCE_WORDS];
-        const VgMeshRange& mr = pk->meshes[pk->tlas_mesh[i]];
-        float m[12];
-        for (int k = 0; k < 12; k++)
-            m[k] = u2f(rec[4 + k]);
-        for (uint32_t t = 0; t < mr.index_count / 3; t++) {
-            for (int v = 0; v < 3; v++) {
-                uint32_t vi = pk->indices[mr.index_offset + 3 * t + v] + rec[0];
-                float x = pk->positions[3 * vi], y = pk->positions[3 * vi + 1], z = pk->positions[3 * vi + 2];
-                for (int row = 0; row < 3; row++)
-                    verts.push_back(m[4 * row] * x + m[4 * row + 1] * y + m[4 * row + 2] * z + m[4 * row + 3]);
-            }
-            tinst.push_back((uint32_t)i);
-            tprim.push_back(t);
-        }
-    }
-    for (int k = 0; k < 3; k++) {
-        r->bounds_lo[k] = 3.0e38f;
-        r->bounds_hi[k] = -3.0e38f;
-    }
-    for (size_t i = 0; i < verts.size(); i++) {
-        r->bounds_lo[i % 3] = std::min(r->bounds_lo[i % 3], verts[i]);
-        r->bounds_hi[i % 3] = std::max(r->bounds_hi[i % 3], verts[i]);
-    }
     Bvh8Host bvh;
-    std::string err;
-    if (!build_bvh8(verts.data(), tinst.data(), tprim.data(), (uint32_t)total, bvh, err)) {
+    if ((st = build_world_bvh(r, pk, bvh)) != VG_OK) {
         delete r;
-        return fail(VG_ERR_SCENE, err);
+        return st;
     }
-    r->bvh.triangles = bvh.triangles;
-    r->bvh.wide_nodes = bvh.wide_nodes;
-    r->bvh.wide_depth = bvh.wide_depth;
-    r->bvh.binary_nodes = bvh.binary_nodes;
-    r->bvh.binary_depth = bvh.binary_depth;
-    r->bvh.node_bytes = bvh.nodes.size() * 4;
-    r->bvh.triangle_bytes = bvh.tris.size() * 4;
-    r->bvh.build_seconds = bvh.build_seconds;
-
-    bool translucent = false;
-    for (size_t m = 0; m < pk->materials_len / MATERIAL_WORDS; m++)
-        if (pk->materials[m * MATERIAL_WORDS + 22] < 1.0f || pk->materials[m * MATERIAL_WORDS + 23] > 0.0f)
-            translucent = true;
+    bool translucent = translucent_materials(pk);
 
 #define UP(buf, src, n)                                                                                             \
     do {                                                                                                            \
@@ -201,22 +261,9 @@ int vg_renderer_create(VgContext* ctx, const VgPacked* pk, VgRenderer** out)
         vg_renderer_destroy(r);
         return cuda_fail(e, "upload");
     }
-    r->ds.positions = (const float*)r->positions.p;
-    r->ds.indices = (const uint32_t*)r->indices.p;
-    r->ds.instances = (const uint32_t*)r->instances.p;
-    r->ds.materials = (const float*)r->materials.p;
-    r->ds.lights = (const uint32_t*)r->lights.p;
-    r->ds.emitters = (const float*)r->emitters.p;
-    r->ds.emit_cdf = (const float*)r->emit_cdf.p;
-    r->ds.env_pixels = (const float*)r->env_pixels.p;
-    r->ds.env_marginal = (const float*)r->env_marginal.p;
-    r->ds.env_cond = (const float*)r->env_cond.p;
-    r->ds.uvs = (const float*)r->uvs.p;
-    r->ds.texels = (const float*)r->texels.p;
-    r->ds.tex_info = (const uint32_t*)r->tex_info.p;
-    r->ds.vnormals = (const float*)r->vnormals.p;
-    r->ds.nodes = (const uint4*)r->nodes.p;
-    r->ds.tris = (const float4*)r->tris.p;
+    r->texel_key = table_key(pk->texels, pk->texels_len, pk->tex_info, pk->tex_info_len);
+    r->env_key = table_key(pk->env_pixels, pk->env_pixels_len, pk->env_conditional, pk->env_conditional_len);
+    bind_tables(r);
     r->ds.shadow_any = translucent ? 0u : 1u;
     r->extend_blocks = vgx::wf_extend_blocks_per_sm();
     *out = r;
@@ -227,6 +274,144 @@ void vg_renderer_destroy(VgRenderer* r)
 {
     // As vg_accum_destroy: frees device memory only, independent of the context's lifetime.
     delete r;
+}
+
+int vg_renderer_update(VgRenderer* r, const VgPacked* pk, const VgUpdatePlan* plan, VgUpdateReport* out)
+{
+    if (!r || !pk || !plan || !out)
+        return fail(VG_ERR_INVALID, "null argument");
+    memset(out, 0, sizeof(*out));
+    int st = validate(pk);
+    if (st != VG_OK)
+        return st;
+    VgContext* ctx = r->ctx;
+    if (plan->camera)
+        r->view = pk->view;
+    if (plan->full) {
+        VgRenderer* f = nullptr;
+        if ((st = vg_renderer_create(ctx, pk, &f)) != VG_OK)
+            return st;
+        DevBuf* mine[] = {&r->positions, &r->indices, &r->uvs, &r->vnormals, &r->instances, &r->materials,
+                          &r->lights, &r->emitters, &r->emit_cdf, &r->env_pixels, &r->env_marginal, &r->env_cond,
+                          &r->texels, &r->tex_info, &r->nodes, &r->tris};
+        DevBuf* theirs[] = {&f->positions, &f->indices, &f->uvs, &f->vnormals, &f->instances, &f->materials,
+                            &f->lights, &f->emitters, &f->emit_cdf, &f->env_pixels, &f->env_marginal, &f->env_cond,
+                            &f->texels, &f->tex_info, &f->nodes, &f->tris};
+        uint64_t bytes = 0;
+        for (size_t i = 0; i < sizeof(mine) / sizeof(mine[0]); i++) {
+            std::swap(mine[i]->p, theirs[i]->p);
+            std::swap(mine[i]->bytes, theirs[i]->bytes);
+            bytes += mine[i]->bytes;
+        }
+        r->info = f->info;
+        r->bvh = f->bvh;
+        r->instance_count = f->instance_count;
+        r->texel_key = f->texel_key;
+        r->env_key = f->env_key;
+        for (int k = 0; k < 3; k++) {
+            r->bounds_lo[k] = f->bounds_lo[k];
+            r->bounds_hi[k] = f->bounds_hi[k];
+        }
+        uint32_t shadow_any = f->ds.shadow_any;
+        bind_tables(r);
+        r->ds.shadow_any = shadow_any;
+        vg_renderer_destroy(f); // frees the old tables
+        out->blases_built = pk->mesh_count;
+        out->tlas_built = 1;
+        out->bytes_uploaded = bytes;
+        return VG_OK;
+    }
+    cudaStream_t s = ctx->stream;
+    uint64_t bytes = 0;
+    if (plan->vertices) {
+        if (std::max<size_t>(pk->positions_len * 4, 16) != r->positions.bytes ||
+            std::max<size_t>(pk->uvs_len * 4, 16) != r->uvs.bytes ||
+            std::max<size_t>(pk->vnormals_len * 4, 16) != r->vnormals.bytes || (plan->blas_count > 0 && !plan->blases))
+            return fail(VG_ERR_SCENE, "a deformed mesh changed its vertex count: that needs a full update");
+        for (size_t i = 0; i < plan->blas_count; i++) {
+            uint32_t m = plan->blases[i];
+            if (m >= pk->mesh_count)
+                return fail(VG_ERR_INVALID, "deformed mesh index out of range");
+            const VgMeshRange& mr = pk->meshes[m];
+            size_t vo = mr.vertex_offset, vc = mr.vertex_count;
+            if ((vo + vc) * 3 > pk->positions_len || (vo + vc) * 2 > pk->uvs_len || (vo + vc) * 3 > pk->vnormals_len)
+                return fail(VG_ERR_INVALID, "mesh range outside the vertex tables");
+            VG_CHECK(cudaMemcpyAsync((float*)r->positions.p + vo * 3, pk->positions + vo * 3, vc * 12,
+                                     cudaMemcpyHostToDevice, s),
+                     "vertex upload");
+            VG_CHECK(cudaMemcpyAsync((float*)r->uvs.p + vo * 2, pk->uvs + vo * 2, vc * 8, cudaMemcpyHostToDevice, s),
+                     "vertex upload");
+            VG_CHECK(cudaMemcpyAsync((float*)r->vnormals.p + vo * 3, pk->vnormals + vo * 3, vc * 12,
+                                     cudaMemcpyHostToDevice, s),
+                     "vertex upload");
+            bytes += vc * 32;
+        }
+        out->blases_built = plan->blas_count;
+    }
+    if (plan->materials) {
+        if ((st = upload(ctx, r->materials, pk->materials, pk->materials_len * 4)) != VG_OK)
+            return st;
+        bytes += pk->materials_len * 4;
+        uint64_t key = table_key(pk->texels, pk->texels_len, pk->tex_info, pk->tex_info_len);
+        if (key != r->texel_key) {
+            if ((st = upload(ctx, r->texels, pk->texels, pk->texels_len * 4)) != VG_OK ||
+                (st = upload(ctx, r->tex_info, pk->tex_info, pk->tex_info_len * 4)) != VG_OK)
+                return st;
+            bytes += (pk->texels_len + pk->tex_info_len) * 4;
+            r->texel_key = key;
+        }
+        r->ds.shadow_any = translucent_materials(pk) ? 0u : 1u;
+    }
+    if (plan->lights) {
+        if ((st = upload(ctx, r->lights, pk->lights, pk->lights_len * 4)) != VG_OK)
+            return st;
+        bytes += pk->lights_len * 4;
+        r->info.light_count = pk->info.light_count;
+        for (int k = 0; k < 3; k++)
+            r->info.sky[k] = pk->info.sky[k];
+        r->info.virtual_light = pk->info.virtual_light;
+        r->info.transparent_background = pk->info.transparent_background;
+        uint64_t key = table_key(pk->env_pixels, pk->env_pixels_len, pk->env_conditional, pk->env_conditional_len);
+        if (key != r->env_key || pk->info.env_width != r->info.env_width || pk->info.env_height != r->info.env_height) {
+            if ((st = upload(ctx, r->env_pixels, pk->env_pixels, pk->env_pixels_len * 4)) != VG_OK ||
+                (st = upload(ctx, r->env_marginal, pk->env_marginal, pk->env_marginal_len * 4)) != VG_OK ||
+                (st = upload(ctx, r->env_cond, pk->env_conditional, pk->env_conditional_len * 4)) != VG_OK)
+                return st;
+            bytes += (pk->env_pixels_len + pk->env_marginal_len + pk->env_conditional_len) * 4;
+            r->info.env_width = pk->info.env_width;
+            r->info.env_height = pk->info.env_height;
+            r->info.env_pdf_scale = pk->info.env_pdf_scale;
+            r->env_key = key;
+        }
+    }
+    if (plan->emitters) {
+        if ((st = upload(ctx, r->emitters, pk->emitters, pk->emitters_len * 4)) != VG_OK ||
+            (st = upload(ctx, r->emit_cdf, pk->emit_cdf, pk->emit_cdf_len * 4)) != VG_OK)
+            return st;
+        bytes += (pk->emitters_len + pk->emit_cdf_len) * 4;
+        r->info.emitter_count = pk->info.emitter_count;
+    }
+    if (plan->instances) {
+        if ((st = upload(ctx, r->instances, pk->instances, pk->instances_len * 4)) != VG_OK)
+            return st;
+        bytes += pk->instances_len * 4;
+        r->instance_count = (uint32_t)pk->instance_count;
+    }
+    if (plan->tlas || plan->vertices) {
+        Bvh8Host bvh;
+        if ((st = build_world_bvh(r, pk, bvh)) != VG_OK ||
+            (st = upload(ctx, r->nodes, bvh.nodes.data(), bvh.nodes.size() * 4)) != VG_OK ||
+            (st = upload(ctx, r->tris, bvh.tris.data(), bvh.tris.size() * 4)) != VG_OK)
+            return st;
+        bytes += (bvh.nodes.size() + bvh.tris.size()) * 4;
+        out->tlas_built = 1;
+    }
+    VG_CHECK(cudaStreamSynchronize(s), "update");
+    uint32_t shadow_any = r->ds.shadow_any;
+    bind_tables(r);
+    r->ds.shadow_any = shadow_any;
+    out->bytes_uploaded = bytes;
+    return VG_OK;
 }
 
 int vg_renderer_bvh_info(const VgRenderer* r, VgBvhInfo* out)

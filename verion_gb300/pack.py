@@ -426,6 +426,47 @@ def pack(s: sc.Scene) -> Packed:
                   info, View.new(s.camera))
 
 
+@dataclass
+class UpdatePlan:
+    """pack.rs:758-784: what a batch of scene edits makes a backend redo."""
+    full: bool = False
+    materials: bool = False
+    lights: bool = False
+    emitters: bool = False
+    instances: bool = False
+    vertices: bool = False
+    blases: tuple = ()
+    tlas: bool = False
+    camera: bool = False
+
+    @staticmethod
+    def new(camera: bool = False, lights: bool = False, materials=(), instances=(), deformed=(),
+            geometry: bool = False) -> "UpdatePlan":
+        """pack.rs:786-823 (`UpdatePlan::new` over `verion_scene::Changes`): `materials`,
+        `instances` and `deformed` are the edited material, instance and mesh indices."""
+        p = UpdatePlan(camera=camera, lights=lights)
+        if geometry:
+            return UpdatePlan(True, True, True, True, True, True, (), True, camera)
+        if materials:
+            p.materials = True
+            p.emitters = True
+        if instances:
+            p.instances = True
+            p.tlas = True
+            p.emitters = True
+        if deformed:
+            p.vertices = True
+            p.blases = tuple(int(m) for m in deformed)
+            p.tlas = True
+            p.emitters = True
+        # Emitters carry the instance table's emitter bases.
+        p.instances |= p.emitters
+        return p
+
+    def is_empty(self) -> bool:
+        return self == UpdatePlan()
+
+
 def base_params(info: SceneInfo, view: View, size, lighting: bool, multiscatter: bool, adaptive=None,
                 restir=None, max_depth: int = MAX_DEPTH) -> np.ndarray:
     """pack.rs:828-874: the parameter block with the per-dispatch words (6, 30, 31, 35) zero."""
