@@ -180,8 +180,9 @@ int vg_integrator(const VgRenderer* r);
 int vg_set_stage_timing(VgRenderer* r, int on);
 /* RayTracingBackend::set_adaptive (lib.rs:39): on = 0 is None. */
 int vg_set_adaptive(VgRenderer* r, int on, float threshold, uint32_t min_spp);
-/* RayTracingBackend::set_restir (lib.rs:42): on = 0 is None. ReSTIR GI is not built yet:
- * gi != 0 returns VG_ERR_UNSUPPORTED. */
+/* RayTracingBackend::set_restir (lib.rs:42): on = 0 is None. `di` and `gi` select ReSTIR DI
+ * (pt_core.slang:759-882) and ReSTIR GI (:897-981, :1566-1617); GI stays off with the lighting
+ * split, as in the reference. */
 int vg_set_restir(VgRenderer* r, int on, int di, int gi, uint32_t candidates, uint32_t history);
 
 /* Extensions with no reference counterpart. */

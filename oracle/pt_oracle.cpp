@@ -1023,6 +1023,137 @@ struct PT {
         rwu(co + 27, 0u);
     }
 
+    // pt_core.slang:713
+    static uint32_t restirScratch(uint32_t pixel) { return pixel * RESTIR_STRIDE + 2 * RESTIR_HALF; }
+
+    // pt_core.slang:897-981: the previous frame's second-hit samples of this pixel and its
+    // neighbours, reconnected to this shading point (Jacobian of the solid-angle change), RIS over
+    // them; the pick goes to the scratch words for giFinish.
+    void restirGIPrepare(uint32_t pixel, V<R> p, V<R> n, R pHitT, const Surface<R>& surf, V<R> Tt, V<R> B, V<R> woL,
+                         Rng<R>& rng) const
+    {
+        uint32_t w = P[0];
+        uint32_t cur = P[6] & 1u;
+        R cap = R((float)std::max(P[38], 1u));
+        R wsum = 0, mTotal = 0, pSel = 0;
+        V<R> cSel(R(0)), xSel(R(0)), nSel(R(0)), lSel(R(0));
+        if (P[6] > 0) {
+            int px = (int)(pixel % w);
+            int py = (int)(pixel / w);
+            for (uint32_t k = 0; k < 1 + RESTIR_NEIGHBOURS; k++) {
+                int nx = px, ny = py;
+                if (k > 0) {
+                    nx += (int)(rng.next() * R(2 * RESTIR_RADIUS + 1)) - RESTIR_RADIUS;
+                    ny += (int)(rng.next() * R(2 * RESTIR_RADIUS + 1)) - RESTIR_RADIUS;
+                    if (nx < 0 || ny < 0 || nx >= (int)w || ny >= (int)P[1])
+                        continue;
+                }
+                uint32_t ro = restirBase((uint32_t)ny * w + (uint32_t)nx, cur ^ 1u);
+                if (ru(ro + 14) == 0 || ru(ro + 27) == 0)
+                    continue;
+                V<R> pq(rr(ro + 8), rr(ro + 9), rr(ro + 10));
+                V<R> nq(rr(ro + 11), rr(ro + 12), rr(ro + 13));
+                if (dot(nq, n) < R(0.9f) || length(pq - p) > R(0.05f) * mmax(pHitT, R(0.01f)))
+                    continue;
+                V<R> x2(rr(ro + 16), rr(ro + 17), rr(ro + 18));
+                V<R> n2(rr(ro + 19), rr(ro + 20), rr(ro + 21));
+                V<R> l2(rr(ro + 22), rr(ro + 23), rr(ro + 24));
+                R mq = mmin(rr(ro + 26), cap);
+                mTotal += mq;
+                V<R> toX = x2 - p;
+                R dR = length(toX);
+                V<R> wi = toX / mmax(dR, R(1.0e-6f));
+                R dQ = length(x2 - pq);
+                R cosT = dot(n, wi);
+                R cosR = std::fabs(dot(n2, wi));
+                R cosQ = std::fabs(dot(n2, normalize(pq - x2)));
+                if (cosT <= R(0) || dR < R(1.0e-3f) || cosR < R(1.0e-3f) || cosQ < R(1.0e-3f))
+                    continue;
+                R jac = (cosR / cosQ) * (dQ * dQ) / (dR * dR);
+                if (jac > R(10) || jac < R(1) / R(10))
+                    continue;
+                V<R> c = evalReflective(surf, woL, V<R>(dot(wi, Tt), dot(wi, B), cosT)) * l2;
+                R phat = lum(c);
+                if (phat <= R(0) || occluded(p, wi, dR * (R(1) - R(1.0e-3f))))
+                    continue;
+                R wgt = phat * rr(ro + 25) * mq * jac;
+                wsum += wgt;
+                if (rng.next() * wsum < wgt) {
+                    pSel = phat;
+                    cSel = c;
+                    xSel = x2;
+                    nSel = n2;
+                    lSel = l2;
+                }
+            }
+        }
+        uint32_t so = restirScratch(pixel);
+        rw(so, wsum);
+        rw(so + 1, mTotal);
+        rw(so + 2, pSel);
+        V<R> vs[4] = {cSel, xSel, nSel, lSel};
+        for (int q = 0; q < 4; q++) {
+            rw(so + 3 + 3 * q, vs[q].x);
+            rw(so + 4 + 3 * q, vs[q].y);
+            rw(so + 5 + 3 * q, vs[q].z);
+        }
+        rwu(so + 22, 0u);
+    }
+
+    // pt_core.slang:1566-1617: the path's own candidate joins the resampled ones; the pixel gets
+    // its direct light plus the indirect light of the pick; the new reservoir goes to this frame's
+    // half.
+    V<R> giFinish(V<R> pathTotal, uint32_t pixel) const
+    {
+        uint32_t co = restirBase(pixel, P[6] & 1u);
+        uint32_t so = restirScratch(pixel);
+        R wsum = rr(so);
+        R m = rr(so + 1) + R(1);
+        R pSel = rr(so + 2);
+        V<R> cSel(rr(so + 3), rr(so + 4), rr(so + 5));
+        V<R> xSel(rr(so + 6), rr(so + 7), rr(so + 8));
+        V<R> nSel(rr(so + 9), rr(so + 10), rr(so + 11));
+        V<R> lSel(rr(so + 12), rr(so + 13), rr(so + 14));
+        V<R> thr1(rr(so + 15), rr(so + 16), rr(so + 17));
+        V<R> d0(rr(so + 18), rr(so + 19), rr(so + 20));
+        R qPrev = rr(so + 21);
+        bool own = ru(so + 22) != 0 && qPrev > R(0);
+        V<R> giTotal = pathTotal - d0;
+        V<R> result = d0;
+        if (own) {
+            V<R> cOwn = giTotal * qPrev;
+            R pOwn = lum(cOwn);
+            if (pOwn > R(0)) {
+                R wOwn = pOwn / qPrev;
+                wsum += wOwn;
+                Rng<R> r;
+                r.state = pcg(pixel ^ pcg(P[6] * 0x85EBCA6Bu + 0x1234u));
+                if (r.next() * wsum < wOwn) {
+                    pSel = pOwn;
+                    cSel = cOwn;
+                    xSel = V<R>(rr(co + 16), rr(co + 17), rr(co + 18));
+                    nSel = V<R>(rr(co + 19), rr(co + 20), rr(co + 21));
+                    lSel = V<R>(thr1.x > R(1.0e-6f) ? giTotal.x / thr1.x : R(0),
+                                thr1.y > R(1.0e-6f) ? giTotal.y / thr1.y : R(0),
+                                thr1.z > R(1.0e-6f) ? giTotal.z / thr1.z : R(0));
+                }
+            }
+        } else
+            result = result + giTotal;
+        R W = pSel > R(0) ? wsum / (m * pSel) : R(0);
+        result = result + cSel * W;
+        V<R> vs[3] = {xSel, nSel, lSel};
+        for (int q = 0; q < 3; q++) {
+            rw(co + 16 + 3 * q, vs[q].x);
+            rw(co + 17 + 3 * q, vs[q].y);
+            rw(co + 18 + 3 * q, vs[q].z);
+        }
+        rw(co + 25, W);
+        rw(co + 26, m);
+        rwu(co + 27, pSel > R(0) ? 1u : 0u);
+        return result;
+    }
+
     // pt_core.slang:992-1543
     bool shadePath(PathState<R>& st, HitRec<R> hq, uint32_t depth, uint32_t pixel) const
     {
@@ -1084,6 +1215,13 @@ struct PT {
                 break;
             }
             V<R> p = hit + ng * R(1.0e-4f);
+            if (depth == 1 && st.gi) {
+                // pt_core.slang:1072-1082: the first bounce's surface is ReSTIR GI's candidate.
+                uint32_t co = restirBase(pixel, P[6] & 1u);
+                rw(co + 16, hit.x), rw(co + 17, hit.y), rw(co + 18, hit.z);
+                rw(co + 19, ng.x), rw(co + 20, ng.y), rw(co + 21, ng.z);
+                rwu(restirScratch(pixel) + 22, 1u);
+            }
             V<R> nsObj = (R(1) - b1 - b2) * vertexNormal(i0) + b1 * vertexNormal(i1) + b2 * vertexNormal(i2);
             V<R> ns = nOut;
             if (dot(nsObj, nsObj) > R(1.0e-12f)) {
@@ -1148,6 +1286,14 @@ struct PT {
                     wB = st.qPrev * st.qPrev / (st.qPrev * st.qPrev + pl * pl);
                 }
                 st.parts.add(depth, cls, thr * le * wB);
+                if (depth == 1 && st.gi) {
+                    // pt_core.slang:1161-1168: counted with what the first hit gathered itself.
+                    uint32_t so = restirScratch(pixel) + 18;
+                    V<R> e = thr * le * wB;
+                    rw(so, rr(so) + e.x);
+                    rw(so + 1, rr(so + 1) + e.y);
+                    rw(so + 2, rr(so + 2) + e.z);
+                }
             }
             R metallic = fm(mi + 6) * texRy, rough = fm(mi + 7) * texRx, transmission = fm(mi + 8), ior = fm(mi + 9);
             R dispersion = fm(mi + 21);
@@ -1158,6 +1304,9 @@ struct PT {
                 }
                 ior = mmax(ior + R(chan - 1) * (ior - R(1)) * R(0.025f) * dispersion, R(1));
             }
+            // pt_core.slang:1187-1190: a glass second hit cannot be reconnected to.
+            if (depth == 1 && st.gi && transmission > R(0))
+                rwu(restirScratch(pixel) + 22, 0u);
             R alpha = mmax(rough * rough, R(1.0e-3f));
             R eta = outside ? ior : R(1) / ior;
             V<R> Tt, B;
@@ -1242,11 +1391,14 @@ struct PT {
                 bool suits = pf(3) == R(0) && transmission == R(0) && surf.alpha >= R(0.15f) &&
                              (surf.coat == R(0) || surf.coatAlpha >= R(0.15f));
                 reDI = suits && (P[36] & 1u) != 0 && emitterCount > 0;
+                bool reGI = suits && (P[36] & 2u) != 0 && !lightingOn;
                 st.restir = reDI;
-                st.gi = false;
-                if (suits)
+                st.gi = reGI;
+                if (suits) {
                     restirGbuffer(pixel, p, n);
-                else
+                    if (reGI)
+                        restirGIPrepare(pixel, p, n, pHitT, surf, Tt, B, woL, rng);
+                } else
                     restirClear(pixel);
             }
             if (reDI) {
@@ -1436,6 +1588,13 @@ struct PT {
         st.thr = thr;
         st.cls = cls;
         st.chan = chan;
+        if (depth == 0 && st.gi) {
+            // pt_core.slang:1531-1541: what the first hit gathered and what the first bounce carries.
+            uint32_t so = restirScratch(pixel);
+            rw(so + 15, thr.x), rw(so + 16, thr.y), rw(so + 17, thr.z);
+            rw(so + 18, st.parts.total.x), rw(so + 19, st.parts.total.y), rw(so + 20, st.parts.total.z);
+            rw(so + 21, st.qPrev);
+        }
         return alive;
     }
 
@@ -1460,6 +1619,12 @@ struct PT {
         Parts<R> parts = st.parts;
         R visLit = st.visLit, visTotal = st.visTotal;
         V<R> radiance = parts.total;
+        if (st.gi) {
+            // pt_core.slang:1627-1633: a dispersive path follows one channel and is not shared.
+            if (st.chan >= 0)
+                rwu(restirScratch(pixel) + 22, 0u);
+            radiance = giFinish(radiance, pixel);
+        }
         if (badV(radiance)) {
             radiance = V<R>();
             parts = Parts<R>();

@@ -202,3 +202,46 @@ def feature_zoo(transparent_background: bool = False) -> sc.Scene:
     s.camera = scenes.look_at((0.0, 0.8, 3.2), (0.0, -0.1, 0.0), fov=0.8)
     s.transparent_background = transparent_background
     return s
+
+
+def quads(cells) -> sc.Mesh:
+    """crates/verion-gpu-vulkan/tests/restir.rs:8-22: squares in z planes, (centre, half size)."""
+    p, i = [], []
+    for (x, y, z), h in cells:
+        b = len(p)
+        p += [[x - h, y - h, z], [x + h, y - h, z], [x + h, y + h, z], [x - h, y + h, z]]
+        i += [b, b + 1, b + 2, b, b + 2, b + 3]
+    return sc.Mesh(np.array(p, np.float32), np.array(i, np.uint32))
+
+
+def room_with(roughness: float, glass: bool) -> sc.Scene:
+    """restir.rs:152-231: a closed room of rough walls lit by 16 small ceiling panels and a rough
+    ball, seen from inside (mostly indirect light); with `glass`, a strongly dispersive glass block."""
+    s = sc.Scene()
+    room = s.add_mesh(scenes.cube(1.5))
+    ball = s.add_mesh(scenes.cube(0.4))
+    pos, idx = [], []
+    for k in range(16):
+        gx, gz = float(k % 4), float(k // 4)
+        q = quads([([-0.6 + gx * 0.4, -0.6 + gz * 0.4, 0.0], 0.06)])
+        b = len(pos)
+        pos += [[v[0], 1.45, v[1]] for v in q.positions]
+        idx += [int(j) + b for j in q.indices]
+    lamps = s.add_mesh(sc.Mesh(np.array(pos, np.float32), np.array(idx, np.uint32)))
+    walls = s.add_material(sc.BaseBsdf(base_color=(0.7, 0.65, 0.6), roughness=roughness, ior=1.0))
+    glow = s.add_material(sc.BaseBsdf(base_color=(0.0, 0.0, 0.0), emission=(30.0, 30.0, 30.0), roughness=roughness))
+    parts = [(room, walls, sc.IDENTITY), (ball, walls, sc.IDENTITY), (lamps, glow, sc.IDENTITY)]
+    if glass:
+        block = s.add_mesh(scenes.cube(0.35))
+        dispersive = s.add_material(sc.BaseBsdf(base_color=(1.0, 1.0, 1.0), transmission=1.0, roughness=0.0, ior=1.6,
+                                                dispersion=8.0))
+        parts.append((block, dispersive, ((1, 0, 0, -0.7), (0, 1, 0, -0.9), (0, 0, 1, 0.0))))
+    for mesh, material, t in parts:
+        s.add_instance(sc.Instance(mesh, material, t))
+    s.camera = sc.Camera(transform=((1, 0, 0, 0), (0, 1, 0, 0), (0, 0, 1, 1.4)))
+    return s
+
+
+def closed_room(roughness: float) -> sc.Scene:
+    """restir.rs:152-157"""
+    return room_with(roughness, False)

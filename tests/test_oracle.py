@@ -165,6 +165,25 @@ def test_restir_converges_to_the_plain_image(oracle_lib):
     assert abs(re.mean() - plain.mean()) / plain.mean() < 0.03
 
 
+def test_restir_gi_leaves_sharp_surfaces_alone(oracle_lib):
+    # crates/verion-gpu-vulkan/tests/restir.rs:263-271: walls of roughness 0.05 are too sharp for
+    # reuse, so the image is the plain one bit for bit.
+    from .analytic import closed_room
+
+    plain = render(closed_room(0.05), 24, 24, 4)
+    gi = render(closed_room(0.05), 24, 24, 4, restir=Restir(di=False, gi=True))
+    assert np.array_equal(plain.sums, gi.sums)
+
+
+def test_restir_gi_converges_to_the_plain_image(oracle_lib):
+    # restir.rs:240-250 (3% at 64x64 and 1024 spp on the GPU); a smaller run here.
+    from .analytic import closed_room
+
+    plain = image(render(closed_room(0.9), 24, 24, 96))
+    gi = image(render(closed_room(0.9), 24, 24, 96, restir=Restir(di=False, gi=True)))
+    assert abs(gi.mean() - plain.mean()) / plain.mean() < 0.06
+
+
 def test_double_precision_agrees_with_single(oracle_lib):
     f = image(render(scenes.cornell(), 24, 24, 16))
     d = image(render(scenes.cornell(), 24, 24, 16, double=True, acc64=True))

@@ -39,6 +39,12 @@ struct Reservoirs {
     float4* n[2]; // shading normal xyz, emitter + 1 (bits, 0 = none)          (words 11..13, 0)
     float4* x[2]; // sample point xyz, contribution weight W                    (words 1..3, 4)
     float* m[2];  // sample count M                                             (word 5)
+    // ReSTIR GI (pt_core.slang:897-981, 1566-1617), per frame parity:
+    float4* gx[2]; // second-hit sample point xyz, contribution weight W        (words 16..18, 25)
+    float4* gn[2]; // second-hit facing normal xyz, sample count M              (words 19..21, 26)
+    float4* gl[2]; // radiance the sample point sent, usable (bits, 1 or 0)      (words 22..24, 27)
+    // ...and the scratch of the current sample (words 56..78 of the reference's layout):
+    float4* s[7]; // (wsum, M, p-hat, own bits), (c, qPrev), x, n, l, throughput of the first bounce, direct light
 };
 
 // Everything a launch reads: the tables, the parameter block and the accumulation buffers.

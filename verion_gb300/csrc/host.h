@@ -178,6 +178,7 @@ struct VgAccum {
     bool adaptive = false;
     Restir restir;               // captured at the first sample
     DevBuf re_g[2], re_n[2], re_x[2], re_m[2];
+    DevBuf re_gx[2], re_gn[2], re_gl[2], re_s[7]; // ReSTIR GI planes
     DevBuf state, hits, queue[2], counts, fetch, tstats, meta, sreq;
     uint32_t* host_counts = nullptr; // pinned ring of wave output counts (streaming wavefront)
     uint32_t last_waves = 0;
@@ -399,7 +400,12 @@ vgd::Ctx make_ctx(VgRenderer* r, VgAccum* acc)
             c.re.n[h] = (float4*)acc->re_n[h].p;
             c.re.x[h] = (float4*)acc->re_x[h].p;
             c.re.m[h] = (float*)acc->re_m[h].p;
+            c.re.gx[h] = (float4*)acc->re_gx[h].p;
+            c.re.gn[h] = (float4*)acc->re_gn[h].p;
+            c.re.gl[h] = (float4*)acc->re_gl[h].p;
         }
+        for (int k = 0; k < 7; k++)
+            c.re.s[k] = (float4*)acc->re_s[k].p;
     }
     c.err = (uint32_t*)r->err.p;
     return c;

@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(128) mk_pathtrace(const __grid_constant__ Ctx 
             if (!shadePath<LIGHT, RESTIR>(c, st, traceClosest(c, st.org, st.dir), depth, pixel))
                 break;
         }
-        finishPath<LIGHT, A>(c, st, pixel);
+        finishPath<LIGHT, A, RESTIR>(c, st, pixel);
     }
 }
 
@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_shade(const __gri
                 storePath<LIGHT>(w, st, p);
                 live = true;
             } else {
-                finishPath<LIGHT, A>(c, st, p);
+                finishPath<LIGHT, A, RESTIR>(c, st, p);
             }
         }
         __syncwarp();

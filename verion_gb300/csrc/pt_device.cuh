@@ -793,6 +793,132 @@ static __device__ __forceinline__ void restirClear(const Ctx& c, uint32_t pixel)
     float4 g = c.re.g[cur][pixel];
     g.w = __uint_as_float(0u);
     c.re.g[cur][pixel] = g;
+    if (c.re.gl[cur]) {
+        float4 l = c.re.gl[cur][pixel];
+        l.w = __uint_as_float(0u);
+        c.re.gl[cur][pixel] = l;
+    }
+}
+
+// pt_core.slang:897-981 (ReSTIR GI, first half): the previous frame's second-hit samples of this
+// pixel and its neighbours, reconnected to this shading point (the Jacobian of the solid-angle
+// change, at most 10 either way), resampled by their reflected luminance; a candidate must see the
+// point. The pick waits in the scratch planes for giFinish.
+static __device__ __noinline__ void restirGIPrepare(const Ctx& c, uint32_t pixel, V3 p, V3 n, float pHitT,
+                                                   const Surface& surf, V3 T, V3 B, V3 woL, Rng& rng)
+{
+    uint32_t w = c.p[P_WIDTH];
+    uint32_t cur = c.p[P_SAMPLE] & 1u;
+    float cap = (float)max(c.p[P_RESTIR_HISTORY], 1u);
+    float wsum = 0.0f, mTotal = 0.0f, pSel = 0.0f;
+    V3 cSel = v3(0.0f), xSel = v3(0.0f), nSel = v3(0.0f), lSel = v3(0.0f);
+    if (c.p[P_SAMPLE] > 0) {
+        int px = (int)(pixel % w);
+        int py = (int)(pixel / w);
+        uint32_t prev = cur ^ 1u;
+        for (uint32_t k = 0; k < 1 + RESTIR_NEIGHBOURS; k++) {
+            int nx = px, ny = py;
+            if (k > 0) {
+                nx += (int)(rng.next() * (float)(2 * RESTIR_RADIUS + 1)) - RESTIR_RADIUS;
+                ny += (int)(rng.next() * (float)(2 * RESTIR_RADIUS + 1)) - RESTIR_RADIUS;
+                if (nx < 0 || ny < 0 || nx >= (int)w || ny >= (int)c.p[P_HEIGHT])
+                    continue;
+            }
+            uint32_t q = (uint32_t)ny * w + (uint32_t)nx;
+            float4 G = c.re.g[prev][q];
+            float4 L = c.re.gl[prev][q];
+            if (__float_as_uint(G.w) == 0 || __float_as_uint(L.w) == 0)
+                continue;
+            float4 Nn = c.re.n[prev][q];
+            V3 pq = v3(G.x, G.y, G.z);
+            V3 nq = v3(Nn.x, Nn.y, Nn.z);
+            if (dot(nq, n) < 0.9f || length(pq - p) > 0.05f * fmaxf(pHitT, 0.01f))
+                continue;
+            float4 X = c.re.gx[prev][q];
+            float4 N2 = c.re.gn[prev][q];
+            V3 x2 = v3(X.x, X.y, X.z);
+            V3 n2 = v3(N2.x, N2.y, N2.z);
+            V3 l2 = v3(L.x, L.y, L.z);
+            float mq = fminf(N2.w, cap);
+            mTotal += mq;
+            V3 toX = x2 - p;
+            float dR = length(toX);
+            V3 wi = toX / fmaxf(dR, 1.0e-6f);
+            float dQ = length(x2 - pq);
+            float cosT = dot(n, wi);
+            float cosR = fabsf(dot(n2, wi));
+            float cosQ = fabsf(dot(n2, normalize(pq - x2)));
+            if (cosT <= 0.0f || dR < 1.0e-3f || cosR < 1.0e-3f || cosQ < 1.0e-3f)
+                continue;
+            float jac = (cosR / cosQ) * (dQ * dQ) / (dR * dR);
+            if (jac > 10.0f || jac < 1.0f / 10.0f)
+                continue;
+            V3 cc = evalReflective(c, surf, woL, v3(dot(wi, T), dot(wi, B), cosT)) * l2;
+            float phat = lum(cc);
+            if (phat <= 0.0f || occluded(c, p, wi, dR * (1.0f - 1.0e-3f)))
+                continue;
+            float wgt = phat * X.w * mq * jac;
+            wsum += wgt;
+            if (rng.next() * wsum < wgt) {
+                pSel = phat;
+                cSel = cc;
+                xSel = x2;
+                nSel = n2;
+                lSel = l2;
+            }
+        }
+    }
+    c.re.s[0][pixel] = make_float4(wsum, mTotal, pSel, __uint_as_float(0u));
+    c.re.s[1][pixel] = make_float4(cSel.x, cSel.y, cSel.z, 0.0f);
+    c.re.s[2][pixel] = make_float4(xSel.x, xSel.y, xSel.z, 0.0f);
+    c.re.s[3][pixel] = make_float4(nSel.x, nSel.y, nSel.z, 0.0f);
+    c.re.s[4][pixel] = make_float4(lSel.x, lSel.y, lSel.z, 0.0f);
+}
+
+// pt_core.slang:1566-1617 (ReSTIR GI, second half): the path's own candidate (the surface its
+// first bounce reached, with the radiance the rest of the path gathered there) joins the
+// resampled ones; the pixel gets its direct light plus the indirect light of the pick, and the new
+// reservoir goes to this frame's parity for the next frame.
+static __device__ __noinline__ V3 giFinish(const Ctx& c, V3 pathTotal, uint32_t pixel)
+{
+    uint32_t cur = c.p[P_SAMPLE] & 1u;
+    float4 s0 = c.re.s[0][pixel], s1 = c.re.s[1][pixel], s2 = c.re.s[2][pixel], s3 = c.re.s[3][pixel];
+    float4 s4 = c.re.s[4][pixel], s5 = c.re.s[5][pixel], s6 = c.re.s[6][pixel];
+    float wsum = s0.x;
+    float m = s0.y + 1.0f;
+    float pSel = s0.z;
+    V3 cSel = v3(s1.x, s1.y, s1.z), xSel = v3(s2.x, s2.y, s2.z), nSel = v3(s3.x, s3.y, s3.z);
+    V3 lSel = v3(s4.x, s4.y, s4.z), thr1 = v3(s5.x, s5.y, s5.z), d0 = v3(s6.x, s6.y, s6.z);
+    float qPrev = s1.w;
+    bool own = __float_as_uint(s0.w) != 0 && qPrev > 0.0f;
+    V3 giTotal = pathTotal - d0;
+    V3 result = d0;
+    if (own) {
+        V3 cOwn = giTotal * qPrev;
+        float pOwn = lum(cOwn);
+        if (pOwn > 0.0f) {
+            float wOwn = pOwn / qPrev;
+            wsum += wOwn;
+            Rng r;
+            r.state = pcg(pixel ^ pcg(c.p[P_SAMPLE] * 0x85EBCA6Bu + 0x1234u));
+            if (r.next() * wsum < wOwn) {
+                pSel = pOwn;
+                cSel = cOwn;
+                float4 X = c.re.gx[cur][pixel], N2 = c.re.gn[cur][pixel];
+                xSel = v3(X.x, X.y, X.z);
+                nSel = v3(N2.x, N2.y, N2.z);
+                lSel = v3(thr1.x > 1.0e-6f ? giTotal.x / thr1.x : 0.0f, thr1.y > 1.0e-6f ? giTotal.y / thr1.y : 0.0f,
+                          thr1.z > 1.0e-6f ? giTotal.z / thr1.z : 0.0f);
+            }
+        }
+    } else
+        result = result + giTotal;
+    float W = pSel > 0.0f ? wsum / (m * pSel) : 0.0f;
+    result = result + cSel * W;
+    c.re.gx[cur][pixel] = make_float4(xSel.x, xSel.y, xSel.z, W);
+    c.re.gn[cur][pixel] = make_float4(nSel.x, nSel.y, nSel.z, m);
+    c.re.gl[cur][pixel] = make_float4(lSel.x, lSel.y, lSel.z, __uint_as_float(pSel > 0.0f ? 1u : 0u));
+    return result;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -908,6 +1034,15 @@ __device__ bool shadePath(const Ctx& c, PathState<LIGHT>& st, Hit hq, uint32_t d
             break;
         }
         V3 p = hit + ng * 1.0e-4f;
+        if (RESTIR && depth == 1 && st.gi) {
+            // pt_core.slang:1072-1082: the first bounce's surface is ReSTIR GI's candidate.
+            uint32_t cur = c.p[P_SAMPLE] & 1u;
+            c.re.gx[cur][pixel] = make_float4(hit.x, hit.y, hit.z, 0.0f);
+            c.re.gn[cur][pixel] = make_float4(ng.x, ng.y, ng.z, 0.0f);
+            float4 s0 = c.re.s[0][pixel];
+            s0.w = __uint_as_float(1u);
+            c.re.s[0][pixel] = s0;
+        }
 
         V3 nsObj = (1.0f - b1 - b2) * vertexNormal(c, i0) + b1 * vertexNormal(c, i1) + b2 * vertexNormal(c, i2);
         V3 ns = nOut;
@@ -980,6 +1115,12 @@ __device__ bool shadePath(const Ctx& c, PathState<LIGHT>& st, Hit hq, uint32_t d
                 wB = st.qPrev * st.qPrev / (st.qPrev * st.qPrev + pl * pl);
             }
             st.parts.add(depth, cls, thr * le * wB);
+            if (RESTIR && depth == 1 && st.gi) {
+                // pt_core.slang:1161-1168: counted with what the first hit gathered itself.
+                V3 e = thr * le * wB;
+                float4 d = c.re.s[6][pixel];
+                c.re.s[6][pixel] = make_float4(d.x + e.x, d.y + e.y, d.z + e.z, d.w);
+            }
         }
         float metallic = fget(M, mi + 6) * texRy;
         float rough = fget(M, mi + 7) * texRx;
@@ -1017,6 +1158,12 @@ __device__ bool shadePath(const Ctx& c, PathState<LIGHT>& st, Hit hq, uint32_t d
                 thr *= 3.0f * v3(chan == 0 ? 1.0f : 0.0f, chan == 1 ? 1.0f : 0.0f, chan == 2 ? 1.0f : 0.0f);
             }
             ior = fmaxf(ior + (float)(chan - 1) * (ior - 1.0f) * 0.025f * dispersion, 1.0f);
+        }
+        if (RESTIR && depth == 1 && st.gi && transmission > 0.0f) {
+            // pt_core.slang:1187-1190: a glass second hit cannot be reconnected to.
+            float4 s0 = c.re.s[0][pixel];
+            s0.w = __uint_as_float(0u);
+            c.re.s[0][pixel] = s0;
         }
         float alpha = fmaxf(rough * rough, 1.0e-3f);
         float eta = outside ? ior : 1.0f / ior;
@@ -1106,11 +1253,15 @@ __device__ bool shadePath(const Ctx& c, PathState<LIGHT>& st, Hit hq, uint32_t d
             bool suits = pf(c, P_APERTURE) == 0.0f && transmission == 0.0f && surf.alpha >= RESTIR_MIN_ALPHA &&
                          (surf.coat == 0.0f || surf.coatAlpha >= RESTIR_MIN_ALPHA);
             reDI = suits && (c.p[P_RESTIR] & 1u) != 0 && emitterCount > 0;
+            // ReSTIR GI replaces the path's own indirect light, which the lighting split cannot follow.
+            bool reGI = suits && (c.p[P_RESTIR] & 2u) != 0 && !lightingOn;
             st.restir = reDI;
-            st.gi = false;
-            if (suits)
+            st.gi = reGI;
+            if (suits) {
                 restirGbuffer(c, pixel, p, n);
-            else
+                if (reGI)
+                    restirGIPrepare(c, pixel, p, n, pHitT, surf, T, B, woL, rng);
+            } else
                 restirClear(c, pixel);
         }
         if (RESTIR && reDI) {
@@ -1338,6 +1489,14 @@ __device__ bool shadePath(const Ctx& c, PathState<LIGHT>& st, Hit hq, uint32_t d
     st.thr = thr;
     st.cls = cls;
     st.chan = chan;
+    if (RESTIR && depth == 0 && st.gi) {
+        // pt_core.slang:1531-1541: what the first hit gathered and what the first bounce carries on.
+        c.re.s[5][pixel] = make_float4(thr.x, thr.y, thr.z, 0.0f);
+        c.re.s[6][pixel] = make_float4(st.parts.total.x, st.parts.total.y, st.parts.total.z, 0.0f);
+        float4 s1 = c.re.s[1][pixel];
+        s1.w = st.qPrev;
+        c.re.s[1][pixel] = s1;
+    }
     return alive;
 }
 
@@ -1359,13 +1518,22 @@ __device__ __forceinline__ bool pixelActive(const Ctx& c, uint32_t p)
 
 // pt_core.slang:1620-1667: adds a finished path to its pixel's sums. Only this path's thread
 // writes the pixel during a sample, so plain read-modify-writes keep the reference's order.
-template <bool LIGHT, typename A>
+template <bool LIGHT, typename A, bool GI = false>
 __device__ void finishPath(const Ctx& c, const PathState<LIGHT>& st, uint32_t pixel)
 {
     Parts<LIGHT> parts = st.parts;
     float visLit = st.visLit;
     float visTotal = st.visTotal;
     V3 radiance = parts.total;
+    if (GI && st.gi) {
+        // pt_core.slang:1627-1633: a dispersive path follows one channel and is not shared.
+        if (st.chan >= 0) {
+            float4 s0 = c.re.s[0][pixel];
+            s0.w = __uint_as_float(0u);
+            c.re.s[0][pixel] = s0;
+        }
+        radiance = giFinish(c, radiance, pixel);
+    }
     if (bad3(radiance)) {
         radiance = v3(0.0f);
         parts.zero();

@@ -528,8 +528,6 @@ int vg_set_restir(VgRenderer* r, int on, int di, int gi, uint32_t candidates, ui
 {
     if (!r)
         return fail(VG_ERR_INVALID, "null renderer");
-    if (on && gi)
-        return fail(VG_ERR_UNSUPPORTED, "ReSTIR GI is not available in this backend");
     r->restir.on = on != 0;
     r->restir.di = di != 0;
     r->restir.gi = gi != 0;
@@ -620,6 +618,9 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
             acc->re_n[h].release();
             acc->re_x[h].release();
             acc->re_m[h].release();
+            acc->re_gx[h].release();
+            acc->re_gn[h].release();
+            acc->re_gl[h].release();
         }
         acc->restir_bytes = 0;
         if (r->restir.on) {
@@ -629,8 +630,17 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
                     (st = alloc(acc->re_x[h], px * 16, s, true)) != VG_OK ||
                     (st = alloc(acc->re_m[h], px * 4, s, true)) != VG_OK)
                     return st;
+                if (r->restir.gi && ((st = alloc(acc->re_gx[h], px * 16, s, true)) != VG_OK ||
+                                     (st = alloc(acc->re_gn[h], px * 16, s, true)) != VG_OK ||
+                                     (st = alloc(acc->re_gl[h], px * 16, s, true)) != VG_OK))
+                    return st;
             }
-            acc->restir_bytes = px * 2 * (16 * 3 + 4);
+            for (int k = 0; k < 7; k++) {
+                acc->re_s[k].release();
+                if (r->restir.gi && (st = alloc(acc->re_s[k], px * 16, s, true)) != VG_OK)
+                    return st;
+            }
+            acc->restir_bytes = px * 2 * (16 * 3 + 4) + (r->restir.gi ? px * (2 * 48 + 7 * 16) : 0);
         }
     }
     if (!(acc->restir == r->restir))
