@@ -289,6 +289,46 @@ int vg_trace_closest_device(VgRenderer* r, const float* d_rays, size_t n, uint32
 #define VG_TRACE_NOALLOC_MAX_RAYS 65536u
 int vg_trace_closest_noalloc(VgRenderer* r, const float* rays, size_t n, uint32_t* hits);
 
+/* ---- Batched rendering (no reference counterpart) -----------------------------------------------
+ * Many render requests in one persistent launch: the work items (16 x 8 pixel tiles with all of a
+ * request's samples) of every request are laid out shortest request first (or as given, or longest
+ * first) and taken by the CTAs of one kernel, so small requests finish early while large ones fill
+ * the GPU. A plain request's samples are exactly what vg_accumulate's megakernel adds (same sums);
+ * a request with a cache ends its paths at the cache and evaluates the cache inside the same CTA
+ * (tensor cores); after the launch each cache takes its renderer's training steps (vg_set_cache)
+ * on the batch's training records. The sequence after the request upload is captured in a CUDA
+ * graph the first time and replayed while the batch keeps the same shape (same renderers,
+ * accumulations, sample counts and caches in the same order). */
+typedef enum VgBatchOrder { VG_BATCH_SHORTEST_FIRST = 0, VG_BATCH_AS_GIVEN = 1, VG_BATCH_LONGEST_FIRST = 2 } VgBatchOrder;
+
+typedef struct VgBatchRequest {
+    VgRenderer* renderer; /* scene and settings: megakernel paths without adaptive sampling, ReSTIR or the lighting split */
+    VgAccum* accum;       /* the request's accumulation (its size is the frame size) */
+    uint32_t samples;     /* samples per pixel to add */
+    VgCache* cache;       /* null: plain path tracing; else the renderer's vg_set_cache settings apply */
+} VgBatchRequest;
+
+typedef struct VgBatchResult {
+    double seconds; /* from the batch's start to this request's last tile, device clock */
+} VgBatchResult;
+
+/* Renders all requests (blocking). *total_seconds (optional) is the whole batch on the device
+ * clock, training included; *graph_replayed (optional) tells whether the captured graph was reused. */
+int vg_batch_render(VgContext* ctx, const VgBatchRequest* requests, size_t n, VgBatchResult* out,
+                    double* total_seconds, int* graph_replayed);
+/* Batch kernel CTAs per SM (0: as many as fit) and the item order; vg_batch_tune picks them. */
+int vg_set_batch_options(VgContext* ctx, int blocks_per_sm, int order);
+/* Autotuner: times the batch on scratch accumulations of the requests' sizes for each order and
+ * each CTA count per SM that fits, keeps the setting with the lowest objective (median request
+ * latency plus the total time) and reports it. The requests' own accumulations are not touched. */
+typedef struct VgBatchTune {
+    int blocks_per_sm;
+    int order;
+    double p50_seconds, p99_seconds, total_seconds; /* of the chosen setting */
+    uint32_t trials;
+} VgBatchTune;
+int vg_batch_tune(VgContext* ctx, const VgBatchRequest* requests, size_t n, VgBatchTune* out);
+
 /* ---- EXR output (crates/verion-render-io/src/exr_out.rs) -----------------------------------------
  * Working and target colour spaces, tone map and transfer function (crates/verion-scene/src/color.rs). */
 typedef enum VgColorSpace { VG_COLOR_LINEAR_REC709 = 0, VG_COLOR_ACESCG = 1 } VgColorSpace;

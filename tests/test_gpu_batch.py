@@ -1,0 +1,124 @@
+"""Batched rendering (vg_batch_render): requests of uneven size, scene and sample count in one
+persistent launch. Plain requests add exactly what a megakernel accumulate adds; a cached request
+without training adds exactly what the cache integrator adds; repeated batches replay the captured
+graph; the autotuner returns a setting that renders the same sums."""
+import numpy as np
+import pytest
+
+from verion_gb300 import pack, scenes
+from verion_gb300.backend import (BATCH_AS_GIVEN, BATCH_LONGEST_FIRST, BATCH_SHORTEST_FIRST, BatchRequest, Cache,
+                                  Error, Integrator, Renderer)
+from verion_gb300.readback import Adaptive
+
+pytestmark = pytest.mark.gpu
+
+
+def scenes_for_batch():
+    return [pack.pack(scenes.cornell()), pack.pack(scenes.furnace_room(0.5, 1.0)),
+            pack.pack(scenes.many_spheres(hdri=(64, 32)))]
+
+
+SPEC = [(0, 40, 30, 8, 32), (1, 17, 13, 3, 64), (2, 48, 27, 2, 32), (0, 96, 64, 4, 64), (2, 33, 71, 3, 64),
+        (1, 128, 96, 1, 32)]
+
+
+def make(ctx, packed):
+    rs, accs = [], []
+    for si, w, h, spp, prec in SPEC:
+        r = Renderer(ctx, packed[si])
+        r.set_accum_precision(prec)
+        r.set_max_depth(16 if si == 2 else 8)
+        rs.append(r)
+        accs.append(r.new_accumulation(w, h))
+    return rs, accs
+
+
+@pytest.mark.parametrize("order", [BATCH_SHORTEST_FIRST, BATCH_AS_GIVEN, BATCH_LONGEST_FIRST])
+def test_plain_requests_match_megakernel_accumulates(gpu_ctx, order):
+    packed = scenes_for_batch()
+    rs, accs = make(gpu_ctx, packed)
+    gpu_ctx.set_batch_options(0, order)
+    reqs = [BatchRequest(r, a, spec[3]) for r, a, spec in zip(rs, accs, SPEC)]
+    out = gpu_ctx.batch_render(reqs)
+    again = gpu_ctx.batch_render(reqs)  # same shape: the captured graph is replayed
+    assert again.graph_replayed
+    assert all(t > 0 for t in out.seconds) and out.total_seconds >= max(out.seconds) * 0.5
+    for (si, w, h, spp, prec), a in zip(SPEC, accs):
+        r = Renderer(gpu_ctx, packed[si])
+        r.set_accum_precision(prec)
+        r.set_max_depth(16 if si == 2 else 8)
+        r.set_integrator(Integrator.MEGAKERNEL)
+        ref = r.new_accumulation(w, h)
+        r.accumulate(ref, spp)
+        r.accumulate(ref, spp)
+        assert a.samples() == 2 * spp
+        if prec == 64:
+            assert np.array_equal(a.sums_f64(), ref.sums_f64())
+        else:
+            assert np.array_equal(a.sums(), ref.sums())
+    gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST)
+
+
+def test_shortest_first_finishes_small_requests_early(gpu_ctx):
+    packed = scenes_for_batch()
+    r = Renderer(gpu_ctx, packed[2])
+    r.set_max_depth(16)
+    sizes = [(32, 32, 1), (256, 256, 4), (64, 64, 2), (512, 256, 4)]
+    reqs = [BatchRequest(r, r.new_accumulation(w, h), spp) for w, h, spp in sizes]
+    gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST)
+    out = gpu_ctx.batch_render(reqs)
+    assert out.seconds[0] < out.seconds[1] and out.seconds[0] < out.seconds[3]
+    assert max(out.seconds) == out.seconds[3]
+
+
+def test_cached_request_matches_the_cache_integrator_without_training(gpu_ctx):
+    p = pack.pack(scenes.cornell())
+    w, h, spp = 48, 40, 4
+    r1 = Renderer(gpu_ctx, p)
+    c1 = Cache(gpu_ctx, bounds=r1.bounds())
+    r1.set_cache(c1, spread=0.01, train_paths=256, train_steps=0, train_batch=1024)
+    a1 = r1.new_accumulation(w, h)
+    r1.accumulate(a1, spp)
+    r2 = Renderer(gpu_ctx, p)
+    c2 = Cache(gpu_ctx, bounds=r2.bounds())
+    r2.set_cache(c2, spread=0.01, train_paths=256, train_steps=0, train_batch=1024)
+    a2 = r2.new_accumulation(w, h)
+    plain = r2.new_accumulation(w, h)
+    out = gpu_ctx.batch_render([BatchRequest(r2, a2, spp, c2), BatchRequest(r2, plain, 2)])
+    assert len(out.seconds) == 2
+    assert np.array_equal(a2.sums_f64(), a1.sums_f64())
+
+
+def test_cached_requests_train_their_cache(gpu_ctx):
+    p = pack.pack(scenes.cornell())
+    r = Renderer(gpu_ctx, p)
+    cache = Cache(gpu_ctx, bounds=r.bounds())
+    r.set_cache(cache, spread=0.01, train_paths=1024, train_steps=2, train_batch=4096)
+    before, _ = cache.read_params()
+    gpu_ctx.batch_render([BatchRequest(r, r.new_accumulation(64, 64), 2, cache)])
+    after, _ = cache.read_params()
+    assert not np.array_equal(before, after)
+
+
+def test_tune_picks_a_setting_and_keeps_the_sums(gpu_ctx):
+    packed = scenes_for_batch()
+    rs, accs = make(gpu_ctx, packed)
+    reqs = [BatchRequest(r, a, spec[3]) for r, a, spec in zip(rs, accs, SPEC)]
+    t = gpu_ctx.batch_tune(reqs)
+    assert t["trials"] >= 3 and t["blocks_per_sm"] >= 1 and t["p50_seconds"] > 0
+    assert all(a.samples() == 0 for a in accs)  # the tuner used scratch accumulations
+    gpu_ctx.batch_render(reqs)
+    si, w, h, spp, prec = SPEC[0]
+    r = Renderer(gpu_ctx, packed[si])
+    r.set_accum_precision(prec)
+    ref = r.new_accumulation(w, h)
+    r.accumulate(ref, spp)
+    assert np.array_equal(accs[0].sums(), ref.sums())
+    gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST)
+
+
+def test_batch_rejects_adaptive_requests(gpu_ctx):
+    r = Renderer(gpu_ctx, scenes.cornell())
+    r.set_adaptive(Adaptive())
+    with pytest.raises(Error):
+        gpu_ctx.batch_render([BatchRequest(r, r.new_accumulation(16, 16), 1)])

@@ -108,6 +108,34 @@ class CacheStats(C.Structure):
                 ("path_seconds", C.c_double), ("infer_seconds", C.c_double), ("train_seconds", C.c_double)]
 
 
+class _BatchRequest(C.Structure):
+    _fields_ = [("renderer", C.c_void_p), ("accum", C.c_void_p), ("samples", C.c_uint32), ("cache", C.c_void_p)]
+
+
+class _BatchTune(C.Structure):
+    _fields_ = [("blocks_per_sm", C.c_int), ("order", C.c_int), ("p50_seconds", C.c_double),
+                ("p99_seconds", C.c_double), ("total_seconds", C.c_double), ("trials", C.c_uint32)]
+
+
+BATCH_SHORTEST_FIRST, BATCH_AS_GIVEN, BATCH_LONGEST_FIRST = 0, 1, 2
+
+
+@dataclass
+class BatchRequest:
+    """One request of vg_batch_render."""
+    renderer: "Renderer"
+    accum: "Accumulation"
+    samples: int
+    cache: Optional["Cache"] = None
+
+
+@dataclass
+class BatchOutcome:
+    seconds: list          # per request, from the batch start to its last tile (device clock)
+    total_seconds: float   # the whole batch, training included
+    graph_replayed: bool
+
+
 class _UpdatePlan(C.Structure):
     _fields_ = [("full", C.c_int), ("materials", C.c_int), ("lights", C.c_int), ("emitters", C.c_int),
                 ("instances", C.c_int), ("vertices", C.c_int), ("blases", C.c_void_p), ("blas_count", C.c_size_t),
@@ -202,6 +230,9 @@ def lib() -> C.CDLL:
             "vg_cache_train": (i32, [vp, vp, _S, u32, C.POINTER(f64)]),
             "vg_set_cache": (i32, [vp, vp, C.c_float, u32, u32, u32]),
             "vg_cache_time": (i32, [vp, vp, _S, u32, C.POINTER(f64)]),
+            "vg_batch_render": (i32, [vp, vp, _S, vp, C.POINTER(f64), C.POINTER(C.c_int)]),
+            "vg_set_batch_options": (i32, [vp, i32, i32]),
+            "vg_batch_tune": (i32, [vp, vp, _S, C.POINTER(_BatchTune)]),
             "vg_accum_cache_stats": (i32, [vp, C.POINTER(CacheStats)]),
         }
         for name, (res, args) in sig.items():
@@ -258,6 +289,36 @@ class Context:
         m = MemoryUsage()
         _check(lib().vg_memory(self._h, C.byref(m)))
         return m
+
+    def batch_render(self, requests) -> "BatchOutcome":
+        """vg_batch_render: `requests` are BatchRequest(renderer, accumulation, samples, cache)."""
+        arr = (_BatchRequest * len(requests))()
+        for i, q in enumerate(requests):
+            arr[i].renderer = q.renderer._h
+            arr[i].accum = q.accum._h
+            arr[i].samples = q.samples
+            arr[i].cache = q.cache._h if q.cache is not None else None
+        out = (C.c_double * len(requests))()
+        total = C.c_double()
+        replayed = C.c_int()
+        _check(lib().vg_batch_render(self._h, arr, len(requests), out, C.byref(total), C.byref(replayed)))
+        return BatchOutcome(list(out), total.value, bool(replayed.value))
+
+    def set_batch_options(self, blocks_per_sm: int = 0, order: int = 0) -> None:
+        _check(lib().vg_set_batch_options(self._h, blocks_per_sm, order))
+
+    def batch_tune(self, requests) -> dict:
+        """vg_batch_tune: picks the batch kernel's CTAs per SM and item order for these requests."""
+        arr = (_BatchRequest * len(requests))()
+        for i, q in enumerate(requests):
+            arr[i].renderer = q.renderer._h
+            arr[i].accum = q.accum._h
+            arr[i].samples = q.samples
+            arr[i].cache = q.cache._h if q.cache is not None else None
+        t = _BatchTune()
+        _check(lib().vg_batch_tune(self._h, arr, len(requests), C.byref(t)))
+        return {"blocks_per_sm": t.blocks_per_sm, "order": t.order, "p50_seconds": t.p50_seconds,
+                "p99_seconds": t.p99_seconds, "total_seconds": t.total_seconds, "trials": t.trials}
 
     def close(self):
         if self._h:

@@ -1,0 +1,32 @@
+// One request of a batched render (vg_batch_render): what the persistent batch kernel needs to run
+// its work items. Host and device share this layout.
+#pragma once
+#include "ctx.h"
+#include "nrc.cuh"
+
+namespace vgb {
+
+struct alignas(16) BatchReq {
+    vgd::Ctx c;             // scene tables, parameter block (samples from P_SAMPLE, P_SAMPLES_PER_DISPATCH of them), sums
+    vgn::CacheDev cd;       // the radiance cache of a cached request
+    uint32_t cached;        // 1: paths end at the cache (fused inference), 0: plain paths
+    uint32_t f64;           // sums in double precision
+    float spread;           // cache: path-spread threshold
+    uint32_t train_stride;  // cache: one pixel in train_stride traces a training path per sample
+    float* trec;            // cache: training records (shared by the requests of one cache)
+    uint32_t* tcount;
+    uint32_t tcap;
+    uint32_t item_begin;    // this request's work items: [item_begin, item_begin + tiles)
+    uint32_t tiles;
+    uint32_t tiles_x;       // 16 x 8 pixel tiles per row
+    uint32_t index;         // position of the request in the caller's list
+};
+
+// Per-request completion, written by the CTA that finishes the request's last tile.
+struct BatchDone {
+    uint32_t remaining;           // tiles not finished yet
+    uint32_t pad;
+    unsigned long long done_ns;   // %globaltimer at completion
+};
+
+} // namespace vgb

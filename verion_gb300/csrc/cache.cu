@@ -3,46 +3,9 @@
 // per-sample loop of the cache integrator. No reference counterpart.
 #include <cmath>
 
-#include "host.h"
-#include "launch_nrc.h"
+#include "cache_host.h"
 
-struct VgCache {
-    VgContext* ctx = nullptr;
-    VgCacheConfig cfg{};
-    uint32_t res[vgn::MAX_LEVELS] = {};
-    uint32_t dense_mask = 0;
-    size_t grid_params = 0; // levels x entries x 2
-    DevBuf grid, grid_h, grid_grad, grid_m, grid_v;
-    DevBuf mlp, mlp_grad, mlp_m, mlp_v, img;
-    DevBuf loss, err, count;
-    DevBuf X, GX; // encoded input tiles, input-gradient rows (grown on demand)
-    uint32_t step = 0;
-
-    vgn::CacheDev dev() const
-    {
-        vgn::CacheDev d{};
-        d.grid = (const uint32_t*)grid_h.p;
-        d.grid_grad = (float*)grid_grad.p;
-        d.img = (const uint8_t*)img.p;
-        d.mlp_grad = (float*)mlp_grad.p;
-        d.loss = (double*)loss.p;
-        d.err = (uint32_t*)err.p;
-        d.levels = cfg.levels;
-        d.log2_t = cfg.log2_entries;
-        d.dense_mask = dense_mask;
-        for (uint32_t l = 0; l < vgn::MAX_LEVELS; l++)
-            d.res[l] = res[l];
-        float ext = 0.0f;
-        for (int k = 0; k < 3; k++) {
-            d.lo[k] = cfg.bounds_lo[k];
-            ext = std::max(ext, cfg.bounds_hi[k] - cfg.bounds_lo[k]);
-        }
-        d.inv_extent = 1.0f / ext;
-        return d;
-    }
-};
-
-namespace {
+namespace vgc {
 
 // Deterministic parameter initialisation: a PCG-hash stream of uniform numbers in [-1, 1).
 float uniform_pm1(uint32_t seed, uint64_t i)
@@ -86,7 +49,7 @@ int cache_reset_optimiser(VgCache* k)
     VG_CHECK(cudaMemsetAsync(k->mlp_grad.p, 0, k->mlp_grad.bytes, s), "clear");
     VG_CHECK(cudaMemsetAsync(k->mlp_m.p, 0, k->mlp_m.bytes, s), "clear");
     VG_CHECK(cudaMemsetAsync(k->mlp_v.p, 0, k->mlp_v.bytes, s), "clear");
-    k->step = 0;
+    VG_CHECK(cudaMemsetAsync(k->step.p, 0, 4, s), "clear");
     return VG_OK;
 }
 
@@ -131,14 +94,13 @@ int cache_train_step(VgCache* k, const float* rec, const uint32_t* count, uint32
     VG_CHECK(cudaMemsetAsync(k->loss.p, 0, 8, s), "loss");
     if ((st = cache_gradient_pass(k, rec, count, cap, offset, batch)) != VG_OK)
         return st;
-    k->step++;
+    VG_CHECK(vgx::nrc_launch_step(s, (uint32_t*)k->step.p), "step");
     NrcAdam a;
     a.lr = k->cfg.learning_rate;
     a.beta1 = k->cfg.beta1;
     a.beta2 = k->cfg.beta2;
     a.eps = k->cfg.epsilon;
-    a.bc1 = (float)(1.0 - std::pow((double)k->cfg.beta1, (double)k->step));
-    a.bc2 = (float)(1.0 - std::pow((double)k->cfg.beta2, (double)k->step));
+    a.step = (const uint32_t*)k->step.p;
     VG_CHECK(vgx::nrc_launch_adam(s, (float*)k->mlp.p, (float*)k->mlp_grad.p, (float*)k->mlp_m.p, (float*)k->mlp_v.p,
                                   vgn::MLP_PARAMS, count, cap, offset, batch, a, nullptr, false),
              "adam");
@@ -164,7 +126,9 @@ int stage_records(VgCache* k, DevBuf& b, const float* records, size_t n)
     return VG_OK;
 }
 
-} // namespace
+} // namespace vgc
+
+using namespace vgc;
 
 // The cache integrator's samples (called by vg_accumulate with the parameter block filled in).
 int cache_accumulate(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, uint32_t samples, bool timed)
@@ -227,7 +191,7 @@ int cache_accumulate(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, uint32_t samples,
         for (uint32_t t = 0; t < r->cache_steps; t++) {
             if ((st = cache_train_step(k, a.trec, ctr + 1, tcap, t * r->cache_batch, r->cache_batch)) != VG_OK)
                 return st;
-            acc->launches += 6;
+            acc->launches += 7;
         }
         if (timed) {
             VG_CHECK(cudaEventRecord(e3, s), "event");
@@ -296,6 +260,7 @@ int vg_cache_create(VgContext* ctx, const VgCacheConfig* cfg, VgCache** out)
             return fail(VG_ERR_INVALID, "cache bounds are not a box");
     if (!(std::max({c.bounds_hi[0] - c.bounds_lo[0], c.bounds_hi[1] - c.bounds_lo[1], c.bounds_hi[2] - c.bounds_lo[2]}) > 0.0f))
         return fail(VG_ERR_INVALID, "cache bounds are empty");
+    vgx::nrc_prepare();
     VgCache* k = new VgCache();
     k->ctx = ctx;
     k->cfg = c;
@@ -323,7 +288,8 @@ int vg_cache_create(VgContext* ctx, const VgCacheConfig* cfg, VgCache** out)
         (st = alloc(k->mlp_m, vgn::MLP_PARAMS * 4, s, true)) != VG_OK ||
         (st = alloc(k->mlp_v, vgn::MLP_PARAMS * 4, s, true)) != VG_OK ||
         (st = alloc(k->img, vgn::IMG_BYTES, s, true)) != VG_OK || (st = alloc(k->loss, 8, s, true)) != VG_OK ||
-        (st = alloc(k->err, 4, s, true)) != VG_OK || (st = alloc(k->count, 4, s, true)) != VG_OK) {
+        (st = alloc(k->err, 4, s, true)) != VG_OK || (st = alloc(k->count, 4, s, true)) != VG_OK ||
+        (st = alloc(k->step, 4, s, true)) != VG_OK) {
         delete k;
         return st;
     }

@@ -108,11 +108,17 @@ struct DevBuf {
 
 } // namespace
 
+struct BatchState; // vg_batch_render's device buffers and captured graph (batch.cu)
+
 struct VgContext {
     int device = 0;
     cudaStream_t stream = nullptr;
     int sms = 0;
     uint64_t uploaded = 0;
+    BatchState* batch = nullptr;
+    int batch_blocks_per_sm = 0; // 0: as many as fit (vg_batch_tune chooses)
+    int batch_order = 0;         // VgBatchOrder
+    ~VgContext();
 };
 
 struct Restir {

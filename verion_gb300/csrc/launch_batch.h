@@ -1,0 +1,15 @@
+// Host-side launcher of the batch kernel (kern_batch.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "batch.h"
+
+namespace vgx {
+
+// Resident batch CTAs per SM (occupancy of the batch kernel with its shared memory).
+int batch_blocks_per_sm();
+// Writes the start time to *t0, then runs `items` work items of `nreq` requests (sorted by item_begin).
+cudaError_t launch_batch(int blocks, cudaStream_t s, const vgb::BatchReq* reqs, uint32_t nreq, uint32_t items,
+                         uint32_t* next, vgb::BatchDone* done, uint32_t* err, unsigned long long* t0);
+
+} // namespace vgx

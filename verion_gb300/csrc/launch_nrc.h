@@ -5,9 +5,11 @@
 #include "ctx.h"
 #include "nrc.cuh"
 
+// Adam settings; the step count t lives on the device (nrc_launch_step advances it), so a captured
+// training sequence replays with the right bias corrections.
 struct NrcAdam {
     float lr, beta1, beta2, eps;
-    float bc1, bc2; // 1 - beta1^t, 1 - beta2^t
+    const uint32_t* step;
 };
 
 // Path-kernel outputs: query records (one per pixel at most) and training records.
@@ -24,6 +26,9 @@ struct NrcPathArgs {
 
 namespace vgx {
 
+// Sets the cache kernels' shared-memory limits (once; before any stream capture).
+void nrc_prepare();
+
 // Input tiles of records [offset, offset + limit) of the first min(*count, cap) (kern_nrc.cu).
 cudaError_t nrc_launch_encode(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const float* rec,
                               const uint32_t* count, uint32_t cap, uint32_t offset, uint32_t limit, uint8_t* X);
@@ -36,6 +41,7 @@ cudaError_t nrc_launch_train(int blocks, cudaStream_t s, const vgn::CacheDev& cd
 cudaError_t nrc_launch_adam(cudaStream_t s, float* p, float* g, float* m, float* v, size_t n, const uint32_t* count,
                             uint32_t cap, uint32_t offset, uint32_t batch, const NrcAdam& a, void* half_out,
                             bool lazy);
+cudaError_t nrc_launch_step(cudaStream_t s, uint32_t* step);
 cudaError_t nrc_launch_to_half(cudaStream_t s, const float* p, void* out, size_t n);
 cudaError_t nrc_launch_pack(cudaStream_t s, const float* w, uint8_t* img);
 cudaError_t nrc_launch_paths(bool f64, dim3 grid, cudaStream_t s, const vgd::Ctx& c, const NrcPathArgs& a);
