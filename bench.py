@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-cache", action="store_true", help="skip the radiance-cache measurement")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-serving measurement")
+    ap.add_argument("--batch-spp-scale", type=float, default=0.125,
+                    help="batched serving: fraction of the 16-256 spp range to render (1 = the full workload)")
     ap.add_argument("--profile-extend", action="store_true",
                     help="profiling helper: one step with traversal counters inside the NVTX range 'traffic', "
                          "then print the counters (for an ncu capture of the extend kernels' DRAM bytes)")
@@ -353,6 +356,88 @@ def cache_report(ctx, peak_tflops, peak_kind):
     }
 
 
+BATCH_SCENES = [(4, 15, 48), (16, 21, 160), (48, 31, 400), (128, 31, 724)]  # spheres, sphere resolution, grid
+
+
+def _pct(v, q):
+    v = sorted(v)
+    return v[min(len(v) - 1, max(0, int(math.ceil(q * len(v))) - 1))]
+
+
+def batch_report(ctx, spp_scale, side_range=(256, 2048), spp_range=(16, 256)):
+    """Batched serving (64 requests): resolution log-uniform 256^2-2048^2 (square), scenes of ~10k-2M
+    triangles generated like the 1M-triangle workload, spp log-uniform 16-256 (times spp_scale),
+    depth 16, every second request with a radiance cache. One batch (autotuned, graph replayed)
+    against the same requests rendered one at a time with accumulate (wavefront for plain
+    requests, the cache integrator for cached ones), shortest first; latency = device time from the
+    start until the request's last tile."""
+    from verion_gb300 import pack, scenes
+    from verion_gb300.backend import BatchRequest, Cache, Integrator, Renderer
+
+    rng = np.random.default_rng(0x5EED5EED)
+    plain_r, cached_r, tris = [], [], []
+    for sph, n, grid in BATCH_SCENES:
+        p = pack.pack(scenes.many_spheres(spheres=sph, sphere_n=n, grid=grid))
+        r = Renderer(ctx, p)
+        r.set_max_depth(DEPTH)
+        r.set_accum_precision(32)
+        rc = Renderer(ctx, p)
+        rc.set_max_depth(DEPTH)
+        rc.set_accum_precision(32)
+        cache = Cache(ctx, bounds=rc.bounds())
+        rc.set_cache(cache, spread=0.01, train_paths=16384, train_steps=4, train_batch=16384)
+        rc._batch_cache = cache
+        plain_r.append(r)
+        cached_r.append(rc)
+        tris.append(r.bvh_info().triangles)
+    spec = []
+    for i in range(64):
+        side = int(round(math.exp(rng.uniform(math.log(side_range[0]), math.log(side_range[1])))))
+        spp = max(1, int(round(math.exp(rng.uniform(math.log(spp_range[0]), math.log(spp_range[1]))) * spp_scale)))
+        spec.append((side, spp, int(rng.integers(len(BATCH_SCENES))), i % 2 == 1))
+
+    def requests():
+        out = []
+        for side, spp, si, cached in spec:
+            r = cached_r[si] if cached else plain_r[si]
+            out.append(BatchRequest(r, r.new_accumulation(side, side), spp, r._batch_cache if cached else None))
+        return out
+
+    paths = float(sum(side * side * spp for side, spp, _, _ in spec))
+    reqs = requests()
+    tune_reqs = [BatchRequest(q.renderer, q.accum, 1, q.cache) for q in reqs]
+    tuned = ctx.batch_tune(tune_reqs)
+    ctx.batch_render(reqs)  # captures the graph
+    out = ctx.batch_render(reqs)  # replays it
+    # One at a time, shortest first, through accumulate.
+    order = sorted(range(64), key=lambda i: spec[i][0] ** 2 * spec[i][1])
+    seq_t, now, lat = [], 0.0, [0.0] * 64
+    for i in order:
+        side, spp, si, cached = spec[i]
+        r = cached_r[si] if cached else plain_r[si]
+        if not cached:
+            r.set_integrator(Integrator.WAVEFRONT)
+        acc = r.new_accumulation(side, side)
+        r.accumulate(acc, spp)
+        now += acc.gpu_seconds()
+        lat[i] = now
+        del acc
+    for r in plain_r:
+        r.set_integrator(Integrator.MEGAKERNEL)
+    return {
+        "config": f"64 requests, square {min(s[0] for s in spec)}-{max(s[0] for s in spec)} px, "
+                  f"spp {min(s[1] for s in spec)}-{max(s[1] for s in spec)} ({spp_range[0]}-{spp_range[1]} x {spp_scale}), "
+                  f"depth {DEPTH}, "
+                  f"scenes of {min(tris)}-{max(tris)} triangles, 32 requests with a radiance cache",
+        "paths": paths,
+        "batch": {"p50_s": _pct(out.seconds, 0.5), "p99_s": _pct(out.seconds, 0.99), "total_s": out.total_seconds,
+                  "mpaths_s": paths / out.total_seconds / 1e6, "graph_replayed": out.graph_replayed,
+                  "tuned": tuned},
+        "one_at_a_time": {"p50_s": _pct(lat, 0.5), "p99_s": _pct(lat, 0.99), "total_s": now,
+                          "mpaths_s": paths / now / 1e6},
+    }
+
+
 def run_cuda(args):
     rank, world = dist_init(args)
     import torch
@@ -504,6 +589,10 @@ def run_cuda(args):
             if (ROOT / "MEASURED_PEAKS.json").exists() else None
         cache = cache_report(ctx, bf or 1900.0, "measured (bf16_tflops, burst)" if bf else "fallback")
 
+    batch = None
+    if rank == 0 and not args.no_batch:
+        batch = batch_report(ctx, args.batch_spp_scale)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu, _ = cpu_baseline(packed, args.cpu_seconds)
@@ -519,7 +608,7 @@ def run_cuda(args):
                 "clocks": clk.summary(),
                 "stage_seconds": {"extend": stage[0], "shade": stage[1]},
                 "paths_per_step": paths_all / args.steps,
-                "megakernel_value": mega, "radiance_cache": cache}
+                "megakernel_value": mega, "radiance_cache": cache, "batched_serving": batch}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

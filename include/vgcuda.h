@@ -291,9 +291,10 @@ int vg_trace_closest_noalloc(VgRenderer* r, const float* rays, size_t n, uint32_
 
 /* ---- Batched rendering (no reference counterpart) -----------------------------------------------
  * Many render requests in one persistent launch: the work items (16 x 8 pixel tiles with all of a
- * request's samples) of every request are laid out shortest request first (or as given, or longest
- * first) and taken by the CTAs of one kernel, so small requests finish early while large ones fill
- * the GPU. A plain request's samples are exactly what vg_accumulate's megakernel adds (same sums);
+ * request's samples) of every request below a size threshold are laid out shortest request first
+ * (or as given, or longest first) and taken by the CTAs of one kernel, so small requests finish
+ * early while the GPU stays full; requests above the threshold then run one at a time on the
+ * streaming wavefront, which is faster per path on large frames. A plain request's samples are exactly what vg_accumulate's megakernel adds (same sums);
  * a request with a cache ends its paths at the cache and evaluates the cache inside the same CTA
  * (tensor cores); after the launch each cache takes its renderer's training steps (vg_set_cache)
  * on the batch's training records. The sequence after the request upload is captured in a CUDA
@@ -316,14 +317,22 @@ typedef struct VgBatchResult {
  * clock, training included; *graph_replayed (optional) tells whether the captured graph was reused. */
 int vg_batch_render(VgContext* ctx, const VgBatchRequest* requests, size_t n, VgBatchResult* out,
                     double* total_seconds, int* graph_replayed);
-/* Batch kernel CTAs per SM (0: as many as fit) and the item order; vg_batch_tune picks them. */
-int vg_set_batch_options(VgContext* ctx, int blocks_per_sm, int order);
-/* Autotuner: times the batch on scratch accumulations of the requests' sizes for each order and
- * each CTA count per SM that fits, keeps the setting with the lowest objective (median request
- * latency plus the total time) and reports it. The requests' own accumulations are not touched. */
+/* The batch kernel's resident CTAs per SM, registers per thread, local bytes per thread, static
+ * shared bytes, and the CUDA status of the occupancy query, in that order. */
+int vg_batch_kernel_info(VgContext* ctx, int out[5]);
+/* Batch kernel CTAs per SM (0: as many as fit), the item order, and the size (pixels) from which a
+ * request leaves the shared launch and runs on its own through the streaming wavefront (or the
+ * cache integrator) after it, shortest first (~0: never; default 512 x 512). vg_batch_tune picks
+ * all three. */
+int vg_set_batch_options(VgContext* ctx, int blocks_per_sm, int order, uint64_t wavefront_pixels);
+/* Autotuner: times the batch on scratch accumulations of the requests' sizes for each wavefront
+ * threshold (256^2, 512^2, 1024^2 pixels, never), shortest or longest first, and the two largest
+ * CTA counts per SM that fit; keeps the setting with the lowest objective (median plus 99th
+ * percentile request latency) and reports it. The requests' own accumulations are not touched. */
 typedef struct VgBatchTune {
     int blocks_per_sm;
     int order;
+    uint64_t wavefront_pixels;
     double p50_seconds, p99_seconds, total_seconds; /* of the chosen setting */
     uint32_t trials;
 } VgBatchTune;

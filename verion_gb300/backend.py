@@ -113,7 +113,8 @@ class _BatchRequest(C.Structure):
 
 
 class _BatchTune(C.Structure):
-    _fields_ = [("blocks_per_sm", C.c_int), ("order", C.c_int), ("p50_seconds", C.c_double),
+    _fields_ = [("blocks_per_sm", C.c_int), ("order", C.c_int), ("wavefront_pixels", C.c_uint64),
+                ("p50_seconds", C.c_double),
                 ("p99_seconds", C.c_double), ("total_seconds", C.c_double), ("trials", C.c_uint32)]
 
 
@@ -231,7 +232,8 @@ def lib() -> C.CDLL:
             "vg_set_cache": (i32, [vp, vp, C.c_float, u32, u32, u32]),
             "vg_cache_time": (i32, [vp, vp, _S, u32, C.POINTER(f64)]),
             "vg_batch_render": (i32, [vp, vp, _S, vp, C.POINTER(f64), C.POINTER(C.c_int)]),
-            "vg_set_batch_options": (i32, [vp, i32, i32]),
+            "vg_set_batch_options": (i32, [vp, i32, i32, C.c_uint64]),
+            "vg_batch_kernel_info": (i32, [vp, vp]),
             "vg_batch_tune": (i32, [vp, vp, _S, C.POINTER(_BatchTune)]),
             "vg_accum_cache_stats": (i32, [vp, C.POINTER(CacheStats)]),
         }
@@ -304,8 +306,13 @@ class Context:
         _check(lib().vg_batch_render(self._h, arr, len(requests), out, C.byref(total), C.byref(replayed)))
         return BatchOutcome(list(out), total.value, bool(replayed.value))
 
-    def set_batch_options(self, blocks_per_sm: int = 0, order: int = 0) -> None:
-        _check(lib().vg_set_batch_options(self._h, blocks_per_sm, order))
+    def batch_kernel_info(self) -> dict:
+        v = (C.c_int * 5)()
+        _check(lib().vg_batch_kernel_info(self._h, v))
+        return dict(zip(("blocks_per_sm", "registers", "local_bytes", "static_smem", "cuda_status"), list(v)))
+
+    def set_batch_options(self, blocks_per_sm: int = 0, order: int = 0, wavefront_pixels: int = 512 * 512) -> None:
+        _check(lib().vg_set_batch_options(self._h, blocks_per_sm, order, wavefront_pixels))
 
     def batch_tune(self, requests) -> dict:
         """vg_batch_tune: picks the batch kernel's CTAs per SM and item order for these requests."""
@@ -317,7 +324,8 @@ class Context:
             arr[i].cache = q.cache._h if q.cache is not None else None
         t = _BatchTune()
         _check(lib().vg_batch_tune(self._h, arr, len(requests), C.byref(t)))
-        return {"blocks_per_sm": t.blocks_per_sm, "order": t.order, "p50_seconds": t.p50_seconds,
+        return {"blocks_per_sm": t.blocks_per_sm, "order": t.order, "wavefront_pixels": t.wavefront_pixels,
+                "p50_seconds": t.p50_seconds,
                 "p99_seconds": t.p99_seconds, "total_seconds": t.total_seconds, "trials": t.trials}
 
     def close(self):

@@ -64,8 +64,8 @@ std::vector<size_t> order_of(const VgBatchRequest* reqs, size_t n, int order)
     return idx;
 }
 
-int batch_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int blocks_per_sm, int order, VgBatchResult* out,
-              double* total_seconds, int* replayed)
+int batch_kernel_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int blocks_per_sm, int order,
+                     VgBatchResult* out, double* total_seconds, int* replayed)
 {
     if (!ctx || !reqs || n == 0 || n > 65536)
         return fail(VG_ERR_INVALID, "empty or oversized batch");
@@ -149,7 +149,9 @@ int batch_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int blocks_p
         sig.insert(sig.end(), {(uint64_t)(uintptr_t)r, (uint64_t)(uintptr_t)a, q.samples, (uint64_t)(uintptr_t)q.cache,
                                q.cache ? ((uint64_t)r->cache_steps << 32 | r->cache_batch) : 0});
     }
-    int bps = blocks_per_sm > 0 ? std::min(blocks_per_sm, vgx::batch_blocks_per_sm()) : vgx::batch_blocks_per_sm();
+    // A persistent kernel over a work counter: CTAs beyond what fits start when others leave, so a
+    // larger request is safe.
+    int bps = blocks_per_sm > 0 ? std::min(blocks_per_sm, 8) : vgx::batch_blocks_per_sm();
     sig.insert(sig.end(), {(uint64_t)bps, (uint64_t)order});
     if (b->reqs.bytes < n * sizeof(vgb::BatchReq) || b->done.bytes < n * sizeof(vgb::BatchDone)) {
         if ((st = alloc(b->reqs, n * sizeof(vgb::BatchReq), s, false)) != VG_OK ||
@@ -237,6 +239,69 @@ int batch_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int blocks_p
     return VG_OK;
 }
 
+// The hybrid schedule: requests below `big` pixels share the persistent launch; the rest follow
+// one at a time on the streaming wavefront (or the cache integrator), shortest first.
+int batch_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int blocks_per_sm, int order, uint64_t big,
+              VgBatchResult* out, double* total_seconds, int* replayed)
+{
+    if (!ctx || !reqs || n == 0 || n > 65536)
+        return fail(VG_ERR_INVALID, "empty or oversized batch");
+    std::vector<size_t> small, large;
+    for (size_t i = 0; i < n; i++) {
+        if (!reqs[i].renderer || !reqs[i].accum)
+            return fail(VG_ERR_INVALID, "batch request " + std::to_string(i) + " is malformed");
+        uint64_t px = (uint64_t)reqs[i].accum->width * reqs[i].accum->height;
+        (px >= big ? large : small).push_back(i);
+    }
+    for (size_t i : large) {
+        const VgBatchRequest& q = reqs[i];
+        if (q.renderer->ctx != ctx || q.accum->owner != q.renderer || q.samples == 0)
+            return fail(VG_ERR_INVALID, "batch request " + std::to_string(i) + " is malformed");
+        if (!batch_compatible(q.renderer, q.accum))
+            return fail(VG_ERR_UNSUPPORTED, "batch request " + std::to_string(i) +
+                                                " uses adaptive sampling, ReSTIR or the lighting split");
+        if (q.cache && q.cache->ctx != ctx)
+            return fail(VG_ERR_INVALID, "batch request " + std::to_string(i) + " has a cache of another context");
+    }
+    double t = 0.0;
+    int st, rep = 0;
+    if (!small.empty()) {
+        std::vector<VgBatchRequest> sr;
+        for (size_t i : small)
+            sr.push_back(reqs[i]);
+        std::vector<VgBatchResult> so(sr.size());
+        if ((st = batch_kernel_run(ctx, sr.data(), sr.size(), blocks_per_sm, order, so.data(), &t, &rep)) != VG_OK)
+            return st;
+        for (size_t j = 0; j < small.size(); j++)
+            if (out)
+                out[small[j]].seconds = so[j].seconds;
+    }
+    auto cost = [&](size_t i) { return (double)reqs[i].accum->width * reqs[i].accum->height * reqs[i].samples; };
+    std::stable_sort(large.begin(), large.end(), [&](size_t a, size_t b) { return cost(a) < cost(b); });
+    for (size_t i : large) {
+        const VgBatchRequest& q = reqs[i];
+        VgRenderer* r = q.renderer;
+        int integ = r->integrator;
+        VgCache* cache = r->cache;
+        r->integrator = VG_WAVEFRONT;
+        r->cache = q.cache;
+        double g0 = q.accum->gpu_seconds;
+        st = vg_accumulate(r, q.accum, q.samples);
+        r->integrator = integ;
+        r->cache = cache;
+        if (st != VG_OK)
+            return st;
+        t += q.accum->gpu_seconds - g0;
+        if (out)
+            out[i].seconds = t;
+    }
+    if (total_seconds)
+        *total_seconds = t;
+    if (replayed)
+        *replayed = rep;
+    return VG_OK;
+}
+
 } // namespace
 
 extern "C" {
@@ -246,16 +311,25 @@ int vg_batch_render(VgContext* ctx, const VgBatchRequest* requests, size_t n, Vg
 {
     if (!ctx)
         return fail(VG_ERR_INVALID, "null context");
-    return batch_run(ctx, requests, n, ctx->batch_blocks_per_sm, ctx->batch_order, out, total_seconds,
-                     graph_replayed);
+    return batch_run(ctx, requests, n, ctx->batch_blocks_per_sm, ctx->batch_order, ctx->batch_wavefront_pixels, out,
+                     total_seconds, graph_replayed);
 }
 
-int vg_set_batch_options(VgContext* ctx, int blocks_per_sm, int order)
+int vg_batch_kernel_info(VgContext* ctx, int out[5])
+{
+    if (!ctx || !out)
+        return fail(VG_ERR_INVALID, "null argument");
+    out[0] = vgx::batch_kernel_info(&out[1], &out[2], &out[3], &out[4]);
+    return VG_OK;
+}
+
+int vg_set_batch_options(VgContext* ctx, int blocks_per_sm, int order, uint64_t wavefront_pixels)
 {
     if (!ctx || blocks_per_sm < 0 || order < VG_BATCH_SHORTEST_FIRST || order > VG_BATCH_LONGEST_FIRST)
         return fail(VG_ERR_INVALID, "batch options out of range");
     ctx->batch_blocks_per_sm = blocks_per_sm;
     ctx->batch_order = order;
+    ctx->batch_wavefront_pixels = wavefront_pixels;
     return VG_OK;
 }
 
@@ -282,17 +356,21 @@ int vg_batch_tune(VgContext* ctx, const VgBatchRequest* requests, size_t n, VgBa
         trial[i].accum = scratch[i];
     }
     int best_b = 0, best_o = 0;
+    uint64_t best_px = ctx->batch_wavefront_pixels;
     double best = 1e300;
+    const uint64_t thresholds[] = {256ull * 256, 512ull * 512, 1024ull * 1024, ~0ull};
     VgBatchTune res{};
     uint32_t trials = 0;
     std::vector<VgBatchResult> times(n);
     int max_b = vgx::batch_blocks_per_sm();
-    for (int o = VG_BATCH_SHORTEST_FIRST; o <= VG_BATCH_LONGEST_FIRST && st == VG_OK; o++) {
-        for (int bps = 1; bps <= max_b && st == VG_OK; bps++) {
+    // As given is the caller's order: left out. CTA counts: the two largest that fit.
+    for (uint64_t big : thresholds)
+    for (int o : {(int)VG_BATCH_SHORTEST_FIRST, (int)VG_BATCH_LONGEST_FIRST}) {
+        for (int bps = std::max(1, max_b - 1); bps <= max_b && st == VG_OK; bps++) {
             double total = 0.0;
             // One run to capture the graph, one timed replay.
             for (int rep = 0; rep < 2 && st == VG_OK; rep++)
-                st = batch_run(ctx, trial.data(), n, bps, o, times.data(), &total, nullptr);
+                st = batch_run(ctx, trial.data(), n, bps, o, big, times.data(), &total, nullptr);
             if (st != VG_OK)
                 break;
             trials++;
@@ -301,11 +379,12 @@ int vg_batch_tune(VgContext* ctx, const VgBatchRequest* requests, size_t n, VgBa
                 lat[i] = times[i].seconds;
             std::sort(lat.begin(), lat.end());
             double p50 = lat[(n - 1) / 2], p99 = lat[std::min(n - 1, (size_t)std::ceil(0.99 * (double)n) - 1)];
-            double objective = p50 + total;
+            double objective = p50 + p99;
             if (objective < best) {
                 best = objective;
                 best_b = bps;
                 best_o = o;
+                best_px = big;
                 res.p50_seconds = p50;
                 res.p99_seconds = p99;
                 res.total_seconds = total;
@@ -319,8 +398,10 @@ int vg_batch_tune(VgContext* ctx, const VgBatchRequest* requests, size_t n, VgBa
         return st;
     ctx->batch_blocks_per_sm = best_b;
     ctx->batch_order = best_o;
+    ctx->batch_wavefront_pixels = best_px;
     res.blocks_per_sm = best_b;
     res.order = best_o;
+    res.wavefront_pixels = best_px;
     res.trials = trials;
     *out = res;
     return VG_OK;

@@ -118,6 +118,7 @@ struct VgContext {
     BatchState* batch = nullptr;
     int batch_blocks_per_sm = 0; // 0: as many as fit (vg_batch_tune chooses)
     int batch_order = 0;         // VgBatchOrder
+    uint64_t batch_wavefront_pixels = 512 * 512; // requests at least this large run on the wavefront
     ~VgContext();
 };
 

@@ -6,6 +6,8 @@
 // the radiance cache and evaluates the cache for its 128 pixels in the same CTA: the tile is one
 // M = 128 tcgen05 MMA tile, so the queries never leave the SM (the fused form of nrc_encode +
 // nrc_infer).
+#include <algorithm>
+
 #include "batch.h"
 #include "launch_batch.h"
 #include "nrc_device.cuh"
@@ -20,6 +22,11 @@ using namespace vgnd;
 using namespace vgb;
 
 constexpr uint32_t BATCH_SMEM = IMG_FWD_BYTES + 16384 + 1024;
+
+// Register cap of the batch kernel: at least this many 128-thread CTAs per SM.
+#ifndef VG_BATCH_MIN_BLOCKS
+#define VG_BATCH_MIN_BLOCKS 3
+#endif
 constexpr uint32_t MAX_TRAIN_VERTICES = 16;
 static_assert(sizeof(BatchReq) % 16 == 0, "BatchReq is copied to shared memory in 16-byte words");
 
@@ -133,7 +140,7 @@ static __device__ __forceinline__ bool cache_sample(const BatchReq& R, uint32_t 
     return false;
 }
 
-__global__ void __launch_bounds__(128) batch_render(const BatchReq* __restrict__ reqs, uint32_t nreq, uint32_t items,
+__global__ void __launch_bounds__(128, VG_BATCH_MIN_BLOCKS) batch_render(const BatchReq* __restrict__ reqs, uint32_t nreq, uint32_t items,
                                                     uint32_t* next, BatchDone* done, uint32_t* err)
 {
     extern __shared__ uint8_t smem_raw[];
@@ -275,16 +282,45 @@ namespace vgx {
 
 using namespace vgbk;
 
+static cudaError_t g_occ_err = cudaSuccess;
+
 int batch_blocks_per_sm()
 {
     static int n = -1;
     if (n < 0) {
-        cudaFuncSetAttribute(batch_render, cudaFuncAttributeMaxDynamicSharedMemorySize, BATCH_SMEM);
-        int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batch_render, 128, BATCH_SMEM);
-        n = b > 0 ? b : 1;
+        cudaError_t e = cudaFuncSetAttribute(batch_render, cudaFuncAttributeMaxDynamicSharedMemorySize, BATCH_SMEM);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(batch_render, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     cudaSharedmemCarveoutMaxShared);
+        // From the kernel's own resource use: registers (allocated per warp in units of 256) and
+        // shared memory (its static and dynamic bytes plus the driver's 1 KB per block).
+        cudaFuncAttributes a{};
+        if (e == cudaSuccess)
+            e = cudaFuncGetAttributes(&a, batch_render);
+        int dev = 0, regs_sm = 65536, smem_sm = 233472;
+        if (e == cudaSuccess && cudaGetDevice(&dev) == cudaSuccess) {
+            cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+            cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        }
+        g_occ_err = e;
+        int warp_regs = ((a.numRegs * 32 + 255) / 256) * 256;
+        int by_regs = a.numRegs > 0 ? regs_sm / (warp_regs * 4) : 1;
+        int by_smem = smem_sm / (int)(BATCH_SMEM + a.sharedSizeBytes + 1024);
+        n = std::max(1, std::min(std::min(by_regs, by_smem), 16));
     }
     return n;
+}
+
+int batch_kernel_info(int* regs, int* local_bytes, int* static_smem, int* error)
+{
+    int b = batch_blocks_per_sm();
+    cudaFuncAttributes a{};
+    cudaError_t e = cudaFuncGetAttributes(&a, batch_render);
+    *regs = a.numRegs;
+    *local_bytes = (int)a.localSizeBytes;
+    *static_smem = (int)a.sharedSizeBytes;
+    *error = g_occ_err != cudaSuccess ? (int)g_occ_err : (int)e;
+    return b;
 }
 
 cudaError_t launch_batch(int blocks, cudaStream_t s, const vgb::BatchReq* reqs, uint32_t nreq, uint32_t items,

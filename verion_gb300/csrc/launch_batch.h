@@ -8,6 +8,8 @@ namespace vgx {
 
 // Resident batch CTAs per SM (occupancy of the batch kernel with its shared memory).
 int batch_blocks_per_sm();
+// Resource use of the batch kernel (registers, local and static shared bytes, first CUDA error).
+int batch_kernel_info(int* regs, int* local_bytes, int* static_smem, int* error);
 // Writes the start time to *t0, then runs `items` work items of `nreq` requests (sorted by item_begin).
 cudaError_t launch_batch(int blocks, cudaStream_t s, const vgb::BatchReq* reqs, uint32_t nreq, uint32_t items,
                          uint32_t* next, vgb::BatchDone* done, uint32_t* err, unsigned long long* t0);
