@@ -370,7 +370,8 @@ def batch_report(ctx, spp_scale, side_range=(256, 2048), spp_range=(16, 256)):
     depth 16, every second request with a radiance cache. One batch (autotuned, graph replayed)
     against the same requests rendered one at a time with accumulate (wavefront for plain
     requests, the cache integrator for cached ones), shortest first; latency = device time from the
-    start until the request's last tile."""
+    start until the request's last tile. The batch is first autotuned (vg_batch_tune) at a quarter
+    of the sample counts."""
     from verion_gb300 import pack, scenes
     from verion_gb300.backend import BatchRequest, Cache, Integrator, Renderer
 
@@ -405,7 +406,7 @@ def batch_report(ctx, spp_scale, side_range=(256, 2048), spp_range=(16, 256)):
 
     paths = float(sum(side * side * spp for side, spp, _, _ in spec))
     reqs = requests()
-    tune_reqs = [BatchRequest(q.renderer, q.accum, 1, q.cache) for q in reqs]
+    tune_reqs = [BatchRequest(q.renderer, q.accum, max(1, q.samples // 4), q.cache) for q in reqs]
     tuned = ctx.batch_tune(tune_reqs)
     ctx.batch_render(reqs)  # captures the graph
     out = ctx.batch_render(reqs)  # replays it
