@@ -205,6 +205,32 @@ int vg_set_deferred_shadows(VgRenderer* r, int on);
 /* Streaming mode: the extend and shadow stages refill a warp's idle lanes with queued rays
  * (default on) or give each warp 32 rays at a time (off). Same results either way. */
 int vg_set_dynamic_fetch(VgRenderer* r, int on);
+/* Streaming mode: capture `waves` waves (an even count, 0 = off) of the bounce loop in a CUDA graph
+ * once per call and replay it until the slots drain (without stage timing), instead of launching
+ * every wave's kernels from the host. Same sums. */
+int vg_set_wavefront_graph(VgRenderer* r, uint32_t waves);
+/* Rebuilds the BVH8 with another SAH node-visit cost (relative to a triangle test; default 1):
+ * smaller values give deeper trees with smaller leaves. `packed` must be the renderer's scene
+ * tables (pack::pack of the same scene). Hits are the same with any BVH. */
+int vg_set_bvh_traversal_cost(VgRenderer* r, const VgPacked* packed, float cost);
+
+/* Autotuner of the streaming wavefront (no reference counterpart): on scratch accumulations of
+ * width x height and `samples` per trial, a coordinate-descent pass over dynamic fetch, deferred
+ * shadows, the tail threshold (0, 8192, 32768, 131072), the wave graph (0 or 8 waves) and, when
+ * `packed` is given, the BVH8's SAH traversal cost (0.25, 0.5, 1, 2); a change is kept when it is more
+ * than 1% faster. Leaves the renderer on the streaming wavefront with the best setting. All of
+ * these settings give the same sums. */
+typedef struct VgTuneResult {
+    int dynamic_fetch;
+    int deferred_shadows;
+    uint32_t stream_tail;
+    uint32_t graph_waves;
+    float bvh_traversal_cost;
+    double mpaths_before, mpaths_after; /* camera paths per second, first and best trial */
+    uint32_t trials;
+} VgTuneResult;
+int vg_autotune(VgRenderer* r, const VgPacked* packed, uint32_t width, uint32_t height, uint32_t samples,
+                VgTuneResult* out);
 /* With stage timing: seconds of the last call's tail launch (0 if none ran). */
 double vg_accum_tail_seconds(const VgAccum* acc);
 /* Streaming mode: waves (extend + shade pairs) issued by the last vg_accumulate. */

@@ -108,6 +108,12 @@ class CacheStats(C.Structure):
                 ("path_seconds", C.c_double), ("infer_seconds", C.c_double), ("train_seconds", C.c_double)]
 
 
+class _TuneResult(C.Structure):
+    _fields_ = [("dynamic_fetch", C.c_int), ("deferred_shadows", C.c_int), ("stream_tail", C.c_uint32),
+                ("graph_waves", C.c_uint32), ("bvh_traversal_cost", C.c_float), ("mpaths_before", C.c_double),
+                ("mpaths_after", C.c_double), ("trials", C.c_uint32)]
+
+
 class _BatchRequest(C.Structure):
     _fields_ = [("renderer", C.c_void_p), ("accum", C.c_void_p), ("samples", C.c_uint32), ("cache", C.c_void_p)]
 
@@ -195,6 +201,9 @@ def lib() -> C.CDLL:
             "vg_accum_tail_seconds": (f64, [vp]),
             "vg_set_deferred_shadows": (i32, [vp, i32]),
             "vg_set_dynamic_fetch": (i32, [vp, i32]),
+            "vg_set_wavefront_graph": (i32, [vp, u32]),
+            "vg_set_bvh_traversal_cost": (i32, [vp, C.POINTER(_Packed), C.c_float]),
+            "vg_autotune": (i32, [vp, C.POINTER(_Packed), u32, u32, u32, C.POINTER(_TuneResult)]),
             "vg_accum_traversal_stats": (i32, [vp, C.POINTER(C.c_uint64)]),
             "vg_set_accum_precision": (i32, [vp, i32]),
             "vg_accum_create": (i32, [vp, u32, u32, i32, C.POINTER(vp)]),
@@ -562,6 +571,25 @@ class Renderer:
 
     def set_wavefront_mode(self, mode: "WavefrontMode") -> None:
         _check(lib().vg_set_wavefront_mode(self._h, int(mode)))
+
+    def set_bvh_traversal_cost(self, cost: float) -> None:
+        """Rebuilds the BVH8 with another SAH node-visit cost (needs the renderer's packed tables)."""
+        pk = self._struct(self.packed)
+        _check(lib().vg_set_bvh_traversal_cost(self._h, C.byref(pk), cost))
+        self._keep = []
+
+    def autotune(self, width: int, height: int, samples: int, bvh: bool = True) -> dict:
+        """vg_autotune: picks the streaming-wavefront settings (and, with `bvh`, the BVH8's SAH cost)."""
+        pk = self._struct(self.packed) if bvh else None
+        t = _TuneResult()
+        _check(lib().vg_autotune(self._h, C.byref(pk) if pk is not None else None, width, height, samples,
+                                 C.byref(t)))
+        self._keep = []
+        return {k: getattr(t, k) for k, _ in _TuneResult._fields_}
+
+    def set_wavefront_graph(self, waves: int) -> None:
+        """Streaming mode: replay a captured CUDA graph of `waves` waves (even; 0 = off)."""
+        _check(lib().vg_set_wavefront_graph(self._h, waves))
 
     def set_dynamic_fetch(self, on: bool) -> None:
         _check(lib().vg_set_dynamic_fetch(self._h, int(on)))

@@ -59,11 +59,10 @@ struct BNode {
 
 constexpr int BINS = 32;
 constexpr int MEDIAN_DEPTH = 40;   // below this depth splits fall back to the object median
-constexpr float C_TRAV = 1.0f;     // SAH cost of one node visit, relative to one triangle test
-
 struct Builder {
     const float* verts;
     uint32_t n;
+    float c_trav = 1.0f; // SAH cost of one node visit, relative to one triangle test
     std::vector<Box> tbox;
     std::vector<float> cent; // 3 per triangle
     std::vector<uint32_t> order;
@@ -143,7 +142,7 @@ struct Builder {
         }
         float pa = box.area();
         float leaf_cost = (float)cnt;
-        float split_cost = pa > 0.0f ? C_TRAV + best_cost / pa : INFINITY;
+        float split_cost = pa > 0.0f ? c_trav + best_cost / pa : INFINITY;
         if (cnt <= bvh8::MAX_LEAF_TRIS && (best_axis < 0 || leaf_cost <= split_cost))
             return begin;
         if (best_axis < 0)
@@ -227,7 +226,7 @@ float pow2(int e) { return u2f((uint32_t)(e + 127) << 23); }
 } // namespace
 
 bool build_bvh8(const float* verts, const uint32_t* inst, const uint32_t* prim, uint32_t n, Bvh8Host& out,
-                std::string& err)
+                std::string& err, float traversal_cost)
 {
     auto t0 = std::chrono::steady_clock::now();
     for (size_t i = 0; i < 9 * (size_t)n; i++) {
@@ -237,6 +236,7 @@ bool build_bvh8(const float* verts, const uint32_t* inst, const uint32_t* prim, 
         }
     }
     Builder b;
+    b.c_trav = traversal_cost;
     b.verts = verts;
     b.n = n;
     b.build();

@@ -18,6 +18,7 @@ struct Bvh8Host {
 
 // `verts`: 9 floats (three world-space vertices) per triangle; `inst`, `prim`: the instance and
 // the primitive index within its mesh per triangle. The global index of a triangle (its position
-// in `verts`) breaks ties between hits at equal distance.
+// in `verts`) breaks ties between hits at equal distance. `traversal_cost`: the SAH cost of a node
+// visit relative to a triangle test (smaller: deeper trees with smaller leaves).
 bool build_bvh8(const float* verts, const uint32_t* inst, const uint32_t* prim, uint32_t n, Bvh8Host& out,
-                std::string& err);
+                std::string& err, float traversal_cost = 1.0f);

@@ -69,7 +69,7 @@ int build_world_bvh(VgRenderer* r, const VgPacked* pk, Bvh8Host& bvh)
         hi[i % 3] = std::max(hi[i % 3], verts[i]);
     }
     std::string err;
-    if (!build_bvh8(verts.data(), tinst.data(), tprim.data(), (uint32_t)total, bvh, err))
+    if (!build_bvh8(verts.data(), tinst.data(), tprim.data(), (uint32_t)total, bvh, err, r->bvh_traversal_cost))
         return fail(VG_ERR_SCENE, err);
     for (int k = 0; k < 3; k++) {
         r->bounds_lo[k] = lo[k];
@@ -414,6 +414,31 @@ int vg_renderer_update(VgRenderer* r, const VgPacked* pk, const VgUpdatePlan* pl
     return VG_OK;
 }
 
+int vg_set_bvh_traversal_cost(VgRenderer* r, const VgPacked* pk, float cost)
+{
+    if (!r || !pk)
+        return fail(VG_ERR_INVALID, "null argument");
+    if (!(cost > 0.0f && cost <= 16.0f))
+        return fail(VG_ERR_INVALID, "SAH traversal cost out of range");
+    int st = validate(pk);
+    if (st != VG_OK)
+        return st;
+    if (pk->instance_count != r->instance_count)
+        return fail(VG_ERR_SCENE, "the tables are not this renderer's scene");
+    float old = r->bvh_traversal_cost;
+    r->bvh_traversal_cost = cost;
+    Bvh8Host bvh;
+    if ((st = build_world_bvh(r, pk, bvh)) != VG_OK || (st = upload(r->ctx, r->nodes, bvh.nodes.data(), bvh.nodes.size() * 4)) != VG_OK ||
+        (st = upload(r->ctx, r->tris, bvh.tris.data(), bvh.tris.size() * 4)) != VG_OK) {
+        r->bvh_traversal_cost = old;
+        return st;
+    }
+    VG_CHECK(cudaStreamSynchronize(r->ctx->stream), "BVH upload");
+    r->ds.nodes = (const uint4*)r->nodes.p;
+    r->ds.tris = (const float4*)r->tris.p;
+    return VG_OK;
+}
+
 int vg_renderer_bvh_info(const VgRenderer* r, VgBvhInfo* out)
 {
     if (!r || !out)
@@ -475,6 +500,14 @@ int vg_set_stream_tail(VgRenderer* r, uint32_t threshold)
 }
 
 double vg_accum_tail_seconds(const VgAccum* acc) { return acc ? acc->tail_ms * 1e-3 : 0.0; }
+
+int vg_set_wavefront_graph(VgRenderer* r, uint32_t waves)
+{
+    if (!r || (waves & 1u) || waves > 64)
+        return fail(VG_ERR_INVALID, "graph waves must be 0 or an even count up to 64");
+    r->graph_waves = waves;
+    return VG_OK;
+}
 
 int vg_set_dynamic_fetch(VgRenderer* r, int on)
 {
@@ -743,6 +776,80 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
                 e = pool.get();
             bool done = false;
             uint64_t wave = 0;
+            if (r->graph_waves > 0 && !timed) {
+                // Captured chunks of graph_waves waves (even, so the queue parity of every wave in a
+                // replay matches its place in the sequence), each ending with the live count.
+                uint32_t K = r->graph_waves;
+                VG_CHECK(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed), "graph capture");
+                cudaError_t ce = cudaSuccess;
+                for (uint32_t i = 0; i < K && ce == cudaSuccess; i++) {
+                    ce = r->dynamic_fetch ? vgx::launch_stream_extend_dyn(r->traversal_stats, eb, s, c, w, i)
+                                          : vgx::launch_stream_extend(r->traversal_stats, eb, s, c, w, i);
+                    if (ce == cudaSuccess && deferred) {
+                        ce = vgx::launch_stream_shade_deferred(v.f64, dsb, s, c, w, i);
+                        if (ce == cudaSuccess && r->dynamic_fetch && r->ds.shadow_any) {
+                            ce = vgx::launch_stream_shadow_trace(shb, s, c, w, i);
+                            if (ce == cudaSuccess)
+                                ce = vgx::launch_stream_finish(v.f64, shb, s, c, w, i);
+                        } else if (ce == cudaSuccess)
+                            ce = vgx::launch_stream_shadow(v.f64, shb, s, c, w, i);
+                    } else if (ce == cudaSuccess)
+                        ce = vgx::launch_stream_shade(v, ssb, s, c, w, i);
+                }
+                if (ce == cudaSuccess)
+                    ce = cudaMemcpyAsync(&ring[0], (uint32_t*)acc->counts.p + (K & 1u), 4, cudaMemcpyDeviceToHost, s);
+                cudaGraph_t g = nullptr;
+                cudaError_t ee = cudaStreamEndCapture(s, &g);
+                if (ce != cudaSuccess || ee != cudaSuccess) {
+                    if (g)
+                        cudaGraphDestroy(g);
+                    return cuda_fail(ce != cudaSuccess ? ce : ee, "wave graph capture");
+                }
+                cudaGraphExec_t ge = nullptr;
+                ce = cudaGraphInstantiate(&ge, g, 0);
+                cudaGraphDestroy(g);
+                if (ce != cudaSuccess)
+                    return cuda_fail(ce, "wave graph instantiation");
+                uint32_t per_wave = deferred ? (r->dynamic_fetch && r->ds.shadow_any ? 4 : 3) : 2;
+                uint64_t max_rep = (max_waves + K - 1) / K + 2;
+                uint64_t rep = 0;
+                for (; rep < max_rep && !done; rep++) {
+                    ce = cudaGraphLaunch(ge, s);
+                    if (ce == cudaSuccess)
+                        ce = cudaEventRecord(ring_ev[rep & 1u], s);
+                    if (ce != cudaSuccess) {
+                        cudaGraphExecDestroy(ge);
+                        return cuda_fail(ce, "wave graph launch");
+                    }
+                    acc->launches += (uint64_t)K * per_wave;
+                    if (rep >= 1) {
+                        if ((st = wait_event(ring_ev[(rep - 1) & 1u])) != VG_OK) {
+                            cudaGraphExecDestroy(ge);
+                            return st;
+                        }
+                        // The count of the last replay that finished (a later one may have overwritten
+                        // it with a smaller count: live counts never grow).
+                        uint32_t live = ring[0];
+                        acc->wave_live.push_back(live);
+                        done = live == 0;
+                        if (!done && live <= r->tail_threshold) {
+                            ce = vgx::launch_stream_tail(v, live, s, c, w, (uint32_t)((rep + 1) * K));
+                            if (ce != cudaSuccess) {
+                                cudaGraphExecDestroy(ge);
+                                return cuda_fail(ce, "tail launch");
+                            }
+                            acc->launches++;
+                            done = true;
+                        }
+                    }
+                }
+                wave = rep * K;
+                VG_CHECK(cudaStreamSynchronize(s), "waves");
+                cudaGraphExecDestroy(ge);
+                if (!done && ring[0] != 0)
+                    return fail(VG_ERR_KERNEL, "streaming wavefront did not drain within its wave bound");
+                done = true;
+            }
             for (; wave < max_waves && !done; wave++) {
                 cudaEvent_t a = nullptr, m = nullptr, b = nullptr;
                 if (timed) {
@@ -1020,6 +1127,115 @@ static void camera_record(const VgRenderer* r, uint32_t w, uint32_t h, float* re
     rec[1] = (float)h;
     rec[16] = r->view.shift[0];
     rec[17] = r->view.shift[1];
+}
+
+// One autotuner trial: a warm-up accumulate, then the device time of a second one on a scratch
+// accumulation; camera paths per second in millions.
+static double tune_trial(VgRenderer* r, uint32_t w, uint32_t h, uint32_t spp, int* st)
+{
+    VgAccum* a = nullptr;
+    if ((*st = vg_accum_create(r, w, h, 0, &a)) != VG_OK)
+        return 0.0;
+    double m = 0.0;
+    if ((*st = vg_accumulate(r, a, spp)) == VG_OK) {
+        double g0 = a->gpu_seconds;
+        if ((*st = vg_accumulate(r, a, spp)) == VG_OK)
+            m = (double)w * h * spp / std::max(a->gpu_seconds - g0, 1e-9) / 1e6;
+    }
+    vg_accum_destroy(a);
+    return m;
+}
+
+int vg_autotune(VgRenderer* r, const VgPacked* pk, uint32_t width, uint32_t height, uint32_t samples, VgTuneResult* out)
+{
+    if (!r || !out || width == 0 || height == 0 || samples == 0)
+        return fail(VG_ERR_INVALID, "null argument or empty trial");
+    memset(out, 0, sizeof(*out));
+    // Trials run the streaming wavefront without adaptive sampling or stage timing; the renderer is
+    // left on the streaming wavefront with the best setting found.
+    bool adaptive = r->adaptive, timing = r->stage_timing;
+    r->adaptive = false;
+    r->stage_timing = false;
+    r->integrator = VG_WAVEFRONT;
+    r->wavefront_mode = VG_WAVEFRONT_STREAMING;
+    int st = VG_OK;
+    uint32_t trials = 0;
+    double best = tune_trial(r, width, height, samples, &st);
+    trials++;
+    out->mpaths_before = best;
+    // Coordinate descent: one pass over the settings, a change kept when it gains over 1%.
+    auto try_setting = [&](auto apply, auto values) {
+        for (auto v : values) {
+            if (st != VG_OK)
+                return;
+            auto keep = apply(v, true);
+            double m = tune_trial(r, width, height, samples, &st);
+            trials++;
+            if (st == VG_OK && m > best * 1.01)
+                best = m;
+            else
+                apply(keep, false);
+        }
+    };
+    try_setting(
+        [&](bool v, bool) {
+            bool o = r->dynamic_fetch;
+            r->dynamic_fetch = v;
+            return o;
+        },
+        std::vector<bool>{!r->dynamic_fetch});
+    try_setting(
+        [&](bool v, bool) {
+            bool o = r->defer_shadows;
+            r->defer_shadows = v;
+            return o;
+        },
+        std::vector<bool>{!r->defer_shadows});
+    std::vector<uint32_t> tails;
+    for (uint32_t t : {0u, 8192u, 32768u, 131072u})
+        if (t != r->tail_threshold)
+            tails.push_back(t);
+    try_setting(
+        [&](uint32_t v, bool) {
+            uint32_t o = r->tail_threshold;
+            r->tail_threshold = v;
+            return o;
+        },
+        tails);
+    try_setting(
+        [&](uint32_t v, bool) {
+            uint32_t o = r->graph_waves;
+            r->graph_waves = v;
+            return o;
+        },
+        std::vector<uint32_t>{r->graph_waves == 0 ? 8u : 0u});
+    if (pk && st == VG_OK) {
+        std::vector<float> costs;
+        for (float c : {0.25f, 0.5f, 2.0f})
+            if (c != r->bvh_traversal_cost)
+                costs.push_back(c);
+        try_setting(
+            [&](float v, bool) {
+                float o = r->bvh_traversal_cost;
+                int s2 = vg_set_bvh_traversal_cost(r, pk, v);
+                if (s2 != VG_OK)
+                    st = s2;
+                return o;
+            },
+            costs);
+    }
+    r->adaptive = adaptive;
+    r->stage_timing = timing;
+    if (st != VG_OK)
+        return st;
+    out->dynamic_fetch = r->dynamic_fetch;
+    out->deferred_shadows = r->defer_shadows;
+    out->stream_tail = r->tail_threshold;
+    out->graph_waves = r->graph_waves;
+    out->bvh_traversal_cost = r->bvh_traversal_cost;
+    out->mpaths_after = best;
+    out->trials = trials;
+    return VG_OK;
 }
 
 int vg_render_normals(VgRenderer* r, uint32_t width, uint32_t height, float* out)
