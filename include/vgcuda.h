@@ -209,7 +209,7 @@ int vg_set_dynamic_fetch(VgRenderer* r, int on);
  * once per call and replay it until the slots drain (without stage timing), instead of launching
  * every wave's kernels from the host. Same sums. */
 int vg_set_wavefront_graph(VgRenderer* r, uint32_t waves);
-/* Rebuilds the BVH8 with another SAH node-visit cost (relative to a triangle test; default 1):
+/* Rebuilds the BVH8 with another SAH node-visit cost (relative to a triangle test; default 0.5):
  * smaller values give deeper trees with smaller leaves. `packed` must be the renderer's scene
  * tables (pack::pack of the same scene). Hits are the same with any BVH. */
 int vg_set_bvh_traversal_cost(VgRenderer* r, const VgPacked* packed, float cost);

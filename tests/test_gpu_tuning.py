@@ -50,7 +50,7 @@ def test_bvh_traversal_cost_keeps_the_hits(gpu_ctx):
     r = wave_renderer(gpu_ctx, p)
     want = render(r, 64, 36, 2)
     nodes = r.bvh_info().wide_nodes
-    r.set_bvh_traversal_cost(0.5)
+    r.set_bvh_traversal_cost(2.0)
     assert r.bvh_info().wide_nodes != nodes
     assert np.array_equal(render(r, 64, 36, 2), want)
 

@@ -21,4 +21,4 @@ struct Bvh8Host {
 // in `verts`) breaks ties between hits at equal distance. `traversal_cost`: the SAH cost of a node
 // visit relative to a triangle test (smaller: deeper trees with smaller leaves).
 bool build_bvh8(const float* verts, const uint32_t* inst, const uint32_t* prim, uint32_t n, Bvh8Host& out,
-                std::string& err, float traversal_cost = 1.0f);
+                std::string& err, float traversal_cost = 0.5f);

@@ -161,7 +161,7 @@ struct VgRenderer {
     bool defer_shadows = true; // streaming: shadow rays of the light sample in their own stage
     bool dynamic_fetch = true; // streaming: traversal stages refill idle lanes from the queue
     uint32_t graph_waves = 0;  // streaming: waves per captured CUDA graph (0: launched one by one)
-    float bvh_traversal_cost = 1.0f; // SAH node-visit cost the BVH8 was built with
+    float bvh_traversal_cost = 0.5f; // SAH node-visit cost the BVH8 was built with (0.5: the fastest measured on the 1M-triangle scene)
     float bounds_lo[3] = {0, 0, 0}, bounds_hi[3] = {0, 0, 0}; // world box of the triangles
     uint64_t texel_key = 0, env_key = 0; // hashes of the uploaded texture and environment tables
     VgCache* cache = nullptr;  // radiance cache integrator when set
