@@ -119,6 +119,14 @@ __device__ __forceinline__ uint32_t byte_of(uint32_t lo, uint32_t hi, int i)
     return (w >> ((i & 3) * 8)) & 0xffu;
 }
 
+// The byte as a float, exactly: the byte placed in the mantissa of 2^23 (one byte permute), minus
+// 2^23; equal to (float)byte_of(lo, hi, i) without an integer-to-float conversion.
+__device__ __forceinline__ float byte_f(uint32_t lo, uint32_t hi, int i)
+{
+    uint32_t w = i < 4 ? lo : hi;
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u + (uint32_t)(i & 3))) - 8388608.0f;
+}
+
 // Closest hit (ANY = false) or any hit (ANY = true) with 0 < t < tmax.
 template <bool ANY>
 __device__ __forceinline__ TraceHit trace_bvh(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
@@ -173,12 +181,12 @@ __device__ __forceinline__ TraceHit trace_bvh(const uint4* __restrict__ nodes, c
         uint32_t tri_bits = 0;
 #pragma unroll
         for (int i = 0; i < 8; i++) {
-            float tnx = fmaf((float)byte_of(nxl, nxh, i), sx, anx);
-            float tny = fmaf((float)byte_of(nyl, nyh, i), sy, any_);
-            float tnz = fmaf((float)byte_of(nzl, nzh, i), sz, anz);
-            float tfx = fmaf((float)byte_of(fxl, fxh, i), sx, afx);
-            float tfy = fmaf((float)byte_of(fyl, fyh, i), sy, afy);
-            float tfz = fmaf((float)byte_of(fzl, fzh, i), sz, afz);
+            float tnx = fmaf(byte_f(nxl, nxh, i), sx, anx);
+            float tny = fmaf(byte_f(nyl, nyh, i), sy, any_);
+            float tnz = fmaf(byte_f(nzl, nzh, i), sz, anz);
+            float tfx = fmaf(byte_f(fxl, fxh, i), sx, afx);
+            float tfy = fmaf(byte_f(fyl, fyh, i), sy, afy);
+            float tfz = fmaf(byte_f(fzl, fzh, i), sz, afz);
             float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
             float tf = fminf(fminf(tfx, tfy), fminf(tfz, best_t));
             if (tn <= tf) {
@@ -296,12 +304,12 @@ __device__ __forceinline__ bool walk_step(const uint4* __restrict__ nodes, const
     uint32_t inner_hits = 0, tri_bits = 0;
 #pragma unroll
     for (int i = 0; i < 8; i++) {
-        float tnx = fmaf((float)byte_of(nxl, nxh, i), sx, anx);
-        float tny = fmaf((float)byte_of(nyl, nyh, i), sy, any_);
-        float tnz = fmaf((float)byte_of(nzl, nzh, i), sz, anz);
-        float tfx = fmaf((float)byte_of(fxl, fxh, i), sx, afx);
-        float tfy = fmaf((float)byte_of(fyl, fyh, i), sy, afy);
-        float tfz = fmaf((float)byte_of(fzl, fzh, i), sz, afz);
+        float tnx = fmaf(byte_f(nxl, nxh, i), sx, anx);
+        float tny = fmaf(byte_f(nyl, nyh, i), sy, any_);
+        float tnz = fmaf(byte_f(nzl, nzh, i), sz, anz);
+        float tfx = fmaf(byte_f(fxl, fxh, i), sx, afx);
+        float tfy = fmaf(byte_f(fyl, fyh, i), sy, afy);
+        float tfz = fmaf(byte_f(fzl, fzh, i), sz, afz);
         float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
         float tf = fminf(fminf(tfx, tfy), fminf(tfz, best_t));
         if (tn <= tf) {
