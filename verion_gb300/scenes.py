@@ -9,6 +9,8 @@ Workloads (no dataset is involved; every scene is generated here):
   512 x 512 grid (2 x 511^2 triangles) displaced by seeded value noise: 1,014,274 triangles.
   Materials uniform among GGX conductor (roughness U[0.05, 1]), dielectric (IOR 1.5, smooth) and
   Lambertian; a 2048 x 1024 float HDRI of a sky gradient and a sun disk of peak 1e4.
+* `many_lights`: a 317 x 317 floor grid (200,312 triangles) with 120 random boxes and 4096 small
+  emissive triangles at uniform random positions, radiance log-uniform in [0.1, 100].
 """
 from __future__ import annotations
 
@@ -264,6 +266,42 @@ def many_spheres(seed: int = None, spheres: int = 64, sphere_n: int = 31, grid: 
         img = s.add_image(sky_hdri(hdri[0], hdri[1]))
         s.add_light(sc.EnvironmentMap(img, 1.0))
     s.camera = look_at((0.0, 5.5, 15.0), (0.0, 0.3, 0.0), fov=0.75)
+    return s
+
+
+def many_lights(seed: int = None, floor: int = 317, boxes: int = 120, emitters: int = 4096) -> sc.Scene:
+    """The many-light ReSTIR workload: a floor grid of 2 x (floor - 1)^2 triangles (200k at 317) with
+    random boxes standing on it, and `emitters` small emissive triangles at uniform random positions
+    above it, radiance log-uniform in [0.1, 100]. Seeded from config 3."""
+    seed = config_seed(3) if seed is None else seed
+    rng = np.random.default_rng(seed)
+    s = sc.Scene()
+    half = 10.0
+    xs = np.linspace(-half, half, floor)
+    gx, gz = np.meshgrid(xs, xs)
+    pos = np.stack([gx, np.zeros_like(gx), gz], axis=-1).reshape(-1, 3).astype(np.float32)
+    ii = np.arange(floor - 1)
+    a = (ii[:, None] * floor + ii[None, :]).reshape(-1)
+    idx = np.stack([a, a + floor, a + 1, a + 1, a + floor, a + floor + 1], axis=1).reshape(-1).astype(np.uint32)
+    ground = s.add_mesh(sc.Mesh(pos, idx))
+    s.add_instance(sc.Instance(ground, s.add_material(material((0.7, 0.7, 0.7)))))
+    box = s.add_mesh(cube(0.5))
+    for _ in range(boxes):
+        sx, sy, sz = rng.uniform(0.2, 1.2, 3)
+        x, z = rng.uniform(-half * 0.9, half * 0.9, 2)
+        m = s.add_material(material(tuple(rng.uniform(0.2, 0.9, 3))))
+        s.add_instance(sc.Instance(box, m, ((sx, 0, 0, x), (0, sy, 0, sy * 0.5), (0, 0, sz, z))))
+    tri = np.array([[-0.05, 0.0, -0.05], [0.05, 0.0, -0.05], [0.0, 0.0, 0.05]], np.float32)
+    pos, idx, mats = [], [], []
+    lights = s.add_mesh(sc.Mesh(tri, np.array([0, 1, 2], np.uint32)))
+    for _ in range(emitters):
+        p = rng.uniform((-half, 0.2, -half), (half, 4.0, half))
+        le = float(math.exp(rng.uniform(math.log(0.1), math.log(100.0))))
+        m = s.add_material(material((0.0, 0.0, 0.0), (le, le, le)))
+        # Face down, tilted at random.
+        t = rng.normal(size=3) * 0.3
+        s.add_instance(sc.Instance(lights, m, ((1.0, t[0], 0.0, p[0]), (0.0, -1.0, 0.0, p[1]), (0.0, t[1], 1.0, p[2]))))
+    s.camera = look_at((0.0, 6.0, 14.0), (0.0, 0.5, 0.0), fov=0.9)
     return s
 
 
