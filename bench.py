@@ -282,49 +282,122 @@ def _rmse_at(curve, t):
     return None
 
 
-def cache_report(ctx, peak_tflops, peak_kind):
-    """Radiance cache on the Cornell box (512 x 512, depth 8, 32 triangles): plain megakernel path
-    tracing against the cache integrator, RMSE against an 8192-spp plain image over GPU time, and
-    the MLP kernels' device time on 2^20 synthetic records against the tensor roofline."""
-    from verion_gb300 import pack, scenes
-    from verion_gb300.backend import Cache, Renderer
+def _cache_curve(r, acc, ref, chunks, limit_s=None):
+    curve, n = [], 0
+    for k in chunks:
+        r.accumulate(acc, k)
+        n += k
+        curve.append((acc.gpu_seconds(), _rmse(acc.mean(), ref)))
+        if limit_s is not None and acc.gpu_seconds() > limit_s:
+            break
+    return curve, n
 
+
+def _cache_vs_plain(plains, curve, target_at):
+    """Each plain curve's time to the RMSE the first plain curve has at point `target_at`, the
+    cache curve's time to it, and the speed-up against the fastest plain integrator."""
+    first = next(iter(plains.values()))
+    target = first[target_at][1]
+    t_plain = {name: _time_at(c, target) or c[-1][0] for name, c in plains.items()}
+    best = min(t_plain, key=t_plain.get)
+    t_cache = _time_at(curve, target)
+    return {"target_rmse": target, "time_to_target_s": {**{"plain_" + k: v for k, v in t_plain.items()},
+                                                         "cache": t_cache},
+            "speedup": (t_plain[best] / t_cache) if t_cache else None, "speedup_against": "plain " + best}
+
+
+def cache_report(ctx, packed_c2, peak_tflops, peak_kind):
+    """Radiance cache (cache query paths on the streaming wavefront) against plain path tracing:
+    time to reach a plain image's RMSE (against a long plain reference, GPU time), the speed-up
+    taken against the fastest plain integrator. C4: Cornell box 512 x 512, depth 8. C2: the
+    1M-triangle workload at 1920 x 1080, depth 16, against plain wavefront with and without
+    adaptive sampling. Then the MLP kernels' device time on 2^20 synthetic records against the
+    tensor roofline."""
+    from verion_gb300 import pack, scenes
+    from verion_gb300.backend import Cache, Integrator, Renderer
+    from verion_gb300.readback import Adaptive
+
+    out = {}
+    # C4.
     p = pack.pack(scenes.cornell())
     ref_r = Renderer(ctx, p)
+    ref_r.set_integrator(Integrator.WAVEFRONT)
     acc = ref_r.new_accumulation(CACHE_W, CACHE_H)
     for _ in range(CACHE_REF_SPP // 512):
         ref_r.accumulate(acc, 512)
     ref = acc.mean()
-    del acc
-    plain_r = Renderer(ctx, p)
-    acc = plain_r.new_accumulation(CACHE_W, CACHE_H)
-    plain, n = [], 0
-    for k in (32, 32, 64, 128, 256, 512):
-        plain_r.accumulate(acc, k)
-        n += k
-        plain.append((acc.gpu_seconds(), _rmse(acc.mean(), ref)))
-    plain_spp_ms = 1e3 * acc.gpu_seconds() / n
-    del acc
+    del acc, ref_r
+    plains, plain_ms = {}, {}
+    for name, integ in (("megakernel", Integrator.MEGAKERNEL), ("wavefront", Integrator.WAVEFRONT)):
+        plain_r = Renderer(ctx, p)
+        plain_r.set_integrator(integ)
+        acc = plain_r.new_accumulation(CACHE_W, CACHE_H)
+        plains[name], n = _cache_curve(plain_r, acc, ref, (32, 32, 64, 128, 256, 512))
+        plain_ms[name] = 1e3 * acc.gpu_seconds() / n
+        del acc, plain_r
     r = Renderer(ctx, p)
-    cache = Cache(ctx, bounds=r.bounds())
-    r.set_cache(cache, spread=0.01, train_paths=16384, train_steps=4, train_batch=16384)
+    r.set_integrator(Integrator.WAVEFRONT)
+    r.set_cache_frame(8)
+    cache = Cache(ctx, bounds=r.bounds(), log2_entries=17)
+    r.set_cache(cache, spread=0.01, train_paths=8192, train_steps=2, train_batch=32768)
     r.set_stage_timing(True)
     acc = r.new_accumulation(CACHE_W, CACHE_H)
-    curve, n = [], 0
-    for k in (32, 32, 64, 128, 256, 512, 1024):
-        r.accumulate(acc, k)
-        n += k
-        curve.append((acc.gpu_seconds(), _rmse(acc.mean(), ref)))
-    img = acc.mean()
+    curve, n = _cache_curve(r, acc, ref, (32, 32, 64, 128, 256, 512, 1024))
     st = acc.cache_stats()
-    frame_ms = 1e3 * acc.gpu_seconds() / n
-    target = plain[-1][1]
-    t_plain = plain[-1][0]
-    t_cache = _time_at(curve, target)
+    c4 = {"config": "Cornell box 512x512, depth 8; cache 16 levels x 2^17 entries x 2 fp16, MLP 64 x 4 hidden bf16; "
+                    "frames of 8 samples, ~8192 training pixels, 2 Adam steps of 32768 records per frame; "
+                    f"reference {CACHE_REF_SPP} spp plain; target: plain megakernel RMSE at 1024 spp",
+          "plain_ms_per_spp": plain_ms, "cache_ms_per_spp": 1e3 * acc.gpu_seconds() / n,
+          "cache_split_seconds": {"paths": st.path_seconds, "encode_and_infer": st.infer_seconds,
+                                  "train": st.train_seconds},
+          "bias_rel_mean": float((acc.mean().mean() - ref.mean()) / ref.mean()),
+          "cache_curve": curve, "plain_curves": plains}
+    c4.update(_cache_vs_plain(plains, curve, -1))
+    out["cornell_512"] = c4
+    del acc, r
+    # C2.
+    def c2_renderer(adaptive=False):
+        rr = Renderer(ctx, packed_c2)
+        rr.set_integrator(Integrator.WAVEFRONT)
+        rr.set_max_depth(DEPTH)
+        if adaptive:
+            rr.set_adaptive(Adaptive(*ADAPTIVE))
+        return rr
+
+    ref_r = c2_renderer()
+    acc = ref_r.new_accumulation(WIDTH, HEIGHT)
+    for _ in range(16):
+        ref_r.accumulate(acc, 128)
+    ref = acc.mean()
+    del acc, ref_r
+    plains = {}
+    for name, adaptive in (("wavefront", False), ("wavefront_adaptive", True)):
+        rr = c2_renderer(adaptive)
+        acc = rr.new_accumulation(WIDTH, HEIGHT)
+        plains[name], _ = _cache_curve(rr, acc, ref, (8, 8, 16, 32, 64, 128))
+        del acc, rr
+    r = c2_renderer()
+    cache = Cache(ctx, bounds=r.bounds())
+    r.set_cache(cache)  # defaults: spread 0.01, ~16384 training pixels, 4 Adam steps of 16384 records
+    r.set_stage_timing(True)
+    acc = r.new_accumulation(WIDTH, HEIGHT)
+    curve, n = _cache_curve(r, acc, ref, (8, 8, 16, 32, 64, 128))
+    st = acc.cache_stats()
+    c2 = {"config": "1M-triangle workload 1920x1080, depth 16; cache 16 levels x 2^19 entries, frames of 4 samples, "
+                    "~16384 training pixels, 4 Adam steps of 16384 records per frame; reference 2048 spp plain",
+          "cache_ms_per_spp": 1e3 * acc.gpu_seconds() / n,
+          "cache_split_seconds": {"paths": st.path_seconds, "encode_and_infer": st.infer_seconds,
+                                  "train": st.train_seconds},
+          "bias_rel_mean": float((acc.mean().mean() - ref.mean()) / ref.mean()),
+          "cache_curve": curve, "plain_curves": plains}
+    for label, at in (("at_64spp", 3), ("at_256spp", 5)):
+        c2[label] = _cache_vs_plain(plains, curve, at)
+    out["many_spheres_1080p"] = c2
+    del acc, r
     # MLP kernels on synthetic records (random positions in the scene box, unit directions).
     rng = np.random.default_rng(5)
     nrec = 1 << 20
-    lo, hi = r.bounds()
+    lo, hi = ((-1.0,) * 3, (1.0,) * 3)
     rec = np.zeros((nrec, 20), np.float32)
     rec[:, 0:3] = rng.uniform(lo, hi, (nrec, 3))
     for o in (3, 6):
@@ -332,29 +405,16 @@ def cache_report(ctx, peak_tflops, peak_kind):
         rec[:, o:o + 3] = d / np.linalg.norm(d, axis=1, keepdims=True)
     rec[:, 9:15] = rng.uniform(0, 1, (nrec, 6))
     rec[:, 16:19] = rng.uniform(0, 2, (nrec, 3))
-    kt = cache.time_kernels(rec, reps=10)
+    kc = Cache(ctx, bounds=(lo, hi))
+    kt = kc.time_kernels(rec, reps=10)
     infer_tf = CACHE_MLP_FLOP * nrec / kt["infer"] / 1e12
     train_tf = 3 * CACHE_MLP_FLOP * nrec / kt["train"] / 1e12
-    return {
-        "config": "Cornell box 512x512, depth 8, 1 sample per pixel per frame; cache 16 levels x 2^19 entries x 2 fp16, "
-                  "MLP 64 x 4 hidden bf16; 4 Adam steps of 16384 records per frame from ~16384 training paths; "
-                  f"reference {CACHE_REF_SPP} spp plain",
-        "plain_ms_per_spp": plain_spp_ms, "cache_ms_per_frame": frame_ms,
-        "cache_split_seconds": {"paths": st.path_seconds, "encode_and_infer": st.infer_seconds,
-                                "train": st.train_seconds},
-        "queries_per_frame": st.queries, "train_records_per_frame": st.train_records,
-        "target_rmse": target, "target": f"plain RMSE at {sum((32, 32, 64, 128, 256, 512))} spp",
-        "time_to_target_s": {"plain": t_plain, "cache": t_cache},
-        "speedup": (t_plain / t_cache) if t_cache else None,
-        "rmse_equal_time": {"seconds": t_plain, "plain": target, "cache": _rmse_at(curve, t_plain)},
-        "cache_curve": curve, "plain_curve": plain,
-        "bias_rel_mean": float((img.mean() - ref.mean()) / ref.mean()),
-        "mlp_kernels": {"records": nrec, "seconds_per_launch": kt,
-                        "infer_tflops": infer_tf, "train_tflops": train_tf,
-                        "peak_tflops": peak_tflops, "peak_kind": peak_kind,
-                        "infer_frac": infer_tf / peak_tflops, "train_frac": train_tf / peak_tflops,
-                        "flop_per_record": {"infer": CACHE_MLP_FLOP, "train": 3 * CACHE_MLP_FLOP}},
-    }
+    out["mlp_kernels"] = {"records": nrec, "seconds_per_launch": kt,
+                          "infer_tflops": infer_tf, "train_tflops": train_tf,
+                          "peak_tflops": peak_tflops, "peak_kind": peak_kind,
+                          "infer_frac": infer_tf / peak_tflops, "train_frac": train_tf / peak_tflops,
+                          "flop_per_record": {"infer": CACHE_MLP_FLOP, "train": 3 * CACHE_MLP_FLOP}}
+    return out
 
 
 BATCH_SCENES = [(4, 15, 48), (16, 21, 160), (48, 31, 400), (128, 31, 724)]  # spheres, sphere resolution, grid
@@ -645,7 +705,7 @@ def run_cuda(args):
     if rank == 0 and not args.no_cache:
         bf = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("bf16_tflops") \
             if (ROOT / "MEASURED_PEAKS.json").exists() else None
-        cache = cache_report(ctx, bf or 1900.0, "measured (bf16_tflops, burst)" if bf else "fallback")
+        cache = cache_report(ctx, packed, bf or 1900.0, "measured (bf16_tflops, burst)" if bf else "fallback")
 
     restir = None
     if rank == 0 and not args.no_restir:

@@ -466,11 +466,20 @@ int vg_cache_time(VgCache* cache, const float* records, size_t n, uint32_t reps,
  * spread passes `spread` times the primary spread (Mueller et al. 2021), and adds the cache's
  * prediction there times the path throughput; about `train_paths` pixels per sample trace
  * training paths to full depth instead, whose vertices train the cache for `train_steps` Adam
- * steps of `train_batch` records after the sample. Megakernel paths; the lighting split,
- * adaptive sampling and ReSTIR are not available with it (VG_ERR_UNSUPPORTED). The renderer does
- * not own the cache: keep it alive while the renderer uses it. */
+ * steps of `train_batch` records after the sample. With the WAVEFRONT integrator the query paths
+ * run on the streaming wavefront in frames of several samples (vg_set_cache_frame), with
+ * MEGAKERNEL in one kernel per sample; training paths always run in a kernel of their own,
+ * overlapping the query paths. For the same cache state both integrators find the same queries
+ * and answers. The lighting split, adaptive sampling and ReSTIR are not available with it
+ * (VG_ERR_UNSUPPORTED). The renderer does not own the cache: keep it alive while the renderer
+ * uses it. */
 int vg_set_cache(VgRenderer* r, VgCache* cache, float spread, uint32_t train_paths, uint32_t train_steps,
                  uint32_t train_batch);
+/* WAVEFRONT integrator with a cache: samples per cache frame (1-16, default 4). The cache is fixed
+ * within a frame and trained after it (vg_set_cache's steps), so a frame of k samples runs as one
+ * streaming wavefront dispatch of k samples per pixel (the last waves of a dispatch are nearly
+ * empty; k samples share them). The training pixels of a frame trace all its samples. */
+int vg_set_cache_frame(VgRenderer* r, uint32_t samples_per_frame);
 /* Of the last sample of the last accumulate call with the cache: query records, training
  * records (before the capacity clamp), and the last training step's mean loss per channel;
  * with stage timing, seconds spent in the path kernel, inference and training over that call. */

@@ -162,9 +162,12 @@ def rmse(a, b):
     return float(np.sqrt(np.mean((a - b) ** 2)))
 
 
-def test_cache_integrator_gains_over_no_cache(gpu_ctx):
+@pytest.mark.parametrize("integrator", ["megakernel", "wavefront"])
+def test_cache_integrator_gains_over_no_cache(gpu_ctx, integrator):
     # Cornell box: the trained cache's image is far closer to the converged plain image than the
     # same spread-terminated paths with no trained cache (prediction 0), and its bias is small.
+    from verion_gb300.backend import Integrator
+    integ = Integrator.WAVEFRONT if integrator == "wavefront" else Integrator.MEGAKERNEL
     s = scenes.cornell()
     p = pack.pack(s)
     w = h = 64
@@ -173,6 +176,7 @@ def test_cache_integrator_gains_over_no_cache(gpu_ctx):
 
     def run(train_steps, zero):
         r = Renderer(gpu_ctx, p)
+        r.set_integrator(integ)
         cache = Cache(gpu_ctx, bounds=r.bounds())
         if zero:
             m, _ = cache.param_counts()
@@ -190,3 +194,53 @@ def test_cache_integrator_gains_over_no_cache(gpu_ctx):
     e_cache, e_zero = rmse(img, ref), rmse(zero_img, ref)
     assert e_cache < 0.5 * e_zero, (e_cache, e_zero)
     assert abs(img.mean() - ref.mean()) < 0.1 * ref.mean()
+
+
+@pytest.mark.parametrize("scene", ["cornell", "feature_zoo"])
+def test_cache_on_the_wavefront_matches_the_megakernel_cache(gpu_ctx, scene):
+    # Without training the cache is fixed, so the query paths on the streaming wavefront leave the
+    # image of the one-kernel query paths: same paths, same queries, same answers per pixel. One
+    # sample per frame: bit for bit. Three per frame: the training pixels differ (one set per frame
+    # instead of one per sample; with train_paths 0 at most one pixel per frame) and the cache's
+    # answers are added after the frame's path sums rather than after each, so the other pixels
+    # agree to rounding. The feature zoo has glass and cut-out surfaces (shadow rays in the
+    # combined shadow stage), the Cornell box is opaque (any-hit stage).
+    from verion_gb300.backend import Integrator
+    if scene == "cornell":
+        p = pack.pack(scenes.cornell())
+    else:
+        from . import analytic
+        p = pack.pack(analytic.feature_zoo())
+    w, h = 48, 40
+    px = w * h
+
+    def run(integ, frame, train_paths, calls):
+        r = Renderer(gpu_ctx, p)
+        r.set_integrator(integ)
+        cache = Cache(gpu_ctx, bounds=r.bounds(), seed=7)
+        r.set_cache(cache, spread=0.01, train_paths=train_paths, train_steps=0, train_batch=1024)
+        if frame is not None:
+            r.set_cache_frame(frame)
+        acc = r.new_accumulation(w, h)
+        queries = 0
+        for n in calls:
+            r.accumulate(acc, n)
+            queries += acc.cache_stats().queries
+        return acc.sums_f64(), queries
+
+    want, wq = run(Integrator.MEGAKERNEL, None, 64, [1, 1, 1])
+    assert wq > 0
+    got, gq = run(Integrator.WAVEFRONT, 1, 64, [1, 1, 1])
+    assert gq == wq
+    assert np.array_equal(got, want), np.abs(got - want).max()
+
+    want, wq = run(Integrator.MEGAKERNEL, None, 0, [1, 1, 1])
+    got, gq = run(Integrator.WAVEFRONT, 3, 0, [3])
+    train = set()
+    for sample in range(3):
+        off = (sample * 2654435761) % 2**32 % (px + 1)
+        train.add((px + 1 - off) % (px + 1))
+    keep = np.ones(px, bool)
+    keep[[t for t in train if t < px]] = False
+    assert abs(gq - wq) <= 3, (gq, wq)
+    np.testing.assert_allclose(got.reshape(px, 3)[keep], want.reshape(px, 3)[keep], rtol=1e-12, atol=1e-12)

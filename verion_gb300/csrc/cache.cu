@@ -130,8 +130,13 @@ int stage_records(VgCache* k, DevBuf& b, const float* records, size_t n)
 
 using namespace vgc;
 
-// The cache integrator's samples (called by vg_accumulate with the parameter block filled in).
-int cache_accumulate(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, uint32_t samples, bool timed)
+// The cache integrator's samples (called by vg_accumulate with the parameter block filled in), in
+// frames: the query paths and training paths of a frame's samples, then the cache's answers for
+// the queries (encode + inference, one launch pair per sample of the frame, in sample order), then
+// the training steps on the frame's training records. With the streaming wavefront (`w`) a frame
+// holds up to cache_frame samples (the cache is fixed within it); with the one-kernel query
+// paths, one.
+int cache_accumulate(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, uint32_t samples, bool timed, const vgk::Wave* w)
 {
     VgCache* k = r->cache;
     if (acc->lighting || acc->restir.on || acc->adaptive)
@@ -140,59 +145,103 @@ int cache_accumulate(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, uint32_t samples,
     cudaStream_t s = r->ctx->stream;
     size_t px = (size_t)acc->width * acc->height;
     uint32_t tcap = r->cache_steps * r->cache_batch;
+    uint32_t frame = w ? std::max(1u, r->cache_frame) : 1u;
     int st;
-    if (!acc->cache_q.p || acc->cache_q.bytes < px * vgn::REC_WORDS * 4)
-        if ((st = alloc(acc->cache_q, px * vgn::REC_WORDS * 4, s, false)) != VG_OK)
+    if (!acc->cache_q.p || acc->cache_q.bytes < frame * px * vgn::REC_WORDS * 4)
+        if ((st = alloc(acc->cache_q, frame * px * vgn::REC_WORDS * 4, s, false)) != VG_OK)
             return st;
     if (!acc->cache_t.p || acc->cache_t.bytes < (size_t)std::max(tcap, 1u) * vgn::REC_WORDS * 4)
         if ((st = alloc(acc->cache_t, (size_t)std::max(tcap, 1u) * vgn::REC_WORDS * 4, s, false)) != VG_OK)
             return st;
-    if (!acc->cache_ctr.p && (st = alloc(acc->cache_ctr, 16, s, true)) != VG_OK)
+    // Counters: [0] training records, [1 + j] queries of sample j of the frame.
+    if (!acc->cache_ctr.p && (st = alloc(acc->cache_ctr, (1 + MAX_CACHE_FRAME) * 4, s, true)) != VG_OK)
         return st;
+    if (w && !acc->cache_spread.p && (st = alloc(acc->cache_spread, px * 8, s, false)) != VG_OK)
+        return st;
+    if (!r->ctx->side) {
+        VG_CHECK(cudaStreamCreateWithFlags(&r->ctx->side, cudaStreamNonBlocking), "side stream");
+        VG_CHECK(cudaEventCreateWithFlags(&r->ctx->fork, cudaEventDisableTiming), "event");
+        VG_CHECK(cudaEventCreateWithFlags(&r->ctx->join, cudaEventDisableTiming), "event");
+    }
     VG_CHECK(cudaMemsetAsync(k->err.p, 0, 4, s), "error flag");
     uint32_t* ctr = (uint32_t*)acc->cache_ctr.p;
     NrcPathArgs a;
     a.spread = r->cache_spread;
     a.train_stride = (uint32_t)std::max<size_t>(1, r->cache_train_paths ? px / r->cache_train_paths : px + 1);
     a.qrec = (float*)acc->cache_q.p;
-    a.qcount = ctr;
+    a.qcount = ctr + 1;
     a.qcap = (uint32_t)px;
     a.trec = (float*)acc->cache_t.p;
-    a.tcount = ctr + 1;
+    a.tcount = ctr;
     a.tcap = tcap;
     if ((st = ensure_work(k, std::max<size_t>(px, r->cache_batch))) != VG_OK)
         return st;
+    vgk::CacheWave q;
+    q.spread = a.spread;
+    q.st = (float2*)acc->cache_spread.p;
+    q.qrec = a.qrec;
+    q.qcount = a.qcount;
+    q.qcap = a.qcap;
+    q.train_stride = a.train_stride;
     dim3 grid((acc->width + 15) / 16, (acc->height + 7) / 8);
     vgn::CacheDev d = k->dev();
     bool f64 = acc->precision == 64;
+    vgx::Variant v = variant_of(r, acc);
     EventPool pool;
-    for (uint32_t i = 0; i < samples; i++) {
+    StageEvents stages;
+    for (uint32_t i = 0; i < samples;) {
+        uint32_t n = std::min(frame, samples - i);
         uint32_t sample = acc->samples + i;
         c.p[P_SAMPLE] = sample;
-        c.p[P_SAMPLES_PER_DISPATCH] = 1;
+        c.p[P_SAMPLES_PER_DISPATCH] = n;
         a.train_offset = (sample * 2654435761u) % a.train_stride;
+        q.train_offset = a.train_offset;
         cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr, e3 = nullptr;
         if (timed) {
             e0 = pool.get(), e1 = pool.get(), e2 = pool.get(), e3 = pool.get();
             VG_CHECK(cudaEventRecord(e0, s), "event");
         }
-        VG_CHECK(cudaMemsetAsync(ctr, 0, 8, s), "counters");
-        VG_CHECK(vgx::nrc_launch_paths(f64, grid, s, c, a), "cache path launch");
+        VG_CHECK(cudaMemsetAsync(ctr, 0, (1 + n) * 4, s), "counters");
+        // Training paths (full depth, few) on the side stream, overlapping the query paths and the
+        // inference; joined before the training steps. They add to other pixels than the queries.
+        uint32_t first;
+        bool train = vgx::nrc_train_pixels(px, a.train_stride, a.train_offset, &first) > 0;
+        if (train) {
+            VG_CHECK(cudaEventRecord(r->ctx->fork, s), "fork");
+            VG_CHECK(cudaStreamWaitEvent(r->ctx->side, r->ctx->fork, 0), "fork");
+            VG_CHECK(vgx::nrc_launch_train_paths(f64, r->ctx->side, c, a), "cache training path launch");
+            VG_CHECK(cudaEventRecord(r->ctx->join, r->ctx->side), "join");
+            acc->launches++;
+        }
+        if (w) {
+            if ((st = stream_samples(r, acc, c, v, *w, sample, n, false, pool, stages, &q)) != VG_OK)
+                return st;
+        } else {
+            VG_CHECK(vgx::nrc_launch_query_paths(f64, grid, s, c, a), "cache path launch");
+            acc->launches++;
+        }
         if (timed)
             VG_CHECK(cudaEventRecord(e1, s), "event");
-        VG_CHECK(vgx::nrc_launch_encode(encode_blocks(k), s, d, a.qrec, ctr, a.qcap, 0, a.qcap, (uint8_t*)k->X.p),
-                 "cache encode launch");
-        VG_CHECK(vgx::nrc_launch_infer(3 * r->ctx->sms, s, d, (const uint8_t*)k->X.p, a.qrec, ctr, a.qcap, nullptr,
-                                       c.accum, f64 ? 64 : 32),
-                 "cache inference launch");
+        for (uint32_t j = 0; j < n; j++) {
+            const float* rj = a.qrec + (size_t)j * px * vgn::REC_WORDS;
+            VG_CHECK(vgx::nrc_launch_encode(encode_blocks(k), s, d, rj, ctr + 1 + j, a.qcap, 0, a.qcap,
+                                            (uint8_t*)k->X.p),
+                     "cache encode launch");
+            VG_CHECK(vgx::nrc_launch_infer(3 * r->ctx->sms, s, d, (const uint8_t*)k->X.p, rj, ctr + 1 + j, a.qcap,
+                                           nullptr, c.accum, f64 ? 64 : 32),
+                     "cache inference launch");
+            acc->launches += 2;
+        }
         if (timed)
             VG_CHECK(cudaEventRecord(e2, s), "event");
-        acc->launches += 3;
+        if (train)
+            VG_CHECK(cudaStreamWaitEvent(s, r->ctx->join, 0), "join");
         for (uint32_t t = 0; t < r->cache_steps; t++) {
-            if ((st = cache_train_step(k, a.trec, ctr + 1, tcap, t * r->cache_batch, r->cache_batch)) != VG_OK)
+            if ((st = cache_train_step(k, a.trec, ctr, tcap, t * r->cache_batch, r->cache_batch)) != VG_OK)
                 return st;
             acc->launches += 7;
         }
+        acc->cache_frame_last = n;
         if (timed) {
             VG_CHECK(cudaEventRecord(e3, s), "event");
             if ((st = wait_event(e3)) != VG_OK)
@@ -201,10 +250,10 @@ int cache_accumulate(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, uint32_t samples,
             cudaEventElapsedTime(&ms[0], e0, e1);
             cudaEventElapsedTime(&ms[1], e1, e2);
             cudaEventElapsedTime(&ms[2], e2, e3);
-            for (int q = 0; q < 3; q++)
-                acc->cache_seconds[q] += ms[q] * 1e-3;
-            pool.used = 0;
+            for (int m = 0; m < 3; m++)
+                acc->cache_seconds[m] += ms[m] * 1e-3;
         }
+        i += n;
     }
     return VG_OK;
 }
@@ -532,6 +581,16 @@ int vg_set_cache(VgRenderer* r, VgCache* cache, float spread, uint32_t train_pat
     return VG_OK;
 }
 
+int vg_set_cache_frame(VgRenderer* r, uint32_t samples_per_frame)
+{
+    if (!r)
+        return fail(VG_ERR_INVALID, "null renderer");
+    if (samples_per_frame < 1 || samples_per_frame > MAX_CACHE_FRAME)
+        return fail(VG_ERR_INVALID, "cache frame out of range (1-" + std::to_string(MAX_CACHE_FRAME) + " samples)");
+    r->cache_frame = samples_per_frame;
+    return VG_OK;
+}
+
 int vg_accum_cache_stats(const VgAccum* acc, VgCacheStats* out)
 {
     if (!acc || !out)
@@ -543,16 +602,18 @@ int vg_accum_cache_stats(const VgAccum* acc, VgCacheStats* out)
     if (!acc->cache_ctr.p)
         return VG_OK;
     cudaStream_t s = acc->owner->ctx->stream;
-    uint32_t ctr[2] = {0, 0};
-    VG_CHECK(cudaMemcpyAsync(ctr, acc->cache_ctr.p, 8, cudaMemcpyDeviceToHost, s), "readback");
+    uint32_t ctr[1 + MAX_CACHE_FRAME] = {};
+    uint32_t n = std::min<uint32_t>(acc->cache_frame_last, MAX_CACHE_FRAME);
+    VG_CHECK(cudaMemcpyAsync(ctr, acc->cache_ctr.p, (1 + n) * 4, cudaMemcpyDeviceToHost, s), "readback");
     double l = 0.0;
     if (acc->owner->cache)
         VG_CHECK(cudaMemcpyAsync(&l, acc->owner->cache->loss.p, 8, cudaMemcpyDeviceToHost, s), "readback");
     VG_CHECK(cudaStreamSynchronize(s), "readback");
-    out->queries = ctr[0];
-    out->train_records = ctr[1];
+    for (uint32_t j = 0; j < n; j++)
+        out->queries += ctr[1 + j];
+    out->train_records = ctr[0];
     uint32_t tcap = acc->owner->cache_steps * acc->owner->cache_batch;
-    uint32_t avail = std::min(ctr[1], tcap);
+    uint32_t avail = std::min(ctr[0], tcap);
     uint32_t steps = acc->owner->cache_steps;
     if (steps > 0 && acc->owner->cache_batch > 0 && avail > 0) {
         uint32_t last_off = (steps - 1) * acc->owner->cache_batch;

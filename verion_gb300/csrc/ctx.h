@@ -79,4 +79,18 @@ struct Wave {
     uint32_t depth;    // max depth
 };
 
+// Radiance-cache frames on the streaming wavefront: the path spread (a0, a) of every slot,
+// carried between waves, and where a path that ends at the cache leaves its query record: sample
+// k of the frame in range k (records qrec + k qcap ..., count qcount[k]), so that each range holds
+// at most one query per pixel. Training pixels ((pixel + train_offset) % train_stride == 0) are
+// traced by their own kernel.
+struct CacheWave {
+    float spread;          // threshold c of a^2 > c a0
+    float2* st;            // per slot: a0, a
+    float* qrec;           // query records (CACHE_REC_WORDS floats each)
+    uint32_t* qcount;      // one count per sample of the frame
+    uint32_t qcap;         // records per range (pixels)
+    uint32_t train_stride, train_offset;
+};
+
 } // namespace vgk

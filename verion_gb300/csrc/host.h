@@ -119,6 +119,8 @@ struct VgContext {
     int batch_blocks_per_sm = 0; // 0: as many as fit (vg_batch_tune chooses)
     int batch_order = 0;         // VgBatchOrder
     uint64_t batch_wavefront_pixels = 512 * 512; // requests at least this large run on the wavefront
+    cudaStream_t side = nullptr;                 // second stream (created on first use): cache training paths
+    cudaEvent_t fork = nullptr, join = nullptr;  // ordering between `stream` and `side`
     ~VgContext();
 };
 
@@ -131,6 +133,8 @@ struct Restir {
         return on == o.on && (!on || (di == o.di && gi == o.gi && candidates == o.candidates && history == o.history));
     }
 };
+
+constexpr uint32_t MAX_CACHE_FRAME = 16; // samples per radiance-cache frame at most
 
 struct VgRenderer {
     VgContext* ctx = nullptr;
@@ -169,6 +173,8 @@ struct VgRenderer {
     uint32_t cache_train_paths = 16384;
     uint32_t cache_steps = 4;
     uint32_t cache_batch = 16384;
+    uint32_t cache_frame = 4;     // integrator WAVEFRONT: samples per cache frame (one cache update per frame)
+    int cache_shade_blocks[2] = {};
 };
 
 struct VgAccum {
@@ -204,6 +210,8 @@ struct VgAccum {
     size_t restir_bytes = 0;
     uint32_t last_depth = 0; // max depth of the last wavefront sample
     DevBuf cache_q, cache_t, cache_ctr; // radiance cache: query and training records, their counts
+    DevBuf cache_spread;                // radiance cache on the streaming wavefront: a0, a per slot
+    uint32_t cache_frame_last = 0;      // samples in the last cache frame (query counters in use)
     double cache_seconds[3] = {0, 0, 0}; // with stage timing: paths, inference, training
 };
 
@@ -347,6 +355,24 @@ int validate(const VgPacked* pk)
 
 int blocks_for(VgRenderer* r, int per_sm) { return std::max(1, per_sm) * r->ctx->sms; }
 
+// The wavefront buffers of an accumulation (allocated on its first wavefront accumulate).
+vgk::Wave wave_of(const VgRenderer* r, const VgAccum* acc)
+{
+    vgk::Wave w;
+    w.state = (float4*)acc->state.p;
+    w.hits = (uint4*)acc->hits.p;
+    w.queue[0] = (uint32_t*)acc->queue[0].p;
+    w.queue[1] = (uint32_t*)acc->queue[1].p;
+    w.counts = (uint32_t*)acc->counts.p;
+    w.fetch = (uint32_t*)acc->fetch.p;
+    w.tstats = (unsigned long long*)acc->tstats.p;
+    w.sreq = (float4*)acc->sreq.p;
+    w.meta = (uint32_t*)acc->meta.p;
+    w.n = acc->width * acc->height;
+    w.depth = r->max_depth;
+    return w;
+}
+
 vgx::Variant variant_of(const VgRenderer* r, const VgAccum* acc)
 {
     vgx::Variant v;
@@ -432,6 +458,8 @@ int read_err(VgRenderer* r)
     return VG_OK;
 }
 
+} // namespace
+
 struct EventPool {
     std::vector<cudaEvent_t> ev;
     size_t used = 0;
@@ -451,9 +479,15 @@ struct EventPool {
     }
 };
 
-} // namespace
+// Timed stages of a wavefront accumulate: (stage, (start event, end event)).
+using StageEvents = std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>>;
 
-// Radiance-cache integrator (cache.cu): the samples of one accumulate call, and the cache
-// kernels' error status.
-int cache_accumulate(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, uint32_t samples, bool timed);
+// Streaming wavefront (vgcuda.cu) over `samples` samples per pixel from sample0; with `q` the
+// radiance-cache kernel variants.
+int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, const vgk::Wave& w, uint32_t sample0,
+                   uint32_t samples, bool timed, EventPool& pool, StageEvents& stages, const vgk::CacheWave* q);
+
+// Radiance-cache integrator (cache.cu): the samples of one accumulate call (query paths on the
+// streaming wavefront when `w` is given, else in one kernel), and the cache kernels' error status.
+int cache_accumulate(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, uint32_t samples, bool timed, const vgk::Wave* w);
 int cache_status(VgRenderer* r);

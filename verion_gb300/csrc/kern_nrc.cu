@@ -485,38 +485,33 @@ static __device__ __forceinline__ uint32_t warp_reserve(uint32_t* ctr, uint32_t 
     return base + incl - k;
 }
 
-static __device__ __forceinline__ void put_features(float* d, const CacheHook& hk)
-{
-    d[0] = hk.pos.x, d[1] = hk.pos.y, d[2] = hk.pos.z;
-    d[3] = hk.wo.x, d[4] = hk.wo.y, d[5] = hk.wo.z;
-    d[6] = hk.n.x, d[7] = hk.n.y, d[8] = hk.n.z;
-    d[9] = hk.rough;
-    d[10] = hk.albedo.x, d[11] = hk.albedo.y, d[12] = hk.albedo.z;
-    d[13] = hk.metallic;
-    d[14] = hk.transmission;
-    d[15] = 0.0f;
-}
+static_assert(REC_WORDS == CACHE_REC_WORDS, "cache record layout");
 
 // One sample per pixel (sample index P_SAMPLE). A path ends at the first vertex where its
 // spread passes the threshold and leaves a query record (its radiance past that vertex comes
 // from the cache); one pixel in `train_stride` (offset by the frame) traces a training path
 // instead, which never ends for a query and leaves one training record per vertex with the
 // radiance the rest of the path brought, divided by the throughput reaching the vertex.
+// The two kinds run as separate kernels, so that the short query paths of a warp are not held
+// up by a training path's full depth: mk_cache_query over 16 x 8 pixel tiles (training pixels
+// idle), mk_cache_train over the training pixels only.
+static __device__ __forceinline__ bool is_train_pixel(const NrcPathArgs& a, uint32_t pixel)
+{
+    return (pixel + a.train_offset) % a.train_stride == 0;
+}
+
 template <typename A>
-__global__ void __launch_bounds__(128) mk_cache_paths(const __grid_constant__ Ctx c, NrcPathArgs a)
+__global__ void __launch_bounds__(128) mk_cache_query(const __grid_constant__ Ctx c, NrcPathArgs a)
 {
     uint32_t x = blockIdx.x * 16 + (threadIdx.x & 15u);
     uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 4);
-    bool inside = x < c.p[P_WIDTH] && y < c.p[P_HEIGHT];
     uint32_t pixel = y * c.p[P_WIDTH] + x;
+    bool inside = x < c.p[P_WIDTH] && y < c.p[P_HEIGHT] && !is_train_pixel(a, pixel);
     CacheHook hk;
     hk.c = a.spread;
-    hk.train = inside && (pixel + a.train_offset) % a.train_stride == 0;
+    hk.train = false;
     hk.a0 = hk.a = 0.0f;
     hk.query = false;
-    float feat[MAX_TRAIN_VERTICES][16];
-    V3 thr[MAX_TRAIN_VERTICES], Lb[MAX_TRAIN_VERTICES];
-    uint32_t nv = 0;
     bool query = false;
     PathState<false> st;
     if (inside) {
@@ -524,12 +519,6 @@ __global__ void __launch_bounds__(128) mk_cache_paths(const __grid_constant__ Ct
         for (uint32_t depth = 0; depth < c.p[P_MAX_DEPTH]; depth++) {
             bool alive = shadePath<false, false, false, true>(c, st, traceClosest(c, st.org, st.dir), depth, pixel,
                                                               nullptr, &hk);
-            if (hk.vertex && hk.train && nv < MAX_TRAIN_VERTICES) {
-                put_features(feat[nv], hk);
-                thr[nv] = hk.thr;
-                Lb[nv] = hk.L;
-                nv++;
-            }
             if (hk.query) {
                 query = true;
                 break;
@@ -541,26 +530,65 @@ __global__ void __launch_bounds__(128) mk_cache_paths(const __grid_constant__ Ct
     }
     bool ok = inside && !bad3(st.parts.total);
     uint32_t q = warp_reserve(a.qcount, (query && ok) ? 1u : 0u);
-    if (query && ok && q < a.qcap) {
-        float* d = a.qrec + (size_t)q * REC_WORDS;
-        put_features(d, hk);
-        d[16] = hk.thr.x, d[17] = hk.thr.y, d[18] = hk.thr.z;
-        d[19] = __uint_as_float(pixel);
-    }
-    uint32_t nt = (hk.train && ok) ? nv : 0u;
-    uint32_t t0 = warp_reserve(a.tcount, nt);
-    for (uint32_t k = 0; k < nt; k++) {
-        if (t0 + k >= a.tcap)
-            break;
-        float* d = a.trec + (size_t)(t0 + k) * REC_WORDS;
-        V3 rest = st.parts.total - Lb[k];
-        V3 t = thr[k];
-        for (int j = 0; j < 16; j++)
-            d[j] = feat[k][j];
-        d[16] = t.x > 0.0f ? rest.x / t.x : 0.0f;
-        d[17] = t.y > 0.0f ? rest.y / t.y : 0.0f;
-        d[18] = t.z > 0.0f ? rest.z / t.z : 0.0f;
-        d[19] = 0.0f;
+    if (query && ok && q < a.qcap)
+        cacheQueryRecord(a.qrec + (size_t)q * REC_WORDS, hk, pixel);
+}
+
+// Training pixels: pixel = first + k * train_stride for thread k, first = the smallest pixel with
+// (pixel + train_offset) % train_stride == 0; each traces the frame's P_SAMPLES_PER_DISPATCH
+// samples one after the other.
+template <typename A>
+__global__ void __launch_bounds__(128) mk_cache_train(const __grid_constant__ Ctx c, NrcPathArgs a, uint32_t first,
+                                                      uint32_t count)
+{
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    bool inside = k < count;
+    uint32_t pixel = first + k * a.train_stride;
+    uint32_t w = c.p[P_WIDTH];
+    uint32_t x = inside ? pixel % w : 0u, y = inside ? pixel / w : 0u;
+    CacheHook hk;
+    hk.c = a.spread;
+    hk.train = true;
+    hk.a0 = hk.a = 0.0f;
+    hk.query = false;
+    float feat[MAX_TRAIN_VERTICES][16];
+    V3 thr[MAX_TRAIN_VERTICES], Lb[MAX_TRAIN_VERTICES];
+    for (uint32_t ks = 0; ks < c.p[P_SAMPLES_PER_DISPATCH]; ks++) {
+        uint32_t nv = 0;
+        hk.a0 = hk.a = 0.0f;
+        PathState<false> st;
+        if (inside) {
+            st = generatePathFor<false>(c, x, y, c.p[P_SAMPLE] + ks);
+            for (uint32_t depth = 0; depth < c.p[P_MAX_DEPTH]; depth++) {
+                bool alive = shadePath<false, false, false, true>(c, st, traceClosest(c, st.org, st.dir), depth, pixel,
+                                                                  nullptr, &hk);
+                if (hk.vertex && nv < MAX_TRAIN_VERTICES) {
+                    cacheFeatures(feat[nv], hk);
+                    thr[nv] = hk.thr;
+                    Lb[nv] = hk.L;
+                    nv++;
+                }
+                if (!alive)
+                    break;
+            }
+            finishPath<false, A>(c, st, pixel);
+        }
+        bool ok = inside && !bad3(st.parts.total);
+        uint32_t nt = ok ? nv : 0u;
+        uint32_t t0 = warp_reserve(a.tcount, nt);
+        for (uint32_t j = 0; j < nt; j++) {
+            if (t0 + j >= a.tcap)
+                break;
+            float* d = a.trec + (size_t)(t0 + j) * REC_WORDS;
+            V3 rest = st.parts.total - Lb[j];
+            V3 t = thr[j];
+            for (int q = 0; q < 16; q++)
+                d[q] = feat[j][q];
+            d[16] = t.x > 0.0f ? rest.x / t.x : 0.0f;
+            d[17] = t.y > 0.0f ? rest.y / t.y : 0.0f;
+            d[18] = t.z > 0.0f ? rest.z / t.z : 0.0f;
+            d[19] = 0.0f;
+        }
     }
 }
 
@@ -644,12 +672,25 @@ cudaError_t nrc_launch_pack(cudaStream_t s, const float* w, uint8_t* img)
     return cudaGetLastError();
 }
 
-cudaError_t nrc_launch_paths(bool f64, dim3 grid, cudaStream_t s, const vgd::Ctx& c, const NrcPathArgs& a)
+cudaError_t nrc_launch_query_paths(bool f64, dim3 grid, cudaStream_t s, const vgd::Ctx& c, const NrcPathArgs& a)
 {
     if (f64)
-        mk_cache_paths<double><<<grid, 128, 0, s>>>(c, a);
+        mk_cache_query<double><<<grid, 128, 0, s>>>(c, a);
     else
-        mk_cache_paths<float><<<grid, 128, 0, s>>>(c, a);
+        mk_cache_query<float><<<grid, 128, 0, s>>>(c, a);
+    return cudaGetLastError();
+}
+
+cudaError_t nrc_launch_train_paths(bool f64, cudaStream_t s, const vgd::Ctx& c, const NrcPathArgs& a)
+{
+    uint32_t first;
+    uint32_t count = nrc_train_pixels((uint64_t)c.p[P_WIDTH] * c.p[P_HEIGHT], a.train_stride, a.train_offset, &first);
+    if (count == 0)
+        return cudaSuccess;
+    if (f64)
+        mk_cache_train<double><<<(count + 127) / 128, 128, 0, s>>>(c, a, first, count);
+    else
+        mk_cache_train<float><<<(count + 127) / 128, 128, 0, s>>>(c, a, first, count);
     return cudaGetLastError();
 }
 

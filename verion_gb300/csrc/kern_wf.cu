@@ -116,13 +116,13 @@ cudaError_t launch_stream_start(Variant v, cudaStream_t s, const vgd::Ctx& c, co
 {
     unsigned blocks = (w.n + 255) / 256;
     if (v.light && v.f64)
-        vgk::wf_stream_start<true, double><<<blocks, 256, 0, s>>>(c, w);
+        vgk::wf_stream_start<true, double><<<blocks, 256, 0, s>>>(c, w, vgk::CacheWave{});
     else if (v.light)
-        vgk::wf_stream_start<true, float><<<blocks, 256, 0, s>>>(c, w);
+        vgk::wf_stream_start<true, float><<<blocks, 256, 0, s>>>(c, w, vgk::CacheWave{});
     else if (v.f64)
-        vgk::wf_stream_start<false, double><<<blocks, 256, 0, s>>>(c, w);
+        vgk::wf_stream_start<false, double><<<blocks, 256, 0, s>>>(c, w, vgk::CacheWave{});
     else
-        vgk::wf_stream_start<false, float><<<blocks, 256, 0, s>>>(c, w);
+        vgk::wf_stream_start<false, float><<<blocks, 256, 0, s>>>(c, w, vgk::CacheWave{});
     return cudaGetLastError();
 }
 
@@ -170,13 +170,13 @@ cudaError_t launch_stream_tail(Variant v, uint32_t max_slots, cudaStream_t s, co
     if (blocks == 0)
         return cudaSuccess;
     if (v.light && v.f64)
-        vgk::wf_stream_tail<true, double><<<blocks, 128, 0, s>>>(c, w, wave);
+        vgk::wf_stream_tail<true, double><<<blocks, 128, 0, s>>>(c, w, wave, vgk::CacheWave{});
     else if (v.light)
-        vgk::wf_stream_tail<true, float><<<blocks, 128, 0, s>>>(c, w, wave);
+        vgk::wf_stream_tail<true, float><<<blocks, 128, 0, s>>>(c, w, wave, vgk::CacheWave{});
     else if (v.f64)
-        vgk::wf_stream_tail<false, double><<<blocks, 128, 0, s>>>(c, w, wave);
+        vgk::wf_stream_tail<false, double><<<blocks, 128, 0, s>>>(c, w, wave, vgk::CacheWave{});
     else
-        vgk::wf_stream_tail<false, float><<<blocks, 128, 0, s>>>(c, w, wave);
+        vgk::wf_stream_tail<false, float><<<blocks, 128, 0, s>>>(c, w, wave, vgk::CacheWave{});
     return cudaGetLastError();
 }
 
@@ -188,9 +188,55 @@ cudaError_t launch_stream_shade_deferred(bool f64, int blocks, cudaStream_t s, c
                                          uint32_t wave)
 {
     if (f64)
-        vgk::wf_stream_shade_deferred<double><<<blocks, 128, 0, s>>>(c, w, wave);
+        vgk::wf_stream_shade_deferred<double><<<blocks, 128, 0, s>>>(c, w, wave, vgk::CacheWave{});
     else
-        vgk::wf_stream_shade_deferred<float><<<blocks, 128, 0, s>>>(c, w, wave);
+        vgk::wf_stream_shade_deferred<float><<<blocks, 128, 0, s>>>(c, w, wave, vgk::CacheWave{});
+    return cudaGetLastError();
+}
+
+// Radiance-cache frames (lighting split off): start without the training pixels, shade with the
+// cache hook, and the tail with it.
+cudaError_t launch_stream_cache_start(bool f64, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                                      const vgk::CacheWave& q)
+{
+    unsigned blocks = (w.n + 255) / 256;
+    if (f64)
+        vgk::wf_stream_start<false, double, true><<<blocks, 256, 0, s>>>(c, w, q);
+    else
+        vgk::wf_stream_start<false, float, true><<<blocks, 256, 0, s>>>(c, w, q);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_cache_shade(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                                      uint32_t wave, const vgk::CacheWave& q)
+{
+    if (f64)
+        vgk::wf_stream_shade_deferred<double, true><<<blocks, 128, 0, s>>>(c, w, wave, q);
+    else
+        vgk::wf_stream_shade_deferred<float, true><<<blocks, 128, 0, s>>>(c, w, wave, q);
+    return cudaGetLastError();
+}
+
+int stream_cache_shade_blocks_per_sm(bool f64)
+{
+    int n = 0;
+    if (f64)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, vgk::wf_stream_shade_deferred<double, true>, 128, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, vgk::wf_stream_shade_deferred<float, true>, 128, 0);
+    return n > 0 ? n : 1;
+}
+
+cudaError_t launch_stream_cache_tail(bool f64, uint32_t max_slots, cudaStream_t s, const vgd::Ctx& c,
+                                     const vgk::Wave& w, uint32_t wave, const vgk::CacheWave& q)
+{
+    unsigned blocks = (max_slots + 127) / 128;
+    if (blocks == 0)
+        return cudaSuccess;
+    if (f64)
+        vgk::wf_stream_tail<false, double, true><<<blocks, 128, 0, s>>>(c, w, wave, q);
+    else
+        vgk::wf_stream_tail<false, float, true><<<blocks, 128, 0, s>>>(c, w, wave, q);
     return cudaGetLastError();
 }
 

@@ -308,12 +308,14 @@ __device__ __forceinline__ PathState<LIGHT> loadState(const Wave& w, uint32_t p)
 }
 
 // Starts the batch: every pixel that takes a sample (wf_select's test) begins sample params[6].
-template <bool LIGHT, typename A>
-__global__ void __launch_bounds__(256) wf_stream_start(const __grid_constant__ Ctx c, Wave w)
+// With CACHE the training pixels of the frame are left out (a kernel of their own traces them).
+template <bool LIGHT, typename A, bool CACHE = false>
+__global__ void __launch_bounds__(256) wf_stream_start(const __grid_constant__ Ctx c, Wave w, CacheWave q)
 {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     bool live = false;
-    if (p < w.n && c.p[P_SAMPLES_PER_DISPATCH] > 0 && (c.p[P_ADAPTIVE] == 0 || pixelActive<A>(c, p))) {
+    if (p < w.n && c.p[P_SAMPLES_PER_DISPATCH] > 0 && (c.p[P_ADAPTIVE] == 0 || pixelActive<A>(c, p)) &&
+        !(CACHE && (p + q.train_offset) % q.train_stride == 0)) {
         PathState<LIGHT> st = generatePathFor<LIGHT>(c, p % c.p[P_WIDTH], p / c.p[P_WIDTH], c.p[P_SAMPLE]);
         storePath<LIGHT>(w, st, p);
         w.meta[p] = 0;
@@ -417,9 +419,12 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade(cons
 // (w.sreq planes: origin + tmax, direction + flags, contribution); the shadow stage traces it,
 // adds the contribution when unoccluded, and only then finishes, restarts or queues the slot.
 // flags: bit 0 a request is present, bit 1 the path goes on to the next depth.
-template <typename A>
+// With CACHE a path also ends where its spread passes the cache threshold (shadePath's cache
+// hook); it then leaves a query record (one atomic per warp) and finishes like any other.
+template <typename A, bool CACHE = false>
 __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade_deferred(const __grid_constant__ Ctx c,
-                                                                                    Wave w, uint32_t wave)
+                                                                                    Wave w, uint32_t wave,
+                                                                                    CacheWave q)
 {
     uint32_t in = wave & 1u;
     uint32_t count = w.counts[in];
@@ -430,9 +435,14 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade_defe
         if (base >= count)
             break;
         uint32_t i = base + lane_id();
+        bool query = false;
+        uint32_t p = 0, kq = 0;
+        CacheHook hk;
         if (i < count) {
-            uint32_t p = qin[i];
-            uint32_t depth = w.meta[p] & 0xffu;
+            p = qin[i];
+            uint32_t meta = w.meta[p];
+            uint32_t depth = meta & 0xffu;
+            kq = meta >> 8;
             PathState<false> st = loadState<false>(w, p);
             uint4 hr = w.hits[p];
             Hit h;
@@ -441,7 +451,21 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade_defe
             h.prim = hr.z;
             h.t = __uint_as_float(hr.w);
             ShadowReq req;
-            bool alive = shadePath<false, false, true>(c, st, h, depth, p, &req) && depth + 1 < w.depth;
+            if (CACHE) {
+                // The spread starts at zero with each sample (a path may pass a cut-out surface at
+                // depth 0 without meeting the hook).
+                float2 sp = depth > 0 ? q.st[p] : make_float2(0.0f, 0.0f);
+                hk.c = q.spread;
+                hk.train = false;
+                hk.a0 = sp.x;
+                hk.a = sp.y;
+            }
+            bool alive = shadePath<false, false, true, CACHE>(c, st, h, depth, p, &req, &hk) && depth + 1 < w.depth;
+            if (CACHE) {
+                query = hk.query && !bad3(st.parts.total);
+                if (alive)
+                    q.st[p] = make_float2(hk.a0, hk.a);
+            }
             if (alive)
                 storePath<false>(w, st, p);
             else
@@ -452,6 +476,18 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade_defe
                 w.sreq[p] = make_float4(req.o.x, req.o.y, req.o.z, req.tmax);
                 w.sreq[2 * n + p] = make_float4(req.c.x, req.c.y, req.c.z, 0.0f);
             }
+        }
+        if (CACHE && __ballot_sync(FULL, query)) {
+            // Records of sample kq go to range kq (one atomic per sample present in the warp).
+            uint32_t grp = __match_any_sync(FULL, query ? kq : 0xffffffffu);
+            uint32_t leader = __ffs(grp) - 1u;
+            uint32_t first = 0;
+            if (query && lane_id() == leader)
+                first = atomicAdd(q.qcount + kq, __popc(grp));
+            first = __shfl_sync(FULL, first, leader);
+            uint32_t slot = first + __popc(grp & ((1u << lane_id()) - 1u));
+            if (query && slot < q.qcap)
+                cacheQueryRecord(q.qrec + ((size_t)kq * q.qcap + slot) * CACHE_REC_WORDS, hk, p);
         }
         __syncwarp();
     }
@@ -650,10 +686,12 @@ __global__ void __launch_bounds__(128, 8) wf_stream_finish(const __grid_constant
 // The tail of a streaming batch: once few slots are live, one thread per remaining slot runs its
 // path and the rest of its samples to the end, trace and shade in a loop as the megakernel does,
 // instead of one half-empty wave per bounce. Same functions, same order per pixel, same sums.
-template <bool LIGHT, typename A>
+// With CACHE (lighting split off) paths end at the cache as in wf_stream_shade_deferred.
+template <bool LIGHT, typename A, bool CACHE = false>
 __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_tail(const __grid_constant__ Ctx c, Wave w,
-                                                                          uint32_t wave)
+                                                                          uint32_t wave, CacheWave q)
 {
+    static_assert(!(CACHE && LIGHT), "the cache runs with the lighting split off");
     uint32_t in = wave & 1u;
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.counts[in])
@@ -663,16 +701,32 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_tail(const
     uint32_t depth = meta & 0xffu, k = meta >> 8;
     uint32_t batch = c.p[P_SAMPLES_PER_DISPATCH];
     PathState<LIGHT> st = loadState<LIGHT>(w, p);
+    CacheHook hk;
+    if (CACHE) {
+        float2 sp = depth > 0 ? q.st[p] : make_float2(0.0f, 0.0f);
+        hk.c = q.spread;
+        hk.train = false;
+        hk.a0 = sp.x;
+        hk.a = sp.y;
+    }
     for (;;) {
-        if (shadePath<LIGHT, false>(c, st, traceClosest(c, st.org, st.dir), depth, p) && depth + 1 < w.depth) {
+        if (shadePath<LIGHT, false, false, CACHE>(c, st, traceClosest(c, st.org, st.dir), depth, p, nullptr, &hk) &&
+            depth + 1 < w.depth) {
             depth++;
             continue;
+        }
+        if (CACHE && hk.query && !bad3(st.parts.total)) {
+            uint32_t slot = atomicAdd(q.qcount + k, 1u);
+            if (slot < q.qcap)
+                cacheQueryRecord(q.qrec + ((size_t)k * q.qcap + slot) * CACHE_REC_WORDS, hk, p);
         }
         finishPath<LIGHT, A>(c, st, p);
         if (k + 1 < batch && (c.p[P_ADAPTIVE] == 0 || pixelActive<A>(c, p))) {
             k++;
             depth = 0;
             st = generatePathFor<LIGHT>(c, p % c.p[P_WIDTH], p / c.p[P_WIDTH], c.p[P_SAMPLE] + k);
+            if (CACHE)
+                hk.a0 = hk.a = 0.0f;
             continue;
         }
         break;

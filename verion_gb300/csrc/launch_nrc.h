@@ -26,6 +26,14 @@ struct NrcPathArgs {
 
 namespace vgx {
 
+// Training pixels of a frame: those with (pixel + offset) % stride == 0 among px pixels; the
+// smallest is *first, the others follow every `stride` pixels.
+inline uint32_t nrc_train_pixels(uint64_t px, uint32_t stride, uint32_t offset, uint32_t* first)
+{
+    *first = (stride - offset % stride) % stride;
+    return *first < px ? (uint32_t)((px - 1 - *first) / stride + 1) : 0u;
+}
+
 // Sets the cache kernels' shared-memory limits (once; before any stream capture).
 void nrc_prepare();
 
@@ -44,6 +52,8 @@ cudaError_t nrc_launch_adam(cudaStream_t s, float* p, float* g, float* m, float*
 cudaError_t nrc_launch_step(cudaStream_t s, uint32_t* step);
 cudaError_t nrc_launch_to_half(cudaStream_t s, const float* p, void* out, size_t n);
 cudaError_t nrc_launch_pack(cudaStream_t s, const float* w, uint8_t* img);
-cudaError_t nrc_launch_paths(bool f64, dim3 grid, cudaStream_t s, const vgd::Ctx& c, const NrcPathArgs& a);
+// Query paths over the 16 x 8 pixel tiles of `grid`; the training paths of the frame.
+cudaError_t nrc_launch_query_paths(bool f64, dim3 grid, cudaStream_t s, const vgd::Ctx& c, const NrcPathArgs& a);
+cudaError_t nrc_launch_train_paths(bool f64, cudaStream_t s, const vgd::Ctx& c, const NrcPathArgs& a);
 
 } // namespace vgx

@@ -956,6 +956,32 @@ struct CacheHook {
     V3 L;           // path radiance after the vertex's emission
 };
 
+// Query / training record of a cache vertex: position, outgoing direction, normal, roughness,
+// albedo, metallic, transmission, one spare word; then three words (throughput or target) and a
+// fourth (pixel of a query).
+constexpr uint32_t CACHE_REC_WORDS = 20;
+
+__device__ __forceinline__ void cacheFeatures(float* d, const CacheHook& hk)
+{
+    d[0] = hk.pos.x, d[1] = hk.pos.y, d[2] = hk.pos.z;
+    d[3] = hk.wo.x, d[4] = hk.wo.y, d[5] = hk.wo.z;
+    d[6] = hk.n.x, d[7] = hk.n.y, d[8] = hk.n.z;
+    d[9] = hk.rough;
+    d[10] = hk.albedo.x, d[11] = hk.albedo.y, d[12] = hk.albedo.z;
+    d[13] = hk.metallic;
+    d[14] = hk.transmission;
+    d[15] = 0.0f;
+}
+
+// The query record of a path that ended at the cache: features, the throughput arriving at the
+// vertex, and the pixel the cache's answer is added to.
+__device__ __forceinline__ void cacheQueryRecord(float* d, const CacheHook& hk, uint32_t pixel)
+{
+    cacheFeatures(d, hk);
+    d[16] = hk.thr.x, d[17] = hk.thr.y, d[18] = hk.thr.z;
+    d[19] = __uint_as_float(pixel);
+}
+
 template <bool LIGHT, bool RESTIR, bool DEFER = false, bool CACHE = false>
 __device__ bool shadePath(const Ctx& c, PathState<LIGHT>& st, Hit hq, uint32_t depth, uint32_t pixel,
                           ShadowReq* req = nullptr, CacheHook* hk = nullptr)

@@ -137,6 +137,215 @@ void bind_tables(VgRenderer* r)
 
 } // namespace
 
+// Streaming wavefront over `samples` samples per pixel from sample0 (kernels.cuh): the start, waves
+// until no slot is live (the host reads each wave's live count LAG waves later, so the GPU never
+// idles on the poll) and a tail launch once few slots are live. With `q` the radiance-cache
+// variants run (lighting split off, shadow rays always in their own stage).
+int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, const vgk::Wave& w, uint32_t sample0,
+                   uint32_t samples, bool timed, EventPool& pool, StageEvents& stages, const vgk::CacheWave* q)
+{
+    cudaStream_t s = r->ctx->stream;
+    int st;
+    int eb = blocks_for(r, r->extend_blocks);
+    acc->wave_live.clear();
+    acc->wave_ms.clear();
+    acc->tail_ms = 0.0f;
+    int svi = v.index() & 5;
+    if (r->stream_shade_blocks[svi] == 0)
+        r->stream_shade_blocks[svi] = vgx::stream_shade_blocks_per_sm(v);
+    int ssb = blocks_for(r, r->stream_shade_blocks[svi]);
+    // Lighting split off: three-stage waves with the shadow rays in their own kernel.
+    bool deferred = (!acc->lighting && r->defer_shadows) || q;
+    if (deferred && r->deferred_blocks[v.f64 ? 1 : 0] == 0)
+        r->deferred_blocks[v.f64 ? 1 : 0] =
+            vgx::stream_deferred_blocks_per_sm(v.f64, &r->shadow_blocks[v.f64 ? 1 : 0]);
+    int dsb = blocks_for(r, r->deferred_blocks[v.f64 ? 1 : 0]);
+    int csb = 0;
+    if (q) {
+        if (r->cache_shade_blocks[v.f64 ? 1 : 0] == 0)
+            r->cache_shade_blocks[v.f64 ? 1 : 0] = vgx::stream_cache_shade_blocks_per_sm(v.f64);
+        csb = blocks_for(r, r->cache_shade_blocks[v.f64 ? 1 : 0]);
+    }
+    int shb = blocks_for(r, r->shadow_blocks[v.f64 ? 1 : 0]);
+    acc->wave_stages = deferred ? 3 : 2;
+    c.p[P_SAMPLE] = sample0;
+    c.p[P_SAMPLES_PER_DISPATCH] = samples;
+    VG_CHECK(cudaMemsetAsync(acc->counts.p, 0, 2 * 4, s), "counters");
+    VG_CHECK(cudaMemsetAsync(acc->fetch.p, 0, 4 * 4, s), "counters");
+    VG_CHECK((q ? vgx::launch_stream_cache_start(v.f64, s, c, w, *q) : vgx::launch_stream_start(v, s, c, w)), "stream start launch");
+    acc->launches++;
+    // Waves until no slot is live. The host reads each wave's output count LAG waves later,
+    // so the GPU never idles on the poll; extra waves on an empty queue exit at once.
+    const uint32_t LAG = 2, RING = 64;
+    uint64_t max_waves = (uint64_t)samples * r->max_depth + LAG + 1;
+    uint32_t* ring = acc->host_counts;
+    std::vector<cudaEvent_t> ring_ev(RING);
+    for (auto& e : ring_ev)
+        e = pool.get();
+    bool done = false;
+    uint64_t wave = 0;
+    if (r->graph_waves > 0 && !timed) {
+        // Captured chunks of graph_waves waves (even, so the queue parity of every wave in a
+        // replay matches its place in the sequence), each ending with the live count.
+        uint32_t K = r->graph_waves;
+        VG_CHECK(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed), "graph capture");
+        cudaError_t ce = cudaSuccess;
+        for (uint32_t i = 0; i < K && ce == cudaSuccess; i++) {
+            ce = r->dynamic_fetch ? vgx::launch_stream_extend_dyn(r->traversal_stats, eb, s, c, w, i)
+                                  : vgx::launch_stream_extend(r->traversal_stats, eb, s, c, w, i);
+            if (ce == cudaSuccess && deferred) {
+                ce = (q ? vgx::launch_stream_cache_shade(v.f64, csb, s, c, w, i, *q) : vgx::launch_stream_shade_deferred(v.f64, dsb, s, c, w, i));
+                if (ce == cudaSuccess && r->dynamic_fetch && r->ds.shadow_any) {
+                    ce = vgx::launch_stream_shadow_trace(shb, s, c, w, i);
+                    if (ce == cudaSuccess)
+                        ce = vgx::launch_stream_finish(v.f64, shb, s, c, w, i);
+                } else if (ce == cudaSuccess)
+                    ce = vgx::launch_stream_shadow(v.f64, shb, s, c, w, i);
+            } else if (ce == cudaSuccess)
+                ce = vgx::launch_stream_shade(v, ssb, s, c, w, i);
+        }
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync(&ring[0], (uint32_t*)acc->counts.p + (K & 1u), 4, cudaMemcpyDeviceToHost, s);
+        cudaGraph_t g = nullptr;
+        cudaError_t ee = cudaStreamEndCapture(s, &g);
+        if (ce != cudaSuccess || ee != cudaSuccess) {
+            if (g)
+                cudaGraphDestroy(g);
+            return cuda_fail(ce != cudaSuccess ? ce : ee, "wave graph capture");
+        }
+        cudaGraphExec_t ge = nullptr;
+        ce = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess)
+            return cuda_fail(ce, "wave graph instantiation");
+        uint32_t per_wave = deferred ? (r->dynamic_fetch && r->ds.shadow_any ? 4 : 3) : 2;
+        uint64_t max_rep = (max_waves + K - 1) / K + 2;
+        uint64_t rep = 0;
+        for (; rep < max_rep && !done; rep++) {
+            ce = cudaGraphLaunch(ge, s);
+            if (ce == cudaSuccess)
+                ce = cudaEventRecord(ring_ev[rep & 1u], s);
+            if (ce != cudaSuccess) {
+                cudaGraphExecDestroy(ge);
+                return cuda_fail(ce, "wave graph launch");
+            }
+            acc->launches += (uint64_t)K * per_wave;
+            if (rep >= 1) {
+                if ((st = wait_event(ring_ev[(rep - 1) & 1u])) != VG_OK) {
+                    cudaGraphExecDestroy(ge);
+                    return st;
+                }
+                // The count of the last replay that finished (a later one may have overwritten
+                // it with a smaller count: live counts never grow).
+                uint32_t live = ring[0];
+                acc->wave_live.push_back(live);
+                done = live == 0;
+                if (!done && live <= r->tail_threshold) {
+                    ce = (q ? vgx::launch_stream_cache_tail(v.f64, live, s, c, w, (uint32_t)((rep + 1) * K), *q) : vgx::launch_stream_tail(v, live, s, c, w, (uint32_t)((rep + 1) * K)));
+                    if (ce != cudaSuccess) {
+                        cudaGraphExecDestroy(ge);
+                        return cuda_fail(ce, "tail launch");
+                    }
+                    acc->launches++;
+                    done = true;
+                }
+            }
+        }
+        wave = rep * K;
+        VG_CHECK(cudaStreamSynchronize(s), "waves");
+        cudaGraphExecDestroy(ge);
+        if (!done && ring[0] != 0)
+            return fail(VG_ERR_KERNEL, "streaming wavefront did not drain within its wave bound");
+        done = true;
+    }
+    for (; wave < max_waves && !done; wave++) {
+        cudaEvent_t a = nullptr, m = nullptr, b = nullptr;
+        if (timed) {
+            a = pool.get();
+            m = pool.get();
+            b = pool.get();
+            VG_CHECK(cudaEventRecord(a, s), "event");
+        }
+        if (r->dynamic_fetch)
+            VG_CHECK(vgx::launch_stream_extend_dyn(r->traversal_stats, eb, s, c, w, (uint32_t)wave),
+                     "extend launch");
+        else
+            VG_CHECK(vgx::launch_stream_extend(r->traversal_stats, eb, s, c, w, (uint32_t)wave),
+                     "extend launch");
+        if (timed)
+            VG_CHECK(cudaEventRecord(m, s), "event");
+        if (deferred) {
+            VG_CHECK((q ? vgx::launch_stream_cache_shade(v.f64, csb, s, c, w, (uint32_t)wave, *q) : vgx::launch_stream_shade_deferred(v.f64, dsb, s, c, w, (uint32_t)wave)), "shade launch");
+            cudaEvent_t q = nullptr;
+            if (timed) {
+                q = pool.get();
+                VG_CHECK(cudaEventRecord(q, s), "event");
+            }
+            if (r->dynamic_fetch && r->ds.shadow_any) {
+                VG_CHECK(vgx::launch_stream_shadow_trace(shb, s, c, w, (uint32_t)wave), "shadow launch");
+                VG_CHECK(vgx::launch_stream_finish(v.f64, shb, s, c, w, (uint32_t)wave), "finish launch");
+                acc->launches++;
+            } else {
+                VG_CHECK(vgx::launch_stream_shadow(v.f64, shb, s, c, w, (uint32_t)wave), "shadow launch");
+            }
+            if (timed) {
+                VG_CHECK(cudaEventRecord(b, s), "event");
+                stages.push_back({0, {a, m}});
+                stages.push_back({1, {m, q}});
+                stages.push_back({3, {q, b}});
+            }
+            acc->launches += 3;
+        } else {
+            VG_CHECK(vgx::launch_stream_shade(v, ssb, s, c, w, (uint32_t)wave), "shade launch");
+            if (timed) {
+                VG_CHECK(cudaEventRecord(b, s), "event");
+                stages.push_back({0, {a, m}});
+                stages.push_back({1, {m, b}});
+            }
+            acc->launches += 2;
+        }
+        uint32_t slot = (uint32_t)(wave % RING);
+        VG_CHECK(cudaMemcpyAsync(&ring[slot], (uint32_t*)acc->counts.p + ((wave + 1) & 1u), 4,
+                                 cudaMemcpyDeviceToHost, s),
+                 "count readback");
+        VG_CHECK(cudaEventRecord(ring_ev[slot], s), "event");
+        if (wave >= LAG) {
+            uint32_t old = (uint32_t)((wave - LAG) % RING);
+            if ((st = wait_event(ring_ev[old])) != VG_OK)
+                return st;
+            uint32_t live = ring[old];
+            done = live == 0;
+            acc->wave_live.push_back(live);
+            if (!done && live <= r->tail_threshold) {
+                // Few slots left: finish them in one launch (the queue after this wave).
+                cudaEvent_t a = nullptr, b = nullptr;
+                if (timed) {
+                    a = pool.get();
+                    b = pool.get();
+                    VG_CHECK(cudaEventRecord(a, s), "event");
+                }
+                VG_CHECK((q ? vgx::launch_stream_cache_tail(v.f64, live, s, c, w, (uint32_t)(wave + 1), *q) : vgx::launch_stream_tail(v, live, s, c, w, (uint32_t)(wave + 1))), "tail launch");
+                if (timed) {
+                    VG_CHECK(cudaEventRecord(b, s), "event");
+                    stages.push_back({2, {a, b}});
+                }
+                acc->launches++;
+                done = true;
+            }
+        }
+    }
+    acc->last_waves = (uint32_t)wave;
+    VG_CHECK(cudaStreamSynchronize(s), "waves");
+    for (uint64_t k = wave > LAG ? wave - LAG + 1 : 0; k < wave; k++)
+        acc->wave_live.push_back(ring[k % RING]);
+    if (!done) {
+        VG_CHECK(cudaStreamSynchronize(s), "waves");
+        if (ring[(wave - 1) % RING] != 0)
+            return fail(VG_ERR_KERNEL, "streaming wavefront did not drain within its wave bound");
+    }
+    return VG_OK;
+}
+
 extern "C" {
 
 
@@ -191,6 +400,14 @@ void vg_context_destroy(VgContext* ctx)
         return;
     cudaStreamSynchronize(ctx->stream);
     cudaStreamDestroy(ctx->stream);
+    if (ctx->side) {
+        cudaStreamSynchronize(ctx->side);
+        cudaStreamDestroy(ctx->side);
+    }
+    if (ctx->fork)
+        cudaEventDestroy(ctx->fork);
+    if (ctx->join)
+        cudaEventDestroy(ctx->join);
     delete ctx;
 }
 
@@ -680,7 +897,7 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
         return fail(VG_ERR_SCENE, "ReSTIR was switched mid-accumulation; start a new accumulation");
     bool wavefront = r->integrator == VG_WAVEFRONT && !r->cache;
     const uint32_t max_depth_alloc = 64;
-    if (wavefront && !acc->state.p) {
+    if (r->integrator == VG_WAVEFRONT && !acc->state.p) {
         uint32_t planes = vgk::BASE_PLANES + (acc->lighting ? vgk::SPLIT_PLANES : 0);
         if ((st = alloc(acc->state, px * planes * 16, s, false)) != VG_OK ||
             (st = alloc(acc->hits, px * 16, s, false)) != VG_OK ||
@@ -703,13 +920,16 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
     vgx::Variant v = variant_of(r, acc);
     EventPool pool;
     cudaEvent_t t0 = pool.get(), t1 = pool.get();
-    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> stages;
+    StageEvents stages;
     bool timed = r->stage_timing && wavefront;
     VG_CHECK(cudaMemsetAsync(r->err.p, 0, 4, s), "error flag");
     VG_CHECK(cudaEventRecord(t0, s), "event");
     bool streamed = false;
     if (r->cache) {
-        if ((st = cache_accumulate(r, acc, c, samples, r->stage_timing)) != VG_OK)
+        vgk::Wave w = wave_of(r, acc);
+        c.p[P_WF_PATHS] = (uint32_t)px;
+        if ((st = cache_accumulate(r, acc, c, samples, r->stage_timing,
+                                   r->integrator == VG_WAVEFRONT ? &w : nullptr)) != VG_OK)
             return st;
     } else if (!wavefront) {
         dim3 grid((acc->width + 15) / 16, (acc->height + 7) / 8);
@@ -722,219 +942,18 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
             acc->launches++;
         }
     } else {
-        vgk::Wave w;
-        uint32_t planes = vgk::BASE_PLANES + (acc->lighting ? vgk::SPLIT_PLANES : 0);
-        (void)planes;
-        w.state = (float4*)acc->state.p;
-        w.hits = (uint4*)acc->hits.p;
-        w.queue[0] = (uint32_t*)acc->queue[0].p;
-        w.queue[1] = (uint32_t*)acc->queue[1].p;
-        w.counts = (uint32_t*)acc->counts.p;
-        w.fetch = (uint32_t*)acc->fetch.p;
-        w.tstats = (unsigned long long*)acc->tstats.p;
-        w.n = (uint32_t)px;
-        w.depth = r->max_depth;
+        vgk::Wave w = wave_of(r, acc);
         c.p[P_WF_PATHS] = (uint32_t)px;
         int vi = v.index();
         if (r->shade_blocks[vi] == 0)
             r->shade_blocks[vi] = vgx::wf_shade_blocks_per_sm(v);
         int eb = blocks_for(r, r->extend_blocks);
         int sb = blocks_for(r, r->shade_blocks[vi]);
-        w.meta = (uint32_t*)acc->meta.p;
         bool streaming = r->wavefront_mode == VG_WAVEFRONT_STREAMING && !acc->restir.on;
         if (streaming && samples > 0) {
             streamed = true;
-            acc->wave_live.clear();
-            acc->wave_ms.clear();
-            acc->tail_ms = 0.0f;
-            int svi = v.index() & 5;
-            if (r->stream_shade_blocks[svi] == 0)
-                r->stream_shade_blocks[svi] = vgx::stream_shade_blocks_per_sm(v);
-            int ssb = blocks_for(r, r->stream_shade_blocks[svi]);
-            // Lighting split off: three-stage waves with the shadow rays in their own kernel.
-            bool deferred = !acc->lighting && r->defer_shadows;
-            if (deferred && r->deferred_blocks[v.f64 ? 1 : 0] == 0)
-                r->deferred_blocks[v.f64 ? 1 : 0] =
-                    vgx::stream_deferred_blocks_per_sm(v.f64, &r->shadow_blocks[v.f64 ? 1 : 0]);
-            int dsb = blocks_for(r, r->deferred_blocks[v.f64 ? 1 : 0]);
-            int shb = blocks_for(r, r->shadow_blocks[v.f64 ? 1 : 0]);
-            w.sreq = (float4*)acc->sreq.p;
-            acc->wave_stages = deferred ? 3 : 2;
-            c.p[P_SAMPLE] = acc->samples;
-            c.p[P_SAMPLES_PER_DISPATCH] = samples;
-            VG_CHECK(cudaMemsetAsync(acc->counts.p, 0, 2 * 4, s), "counters");
-            VG_CHECK(cudaMemsetAsync(acc->fetch.p, 0, 4 * 4, s), "counters");
-            VG_CHECK(vgx::launch_stream_start(v, s, c, w), "stream start launch");
-            acc->launches++;
-            // Waves until no slot is live. The host reads each wave's output count LAG waves later,
-            // so the GPU never idles on the poll; extra waves on an empty queue exit at once.
-            const uint32_t LAG = 2, RING = 64;
-            uint64_t max_waves = (uint64_t)samples * r->max_depth + LAG + 1;
-            uint32_t* ring = acc->host_counts;
-            std::vector<cudaEvent_t> ring_ev(RING);
-            for (auto& e : ring_ev)
-                e = pool.get();
-            bool done = false;
-            uint64_t wave = 0;
-            if (r->graph_waves > 0 && !timed) {
-                // Captured chunks of graph_waves waves (even, so the queue parity of every wave in a
-                // replay matches its place in the sequence), each ending with the live count.
-                uint32_t K = r->graph_waves;
-                VG_CHECK(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed), "graph capture");
-                cudaError_t ce = cudaSuccess;
-                for (uint32_t i = 0; i < K && ce == cudaSuccess; i++) {
-                    ce = r->dynamic_fetch ? vgx::launch_stream_extend_dyn(r->traversal_stats, eb, s, c, w, i)
-                                          : vgx::launch_stream_extend(r->traversal_stats, eb, s, c, w, i);
-                    if (ce == cudaSuccess && deferred) {
-                        ce = vgx::launch_stream_shade_deferred(v.f64, dsb, s, c, w, i);
-                        if (ce == cudaSuccess && r->dynamic_fetch && r->ds.shadow_any) {
-                            ce = vgx::launch_stream_shadow_trace(shb, s, c, w, i);
-                            if (ce == cudaSuccess)
-                                ce = vgx::launch_stream_finish(v.f64, shb, s, c, w, i);
-                        } else if (ce == cudaSuccess)
-                            ce = vgx::launch_stream_shadow(v.f64, shb, s, c, w, i);
-                    } else if (ce == cudaSuccess)
-                        ce = vgx::launch_stream_shade(v, ssb, s, c, w, i);
-                }
-                if (ce == cudaSuccess)
-                    ce = cudaMemcpyAsync(&ring[0], (uint32_t*)acc->counts.p + (K & 1u), 4, cudaMemcpyDeviceToHost, s);
-                cudaGraph_t g = nullptr;
-                cudaError_t ee = cudaStreamEndCapture(s, &g);
-                if (ce != cudaSuccess || ee != cudaSuccess) {
-                    if (g)
-                        cudaGraphDestroy(g);
-                    return cuda_fail(ce != cudaSuccess ? ce : ee, "wave graph capture");
-                }
-                cudaGraphExec_t ge = nullptr;
-                ce = cudaGraphInstantiate(&ge, g, 0);
-                cudaGraphDestroy(g);
-                if (ce != cudaSuccess)
-                    return cuda_fail(ce, "wave graph instantiation");
-                uint32_t per_wave = deferred ? (r->dynamic_fetch && r->ds.shadow_any ? 4 : 3) : 2;
-                uint64_t max_rep = (max_waves + K - 1) / K + 2;
-                uint64_t rep = 0;
-                for (; rep < max_rep && !done; rep++) {
-                    ce = cudaGraphLaunch(ge, s);
-                    if (ce == cudaSuccess)
-                        ce = cudaEventRecord(ring_ev[rep & 1u], s);
-                    if (ce != cudaSuccess) {
-                        cudaGraphExecDestroy(ge);
-                        return cuda_fail(ce, "wave graph launch");
-                    }
-                    acc->launches += (uint64_t)K * per_wave;
-                    if (rep >= 1) {
-                        if ((st = wait_event(ring_ev[(rep - 1) & 1u])) != VG_OK) {
-                            cudaGraphExecDestroy(ge);
-                            return st;
-                        }
-                        // The count of the last replay that finished (a later one may have overwritten
-                        // it with a smaller count: live counts never grow).
-                        uint32_t live = ring[0];
-                        acc->wave_live.push_back(live);
-                        done = live == 0;
-                        if (!done && live <= r->tail_threshold) {
-                            ce = vgx::launch_stream_tail(v, live, s, c, w, (uint32_t)((rep + 1) * K));
-                            if (ce != cudaSuccess) {
-                                cudaGraphExecDestroy(ge);
-                                return cuda_fail(ce, "tail launch");
-                            }
-                            acc->launches++;
-                            done = true;
-                        }
-                    }
-                }
-                wave = rep * K;
-                VG_CHECK(cudaStreamSynchronize(s), "waves");
-                cudaGraphExecDestroy(ge);
-                if (!done && ring[0] != 0)
-                    return fail(VG_ERR_KERNEL, "streaming wavefront did not drain within its wave bound");
-                done = true;
-            }
-            for (; wave < max_waves && !done; wave++) {
-                cudaEvent_t a = nullptr, m = nullptr, b = nullptr;
-                if (timed) {
-                    a = pool.get();
-                    m = pool.get();
-                    b = pool.get();
-                    VG_CHECK(cudaEventRecord(a, s), "event");
-                }
-                if (r->dynamic_fetch)
-                    VG_CHECK(vgx::launch_stream_extend_dyn(r->traversal_stats, eb, s, c, w, (uint32_t)wave),
-                             "extend launch");
-                else
-                    VG_CHECK(vgx::launch_stream_extend(r->traversal_stats, eb, s, c, w, (uint32_t)wave),
-                             "extend launch");
-                if (timed)
-                    VG_CHECK(cudaEventRecord(m, s), "event");
-                if (deferred) {
-                    VG_CHECK(vgx::launch_stream_shade_deferred(v.f64, dsb, s, c, w, (uint32_t)wave), "shade launch");
-                    cudaEvent_t q = nullptr;
-                    if (timed) {
-                        q = pool.get();
-                        VG_CHECK(cudaEventRecord(q, s), "event");
-                    }
-                    if (r->dynamic_fetch && r->ds.shadow_any) {
-                        VG_CHECK(vgx::launch_stream_shadow_trace(shb, s, c, w, (uint32_t)wave), "shadow launch");
-                        VG_CHECK(vgx::launch_stream_finish(v.f64, shb, s, c, w, (uint32_t)wave), "finish launch");
-                        acc->launches++;
-                    } else {
-                        VG_CHECK(vgx::launch_stream_shadow(v.f64, shb, s, c, w, (uint32_t)wave), "shadow launch");
-                    }
-                    if (timed) {
-                        VG_CHECK(cudaEventRecord(b, s), "event");
-                        stages.push_back({0, {a, m}});
-                        stages.push_back({1, {m, q}});
-                        stages.push_back({3, {q, b}});
-                    }
-                    acc->launches += 3;
-                } else {
-                    VG_CHECK(vgx::launch_stream_shade(v, ssb, s, c, w, (uint32_t)wave), "shade launch");
-                    if (timed) {
-                        VG_CHECK(cudaEventRecord(b, s), "event");
-                        stages.push_back({0, {a, m}});
-                        stages.push_back({1, {m, b}});
-                    }
-                    acc->launches += 2;
-                }
-                uint32_t slot = (uint32_t)(wave % RING);
-                VG_CHECK(cudaMemcpyAsync(&ring[slot], (uint32_t*)acc->counts.p + ((wave + 1) & 1u), 4,
-                                         cudaMemcpyDeviceToHost, s),
-                         "count readback");
-                VG_CHECK(cudaEventRecord(ring_ev[slot], s), "event");
-                if (wave >= LAG) {
-                    uint32_t old = (uint32_t)((wave - LAG) % RING);
-                    if ((st = wait_event(ring_ev[old])) != VG_OK)
-                        return st;
-                    uint32_t live = ring[old];
-                    done = live == 0;
-                    acc->wave_live.push_back(live);
-                    if (!done && live <= r->tail_threshold) {
-                        // Few slots left: finish them in one launch (the queue after this wave).
-                        cudaEvent_t a = nullptr, b = nullptr;
-                        if (timed) {
-                            a = pool.get();
-                            b = pool.get();
-                            VG_CHECK(cudaEventRecord(a, s), "event");
-                        }
-                        VG_CHECK(vgx::launch_stream_tail(v, live, s, c, w, (uint32_t)(wave + 1)), "tail launch");
-                        if (timed) {
-                            VG_CHECK(cudaEventRecord(b, s), "event");
-                            stages.push_back({2, {a, b}});
-                        }
-                        acc->launches++;
-                        done = true;
-                    }
-                }
-            }
-            acc->last_waves = (uint32_t)wave;
-            VG_CHECK(cudaStreamSynchronize(s), "waves");
-            for (uint64_t k = wave > LAG ? wave - LAG + 1 : 0; k < wave; k++)
-                acc->wave_live.push_back(ring[k % RING]);
-            if (!done) {
-                VG_CHECK(cudaStreamSynchronize(s), "waves");
-                if (ring[(wave - 1) % RING] != 0)
-                    return fail(VG_ERR_KERNEL, "streaming wavefront did not drain within its wave bound");
-            }
+            if ((st = stream_samples(r, acc, c, v, w, acc->samples, samples, timed, pool, stages, nullptr)) != VG_OK)
+                return st;
         }
         for (uint32_t k = 0; k < (streaming ? 0u : samples); k++) {
             c.p[P_SAMPLE] = acc->samples + k;
