@@ -276,10 +276,10 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
             VG_CHECK(cudaEventRecord(m, s), "event");
         if (deferred) {
             VG_CHECK((q ? vgx::launch_stream_cache_shade(v.f64, csb, s, c, w, (uint32_t)wave, *q) : vgx::launch_stream_shade_deferred(v.f64, dsb, s, c, w, (uint32_t)wave)), "shade launch");
-            cudaEvent_t q = nullptr;
+            cudaEvent_t qe = nullptr;
             if (timed) {
-                q = pool.get();
-                VG_CHECK(cudaEventRecord(q, s), "event");
+                qe = pool.get();
+                VG_CHECK(cudaEventRecord(qe, s), "event");
             }
             if (r->dynamic_fetch && r->ds.shadow_any) {
                 VG_CHECK(vgx::launch_stream_shadow_trace(shb, s, c, w, (uint32_t)wave), "shadow launch");
@@ -291,8 +291,8 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
             if (timed) {
                 VG_CHECK(cudaEventRecord(b, s), "event");
                 stages.push_back({0, {a, m}});
-                stages.push_back({1, {m, q}});
-                stages.push_back({3, {q, b}});
+                stages.push_back({1, {m, qe}});
+                stages.push_back({3, {qe, b}});
             }
             acc->launches += 3;
         } else {
