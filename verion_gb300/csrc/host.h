@@ -139,7 +139,7 @@ constexpr uint32_t MAX_CACHE_FRAME = 16; // samples per radiance-cache frame at 
 struct VgRenderer {
     VgContext* ctx = nullptr;
     DevBuf positions, indices, uvs, vnormals, instances, materials, lights, emitters, emit_cdf, env_pixels,
-        env_marginal, env_cond, texels, tex_info, nodes, tris, err, scratch;
+        env_marginal, env_cond, env_guide, texels, tex_info, nodes, tris, err, scratch;
     vgd::DeviceScene ds{};
     VgSceneInfo info{};
     VgView view{};

@@ -235,12 +235,16 @@ static __device__ __forceinline__ float envPdf(const Ctx& c, V3 d)
     return lum(envTexel(c, i, j)) * pf(c, P_ENV_PDF_SCALE);
 }
 
-// pt_core.slang:274-306
+// pt_core.slang:274-306. Each CDF search is the reference's: the first entry >= u (the last entry
+// when none is); it starts from the guide table's range for u's bucket, which holds that entry, so
+// it ends at the same one after a few steps instead of log2(n).
 static __device__ __noinline__ V3 envSample(const Ctx& c, float u1, float u2, float u3, float u4, float& pdf, V3& le)
 {
     uint32_t w = c.p[P_ENV_W];
     uint32_t h = c.p[P_ENV_H];
-    uint32_t lo = 0, hi = h - 1;
+    const uint32_t* g = c.s.env_guide;
+    uint32_t k = min((uint32_t)(u1 * (float)ENV_GUIDE_M), ENV_GUIDE_M - 1);
+    uint32_t lo = g[k], hi = g[k + 1];
     while (lo < hi) {
         uint32_t mid = (lo + hi) / 2;
         if (fget(c.s.env_marginal, mid) >= u1)
@@ -249,8 +253,10 @@ static __device__ __noinline__ V3 envSample(const Ctx& c, float u1, float u2, fl
             lo = mid + 1;
     }
     uint32_t j = lo;
-    lo = 0;
-    hi = w - 1;
+    const uint32_t* gr = g + (ENV_GUIDE_M + 1) + j * (ENV_GUIDE_C + 1);
+    k = min((uint32_t)(u2 * (float)ENV_GUIDE_C), ENV_GUIDE_C - 1);
+    lo = gr[k];
+    hi = gr[k + 1];
     while (lo < hi) {
         uint32_t mid = (lo + hi) / 2;
         if (fget(c.s.env_cond, j * w + mid) >= u2)

@@ -95,6 +95,40 @@ bool translucent_materials(const VgPacked* pk)
     return false;
 }
 
+// The environment CDF search (pt_core.slang:274-306): the first of the n entries >= u, the last
+// when none is.
+uint32_t cdf_search(const float* cdf, uint32_t n, float u)
+{
+    uint32_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) / 2;
+        if (cdf[mid] >= u)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    return lo;
+}
+
+// Guide tables of the environment's CDF searches (vgd::ENV_GUIDE_M / ENV_GUIDE_C, ctx.h): entry k
+// of a table is the search's answer for u = k / K. The CDFs are non-decreasing, so the answer for
+// any u of bucket k lies between entries k and k + 1.
+std::vector<uint32_t> env_guide(const VgPacked* pk)
+{
+    uint32_t w = pk->info.env_width, h = pk->info.env_height;
+    if (w == 0 || h == 0)
+        return std::vector<uint32_t>(vgd::ENV_GUIDE_M + 1, 0u);
+    std::vector<uint32_t> g((vgd::ENV_GUIDE_M + 1) + (size_t)h * (vgd::ENV_GUIDE_C + 1));
+    for (uint32_t k = 0; k <= vgd::ENV_GUIDE_M; k++)
+        g[k] = cdf_search(pk->env_marginal, h, (float)k / (float)vgd::ENV_GUIDE_M);
+    for (uint32_t j = 0; j < h; j++) {
+        uint32_t* row = g.data() + (vgd::ENV_GUIDE_M + 1) + (size_t)j * (vgd::ENV_GUIDE_C + 1);
+        for (uint32_t k = 0; k <= vgd::ENV_GUIDE_C; k++)
+            row[k] = cdf_search(pk->env_conditional + (size_t)j * w, w, (float)k / (float)vgd::ENV_GUIDE_C);
+    }
+    return g;
+}
+
 // FNV-1a over two tables: whether a re-packed table differs from the uploaded one.
 uint64_t table_key(const void* a, size_t a_len, const void* b, size_t b_len)
 {
@@ -127,6 +161,7 @@ void bind_tables(VgRenderer* r)
     r->ds.env_pixels = (const float*)r->env_pixels.p;
     r->ds.env_marginal = (const float*)r->env_marginal.p;
     r->ds.env_cond = (const float*)r->env_cond.p;
+    r->ds.env_guide = (const uint32_t*)r->env_guide.p;
     r->ds.uvs = (const float*)r->uvs.p;
     r->ds.texels = (const float*)r->texels.p;
     r->ds.tex_info = (const uint32_t*)r->tex_info.p;
@@ -463,6 +498,10 @@ int vg_renderer_create(VgContext* ctx, const VgPacked* pk, VgRenderer** out)
     UP(env_pixels, pk->env_pixels, pk->env_pixels_len * 4);
     UP(env_marginal, pk->env_marginal, pk->env_marginal_len * 4);
     UP(env_cond, pk->env_conditional, pk->env_conditional_len * 4);
+    {
+        std::vector<uint32_t> guide = env_guide(pk);
+        UP(env_guide, guide.data(), guide.size() * 4);
+    }
     UP(texels, pk->texels, pk->texels_len * 4);
     UP(tex_info, pk->tex_info, pk->tex_info_len * 4);
     UP(nodes, bvh.nodes.data(), bvh.nodes.size() * 4);
@@ -510,10 +549,10 @@ int vg_renderer_update(VgRenderer* r, const VgPacked* pk, const VgUpdatePlan* pl
             return st;
         DevBuf* mine[] = {&r->positions, &r->indices, &r->uvs, &r->vnormals, &r->instances, &r->materials,
                           &r->lights, &r->emitters, &r->emit_cdf, &r->env_pixels, &r->env_marginal, &r->env_cond,
-                          &r->texels, &r->tex_info, &r->nodes, &r->tris};
+                          &r->env_guide, &r->texels, &r->tex_info, &r->nodes, &r->tris};
         DevBuf* theirs[] = {&f->positions, &f->indices, &f->uvs, &f->vnormals, &f->instances, &f->materials,
                             &f->lights, &f->emitters, &f->emit_cdf, &f->env_pixels, &f->env_marginal, &f->env_cond,
-                            &f->texels, &f->tex_info, &f->nodes, &f->tris};
+                            &f->env_guide, &f->texels, &f->tex_info, &f->nodes, &f->tris};
         uint64_t bytes = 0;
         for (size_t i = 0; i < sizeof(mine) / sizeof(mine[0]); i++) {
             std::swap(mine[i]->p, theirs[i]->p);
@@ -594,7 +633,10 @@ int vg_renderer_update(VgRenderer* r, const VgPacked* pk, const VgUpdatePlan* pl
                 (st = upload(ctx, r->env_marginal, pk->env_marginal, pk->env_marginal_len * 4)) != VG_OK ||
                 (st = upload(ctx, r->env_cond, pk->env_conditional, pk->env_conditional_len * 4)) != VG_OK)
                 return st;
-            bytes += (pk->env_pixels_len + pk->env_marginal_len + pk->env_conditional_len) * 4;
+            std::vector<uint32_t> guide = env_guide(pk);
+            if ((st = upload(ctx, r->env_guide, guide.data(), guide.size() * 4)) != VG_OK)
+                return st;
+            bytes += (pk->env_pixels_len + pk->env_marginal_len + pk->env_conditional_len + guide.size()) * 4;
             r->info.env_width = pk->info.env_width;
             r->info.env_height = pk->info.env_height;
             r->info.env_pdf_scale = pk->info.env_pdf_scale;
