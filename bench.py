@@ -432,8 +432,8 @@ def batch_report(ctx, spp_scale, side_range=(256, 2048), spp_range=(16, 256)):
     """Batched serving (64 requests): resolution log-uniform 256^2-2048^2 (square), scenes of ~10k-2M
     triangles generated like the 1M-triangle workload, spp log-uniform 16-256 (times spp_scale),
     depth 16, every second request with a radiance cache. One batch (autotuned, graph replayed)
-    against the same requests rendered one at a time with accumulate (wavefront for plain
-    requests, the cache integrator for cached ones), shortest first; latency = device time from the
+    against the same requests rendered one at a time with accumulate (each on the faster of the
+    wavefront and the megakernel), shortest first; latency = device time from the
     start until the request's last tile. The batch is first autotuned (vg_batch_tune) at a quarter
     of the sample counts."""
     from verion_gb300 import pack, scenes
@@ -474,20 +474,23 @@ def batch_report(ctx, spp_scale, side_range=(256, 2048), spp_range=(16, 256)):
     tuned = ctx.batch_tune(tune_reqs)
     ctx.batch_render(reqs)  # captures the graph
     out = ctx.batch_render(reqs)  # replays it
-    # One at a time, shortest first, through accumulate.
+    # One at a time, shortest first, through accumulate, each request on the faster of the two
+    # integrators (both timed).
     order = sorted(range(64), key=lambda i: spec[i][0] ** 2 * spec[i][1])
     seq_t, now, lat = [], 0.0, [0.0] * 64
     for i in order:
         side, spp, si, cached = spec[i]
         r = cached_r[si] if cached else plain_r[si]
-        if not cached:
-            r.set_integrator(Integrator.WAVEFRONT)
-        acc = r.new_accumulation(side, side)
-        r.accumulate(acc, spp)
-        now += acc.gpu_seconds()
+        best = None
+        for integ in (Integrator.WAVEFRONT, Integrator.MEGAKERNEL):
+            r.set_integrator(integ)
+            acc = r.new_accumulation(side, side)
+            r.accumulate(acc, spp)
+            best = acc.gpu_seconds() if best is None else min(best, acc.gpu_seconds())
+            del acc
+        now += best
         lat[i] = now
-        del acc
-    for r in plain_r:
+    for r in plain_r + cached_r:
         r.set_integrator(Integrator.MEGAKERNEL)
     return {
         "config": f"64 requests, square {min(s[0] for s in spec)}-{max(s[0] for s in spec)} px, "
