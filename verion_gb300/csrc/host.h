@@ -189,6 +189,7 @@ struct VgAccum {
     uint64_t extend_launches_timed = 0;
     uint64_t launches = 0;
     DevBuf accum, stats, light;
+    mutable DevBuf sums32; // f32 copy of f64 sums for vg_accum_read_sums
     bool adaptive_fixed = false; // adaptive setting captured at the first sample
     bool adaptive = false;
     Restir restir;               // captured at the first sample

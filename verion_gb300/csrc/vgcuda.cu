@@ -1083,6 +1083,14 @@ double vg_accum_extend_launch_seconds(const VgAccum* acc)
     return acc->stage_seconds[0] / (double)acc->extend_launches_timed;
 }
 
+// f64 sums to f32 with round-to-nearest-even, the rounding of the host's (float) cast, so that a
+// readback of f32 sums moves half the bytes and needs no conversion on the host.
+static __global__ void sums_to_f32(const double* __restrict__ in, float* __restrict__ out, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = __double2float_rn(in[i]);
+}
+
 static int read_dev(const VgAccum* acc, const DevBuf& b, void* out, size_t bytes)
 {
     cudaStream_t s = acc->owner->ctx->stream;
@@ -1100,13 +1108,17 @@ int vg_accum_read_sums(const VgAccum* acc, float* out, size_t len)
         return fail(VG_ERR_INVALID, "output too short");
     if (acc->precision == 32)
         return read_dev(acc, acc->accum, out, n * 4);
-    std::vector<double> tmp(n);
-    int st = read_dev(acc, acc->accum, tmp.data(), n * 8);
-    if (st != VG_OK)
-        return st;
-    for (size_t i = 0; i < n; i++)
-        out[i] = (float)tmp[i];
-    return VG_OK;
+    // f64 sums: converted on the device, then one copy straight into the caller's buffer (a DMA when
+    // it is pinned).
+    cudaStream_t s = acc->owner->ctx->stream;
+    int st;
+    if (!acc->sums32.p || acc->sums32.bytes < n * 4)
+        if ((st = alloc(acc->sums32, n * 4, s, false)) != VG_OK)
+            return st;
+    int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)acc->owner->ctx->sms * 8);
+    sums_to_f32<<<blocks, 256, 0, s>>>((const double*)acc->accum.p, (float*)acc->sums32.p, n);
+    VG_CHECK(cudaGetLastError(), "sum conversion launch");
+    return read_dev(acc, acc->sums32, out, n * 4);
 }
 
 int vg_accum_read_sums_f64(const VgAccum* acc, double* out, size_t len)
