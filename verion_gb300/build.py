@@ -75,7 +75,7 @@ def build(force: bool = False, verbose: bool = False, defines=(), build_dir: Pat
         o = BUILD / (Path(s).stem + ".o")
         objs.append(o)
         if force or _stale(o, CSRC / s):
-            jobs.append([cxx] + CXX_FLAGS + ["-c", str(CSRC / s), "-o", str(o)])
+            jobs.append([cxx] + CXX_FLAGS + extra + ["-c", str(CSRC / s), "-o", str(o)])
     if jobs:
         with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
             for cmd in jobs:
