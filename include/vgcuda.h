@@ -430,7 +430,7 @@ typedef struct VgCacheConfig {
     uint32_t log2_entries;    /* table entries per level, log2, 8..24 (19) */
     uint32_t base_resolution; /* coarsest grid resolution over the box's largest side (16) */
     uint32_t max_resolution;  /* finest grid resolution (2048) */
-    float learning_rate;      /* Adam step size (0.01) */
+    float learning_rate;      /* Adam step size (0.01; 0 keeps the parameters as they are) */
     float beta1, beta2, epsilon; /* Adam (0.9, 0.99, 1e-8) */
     uint32_t seed;            /* initialisation seed */
     float bounds_lo[3], bounds_hi[3]; /* scene box the grid spans (vg_renderer_bounds) */
@@ -480,6 +480,11 @@ int vg_set_cache(VgRenderer* r, VgCache* cache, float spread, uint32_t train_pat
  * streaming wavefront dispatch of k samples per pixel (the last waves of a dispatch are nearly
  * empty; k samples share them). The training pixels of a frame trace all its samples. */
 int vg_set_cache_frame(VgRenderer* r, uint32_t samples_per_frame);
+/* Radiance cache: training-only frames run before the first sample of each accumulation (default
+ * 0). Each traces one sample of training paths (into a scratch buffer, not the image) and takes
+ * the training steps, so the image does not average in the answers of a cache that has barely
+ * been trained. Their device time counts in the accumulate call. */
+int vg_set_cache_warmup(VgRenderer* r, uint32_t frames);
 /* Of the last sample of the last accumulate call with the cache: query records, training
  * records (before the capacity clamp), and the last training step's mean loss per channel;
  * with stage timing, seconds spent in the path kernel, inference and training over that call. */

@@ -244,3 +244,30 @@ def test_cache_on_the_wavefront_matches_the_megakernel_cache(gpu_ctx, scene):
     keep[[t for t in train if t < px]] = False
     assert abs(gq - wq) <= 3, (gq, wq)
     np.testing.assert_allclose(got.reshape(px, 3)[keep], want.reshape(px, 3)[keep], rtol=1e-12, atol=1e-12)
+
+
+def test_cache_warmup_trains_without_touching_the_image(gpu_ctx):
+    # Warm-up frames trace their training paths into a scratch buffer: with a learning rate of 0
+    # (training changes no parameter) the image is the one without warm-up, bit for bit; with a
+    # learning rate the warm-up frames train the cache before the first sample.
+    from verion_gb300.backend import Integrator
+    p = pack.pack(scenes.cornell())
+
+    def run(warm, lr):
+        r = Renderer(gpu_ctx, p)
+        r.set_integrator(Integrator.WAVEFRONT)
+        cache = Cache(gpu_ctx, bounds=r.bounds(), seed=3, learning_rate=lr)
+        r.set_cache(cache, spread=0.01, train_paths=256, train_steps=2, train_batch=1024)
+        r.set_cache_warmup(warm)
+        acc = r.new_accumulation(40, 32)
+        r.accumulate(acc, 2)
+        assert acc.samples() == 2
+        return acc.sums_f64(), cache.read_params()[0]
+
+    img0, m0 = run(0, 0.0)
+    img3, m3 = run(3, 0.0)
+    assert np.array_equal(img0, img3)
+    assert np.array_equal(m0, m3)
+    _, t0 = run(0, 0.01)
+    _, t3 = run(3, 0.01)
+    assert not np.array_equal(t0, t3)

@@ -240,6 +240,7 @@ def lib() -> C.CDLL:
             "vg_cache_train": (i32, [vp, vp, _S, u32, C.POINTER(f64)]),
             "vg_set_cache": (i32, [vp, vp, C.c_float, u32, u32, u32]),
             "vg_set_cache_frame": (i32, [vp, u32]),
+            "vg_set_cache_warmup": (i32, [vp, u32]),
             "vg_cache_time": (i32, [vp, vp, _S, u32, C.POINTER(f64)]),
             "vg_batch_render": (i32, [vp, vp, _S, vp, C.POINTER(f64), C.POINTER(C.c_int)]),
             "vg_set_batch_options": (i32, [vp, i32, i32, C.c_uint64]),
@@ -680,6 +681,10 @@ class Renderer:
         _check(lib().vg_set_cache(self._h, cache._h if cache else None, spread, train_paths, train_steps,
                                   train_batch))
         self._cache = cache
+
+    def set_cache_warmup(self, frames: int) -> None:
+        """Radiance cache: training-only frames before the first sample of each accumulation."""
+        _check(lib().vg_set_cache_warmup(self._h, frames))
 
     def set_cache_frame(self, samples_per_frame: int) -> None:
         """WAVEFRONT integrator with a cache: samples per cache frame (the cache is trained after

@@ -187,6 +187,32 @@ int cache_accumulate(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, uint32_t samples,
     vgn::CacheDev d = k->dev();
     bool f64 = acc->precision == 64;
     vgx::Variant v = variant_of(r, acc);
+    // Warm-up, before the first sample of an accumulation: training-only frames (one sample of
+    // training paths into a scratch sum buffer, then the training steps) so that the image does
+    // not average in the answers of an untrained cache. Their samples are numbered from
+    // CACHE_WARMUP_SAMPLE, apart from the image's.
+    if (acc->samples == 0 && r->cache_warmup > 0 && r->cache_steps > 0 && tcap > 0) {
+        DevBuf scratch;
+        if ((st = alloc(scratch, px * 3 * (acc->precision == 64 ? 8 : 4), s, false)) != VG_OK)
+            return st;
+        vgd::Ctx cw = c;
+        cw.accum = scratch.p;
+        for (uint32_t f = 0; f < r->cache_warmup; f++) {
+            uint32_t sample = CACHE_WARMUP_SAMPLE + f;
+            cw.p[P_SAMPLE] = sample;
+            cw.p[P_SAMPLES_PER_DISPATCH] = 1; // one sample per training pixel: a quarter of the cost of a 4-sample frame
+            a.train_offset = (sample * 2654435761u) % a.train_stride;
+            VG_CHECK(cudaMemsetAsync(ctr, 0, 4, s), "counters");
+            VG_CHECK(vgx::nrc_launch_train_paths(f64, s, cw, a), "cache training path launch");
+            acc->launches++;
+            for (uint32_t t = 0; t < r->cache_steps; t++) {
+                if ((st = cache_train_step(k, a.trec, ctr, tcap, t * r->cache_batch, r->cache_batch)) != VG_OK)
+                    return st;
+                acc->launches += 7;
+            }
+        }
+        VG_CHECK(cudaStreamSynchronize(s), "cache warm-up"); // the scratch buffer is freed next
+    }
     EventPool pool;
     StageEvents stages;
     for (uint32_t i = 0; i < samples;) {
@@ -301,7 +327,7 @@ int vg_cache_create(VgContext* ctx, const VgCacheConfig* cfg, VgCache** out)
     if (c.levels < 1 || c.levels > vgn::MAX_LEVELS || c.log2_entries < 8 || c.log2_entries > 24 ||
         c.base_resolution < 2 || c.max_resolution < c.base_resolution || c.max_resolution > 65536)
         return fail(VG_ERR_INVALID, "cache grid configuration out of range");
-    if (!(c.learning_rate > 0.0f) || !(c.beta1 >= 0.0f && c.beta1 < 1.0f) || !(c.beta2 >= 0.0f && c.beta2 < 1.0f) ||
+    if (!(c.learning_rate >= 0.0f) || !(c.beta1 >= 0.0f && c.beta1 < 1.0f) || !(c.beta2 >= 0.0f && c.beta2 < 1.0f) ||
         !(c.epsilon > 0.0f))
         return fail(VG_ERR_INVALID, "cache optimiser configuration out of range");
     for (int k = 0; k < 3; k++)
@@ -578,6 +604,16 @@ int vg_set_cache(VgRenderer* r, VgCache* cache, float spread, uint32_t train_pat
     r->cache_train_paths = train_paths;
     r->cache_steps = train_steps;
     r->cache_batch = train_batch;
+    return VG_OK;
+}
+
+int vg_set_cache_warmup(VgRenderer* r, uint32_t frames)
+{
+    if (!r)
+        return fail(VG_ERR_INVALID, "null renderer");
+    if (frames > 4096)
+        return fail(VG_ERR_INVALID, "cache warm-up out of range (0-4096 frames)");
+    r->cache_warmup = frames;
     return VG_OK;
 }
 

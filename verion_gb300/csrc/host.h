@@ -134,7 +134,8 @@ struct Restir {
     }
 };
 
-constexpr uint32_t MAX_CACHE_FRAME = 16; // samples per radiance-cache frame at most
+constexpr uint32_t MAX_CACHE_FRAME = 16;           // samples per radiance-cache frame at most
+constexpr uint32_t CACHE_WARMUP_SAMPLE = 0x40000000u; // first sample index of cache warm-up frames
 
 struct VgRenderer {
     VgContext* ctx = nullptr;
@@ -174,6 +175,7 @@ struct VgRenderer {
     uint32_t cache_steps = 4;
     uint32_t cache_batch = 16384;
     uint32_t cache_frame = 4;     // integrator WAVEFRONT: samples per cache frame (one cache update per frame)
+    uint32_t cache_warmup = 0;    // training-only frames before the first sample of an accumulation
     int cache_shade_blocks[2] = {};
 };
 
