@@ -49,18 +49,6 @@ static __device__ __forceinline__ uint32_t reserve(uint32_t* ctr, uint32_t k)
     return base + incl - k;
 }
 
-static __device__ __forceinline__ void features(float* d, const CacheHook& hk)
-{
-    d[0] = hk.pos.x, d[1] = hk.pos.y, d[2] = hk.pos.z;
-    d[3] = hk.wo.x, d[4] = hk.wo.y, d[5] = hk.wo.z;
-    d[6] = hk.n.x, d[7] = hk.n.y, d[8] = hk.n.z;
-    d[9] = hk.rough;
-    d[10] = hk.albedo.x, d[11] = hk.albedo.y, d[12] = hk.albedo.z;
-    d[13] = hk.metallic;
-    d[14] = hk.transmission;
-    d[15] = 0.0f;
-}
-
 template <typename A>
 static __device__ __forceinline__ void plain_tile(const Ctx& c, uint32_t x, uint32_t y, bool inside)
 {
@@ -77,8 +65,9 @@ static __device__ __forceinline__ void plain_tile(const Ctx& c, uint32_t x, uint
     }
 }
 
-// One sample of a cached tile (mk_cache_paths for one pixel per thread); returns whether this
-// thread's path left a query, with its record in `q`.
+// One sample of a cached tile, one pixel per thread: the query path of mk_cache_query, or the
+// training path of mk_cache_train for a training pixel; returns whether this thread's path left a
+// query, with its record in `q`.
 template <typename A>
 static __device__ __forceinline__ bool cache_sample(const BatchReq& R, uint32_t x, uint32_t y, bool inside,
                                                     uint32_t sample, float* q)
@@ -102,7 +91,7 @@ static __device__ __forceinline__ bool cache_sample(const BatchReq& R, uint32_t 
             bool alive = shadePath<false, false, false, true>(c, st, traceClosest(c, st.org, st.dir), depth, pixel,
                                                               nullptr, &hk);
             if (hk.vertex && hk.train && nv < MAX_TRAIN_VERTICES) {
-                features(feat[nv], hk);
+                cacheFeatures(feat[nv], hk);
                 thr[nv] = hk.thr;
                 Lb[nv] = hk.L;
                 nv++;
@@ -133,7 +122,7 @@ static __device__ __forceinline__ bool cache_sample(const BatchReq& R, uint32_t 
         d[19] = 0.0f;
     }
     if (query && ok) {
-        features(q, hk);
+        cacheFeatures(q, hk);
         q[16] = hk.thr.x, q[17] = hk.thr.y, q[18] = hk.thr.z;
         return true;
     }
