@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--profile-extend", action="store_true",
                     help="profiling helper: one step with traversal counters inside the NVTX range 'traffic', "
                          "then print the counters (for an ncu capture of the extend kernels' DRAM bytes)")
+    ap.add_argument("--profile-cache", action="store_true",
+                    help="profiling helper: the radiance cache on this workload (the cache report's C2 settings), "
+                         "--warmup frames of 4 samples, then one timed frame; prints its device time and split")
     ap.add_argument("--width", type=int, default=WIDTH, help="smaller frames are for profiling runs only")
     ap.add_argument("--height", type=int, default=HEIGHT)
     a = ap.parse_args()
@@ -580,6 +583,28 @@ def run_cuda(args):
     r.set_accum_precision(64)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     total = args.warmup + args.steps
+
+    if args.profile_cache:
+        from verion_gb300.backend import Cache
+
+        rc = Renderer(ctx, packed)
+        rc.set_integrator(Integrator.WAVEFRONT)
+        rc.set_max_depth(DEPTH)
+        cache = Cache(ctx, bounds=rc.bounds())
+        rc.set_cache(cache, spread=0.002)
+        rc.set_stage_timing(True)
+        acc_c = rc.new_accumulation(WIDTH, HEIGHT)
+        for _ in range(args.warmup):
+            rc.accumulate(acc_c, 4)
+        g0, st0 = acc_c.gpu_seconds(), acc_c.cache_stats()
+        rc.accumulate(acc_c, 4)
+        st1 = acc_c.cache_stats()
+        print(json.dumps({"frame_ms": 1e3 * (acc_c.gpu_seconds() - g0),
+                          "paths_ms": 1e3 * (st1.path_seconds - st0.path_seconds),
+                          "encode_and_infer_ms": 1e3 * (st1.infer_seconds - st0.infer_seconds),
+                          "train_ms": 1e3 * (st1.train_seconds - st0.train_seconds),
+                          "queries": st1.queries, "train_records": st1.train_records}), flush=True)
+        return
 
     if args.profile_extend:
         acc_p = r.new_accumulation(WIDTH, HEIGHT)
