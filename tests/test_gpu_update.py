@@ -138,3 +138,17 @@ def test_a_vertex_count_change_needs_a_full_update(gpu_ctx):
     s.meshes[lamp_mesh] = sc.Mesh(np.concatenate([m.positions, m.positions[:1]]), m.indices)
     with pytest.raises(Error):
         r.update(s, UpdatePlan.new(deformed=[lamp_mesh]))
+
+
+@pytestmark_gpu
+def test_an_environment_map_edit_redraws_like_a_rebuild(gpu_ctx):
+    # A new HDRI (its texels, CDFs and the sampling guide tables) through a lights update: the image
+    # is the one of a renderer built on the edited scene.
+    s = scenes.many_spheres(spheres=4, sphere_n=7, grid=16, hdri=None)
+    first = s.add_image(scenes.sky_hdri(64, 32, sun_peak=200.0, seed=1))
+    env = s.add_light(sc.EnvironmentMap(first, 1.0))
+    r = Renderer(gpu_ctx, s)
+    r.set_integrator(Integrator.WAVEFRONT)
+    second = s.add_image(scenes.sky_hdri(128, 64, sun_peak=800.0, seed=2))
+    s.lights[env] = sc.EnvironmentMap(second, 1.0)
+    update_matches_fresh(gpu_ctx, r, s, UpdatePlan.new(lights=True))
