@@ -216,10 +216,11 @@ int vg_set_bvh_traversal_cost(VgRenderer* r, const VgPacked* packed, float cost)
 
 /* Autotuner of the streaming wavefront (no reference counterpart): on scratch accumulations of
  * width x height and `samples` per trial, a coordinate-descent pass over dynamic fetch, deferred
- * shadows, the tail threshold (0, 8192, 32768, 131072), the wave graph (0 or 8 waves) and, when
- * `packed` is given, the BVH8's SAH traversal cost (0.25, 0.5, 1, 2); a change is kept when it is more
- * than 1% faster. Leaves the renderer on the streaming wavefront with the best setting. All of
- * these settings give the same sums. */
+ * shadows, the tail threshold (0, 8192, 32768, 131072), the wave graph (0 or 8 waves), the CTAs
+ * per SM of the persistent extend stage (the most that fit, 3/4 or 1/2 of it) and, when `packed` is
+ * given, the BVH8's SAH traversal cost (0.25, 0.5, 1, 2); a change is kept when it is more than 1%
+ * faster. Leaves the renderer on the streaming wavefront with the best setting. All of these
+ * settings give the same sums. */
 typedef struct VgTuneResult {
     int dynamic_fetch;
     int deferred_shadows;
@@ -228,6 +229,7 @@ typedef struct VgTuneResult {
     float bvh_traversal_cost;
     double mpaths_before, mpaths_after; /* camera paths per second, first and best trial */
     uint32_t trials;
+    int extend_blocks_per_sm;
 } VgTuneResult;
 int vg_autotune(VgRenderer* r, const VgPacked* packed, uint32_t width, uint32_t height, uint32_t samples,
                 VgTuneResult* out);

@@ -61,5 +61,6 @@ def test_autotune_keeps_the_sums(gpu_ctx):
     t = r.autotune(160, 90, 2)
     assert t["trials"] >= 6 and t["mpaths_after"] >= t["mpaths_before"] > 0
     assert t["graph_waves"] in (0, 8) and t["bvh_traversal_cost"] in (0.25, 0.5, 1.0, 2.0)
+    assert t["extend_blocks_per_sm"] >= 1
     fresh = wave_renderer(gpu_ctx, p)
     assert np.array_equal(render(r, 80, 45, 3), render(fresh, 80, 45, 3))

@@ -111,7 +111,7 @@ class CacheStats(C.Structure):
 class _TuneResult(C.Structure):
     _fields_ = [("dynamic_fetch", C.c_int), ("deferred_shadows", C.c_int), ("stream_tail", C.c_uint32),
                 ("graph_waves", C.c_uint32), ("bvh_traversal_cost", C.c_float), ("mpaths_before", C.c_double),
-                ("mpaths_after", C.c_double), ("trials", C.c_uint32)]
+                ("mpaths_after", C.c_double), ("trials", C.c_uint32), ("extend_blocks_per_sm", C.c_int)]
 
 
 class _BatchRequest(C.Structure):

@@ -1282,6 +1282,18 @@ int vg_autotune(VgRenderer* r, const VgPacked* pk, uint32_t width, uint32_t heig
             return o;
         },
         std::vector<uint32_t>{r->graph_waves == 0 ? 8u : 0u});
+    int most = vgx::wf_extend_blocks_per_sm();
+    std::vector<int> extend_blocks;
+    for (int b : {most, (3 * most) / 4, most / 2})
+        if (b >= 1 && b != r->extend_blocks)
+            extend_blocks.push_back(b);
+    try_setting(
+        [&](int v, bool) {
+            int o = r->extend_blocks;
+            r->extend_blocks = v;
+            return o;
+        },
+        extend_blocks);
     if (pk && st == VG_OK) {
         std::vector<float> costs;
         for (float c : {0.25f, 0.5f, 2.0f})
@@ -1306,6 +1318,7 @@ int vg_autotune(VgRenderer* r, const VgPacked* pk, uint32_t width, uint32_t heig
     out->stream_tail = r->tail_threshold;
     out->graph_waves = r->graph_waves;
     out->bvh_traversal_cost = r->bvh_traversal_cost;
+    out->extend_blocks_per_sm = r->extend_blocks;
     out->mpaths_after = best;
     out->trials = trials;
     return VG_OK;
