@@ -61,6 +61,9 @@ def parse():
     ap.add_argument("--profile-cache", action="store_true",
                     help="profiling helper: the radiance cache on this workload (the cache report's C2 settings), "
                          "--warmup frames of 4 samples, then one timed frame; prints its device time and split")
+    ap.add_argument("--profile-mlp", action="store_true",
+                    help="profiling helper: the cache's kernels on 2^20 synthetic records, one untimed and one "
+                         "timed launch of each (encode, inference, training pass, scatter); prints their times")
     ap.add_argument("--width", type=int, default=WIDTH, help="smaller frames are for profiling runs only")
     ap.add_argument("--height", type=int, default=HEIGHT)
     a = ap.parse_args()
@@ -309,6 +312,24 @@ def _cache_vs_plain(plains, curve, target_at):
             "speedup": (t_plain[best] / t_cache) if t_cache else None, "speedup_against": "plain " + best}
 
 
+def mlp_kernel_seconds(ctx, nrec, reps):
+    """Device seconds per launch of the cache's kernels (vg_cache_time: one untimed round, then
+    `reps` launches of each) on nrec synthetic records: positions uniform in a unit box, unit
+    directions, material features and targets uniform."""
+    from verion_gb300.backend import Cache
+
+    rng = np.random.default_rng(5)
+    lo, hi = ((-1.0,) * 3, (1.0,) * 3)
+    rec = np.zeros((nrec, 20), np.float32)
+    rec[:, 0:3] = rng.uniform(lo, hi, (nrec, 3))
+    for o in (3, 6):
+        d = rng.normal(size=(nrec, 3))
+        rec[:, o:o + 3] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rec[:, 9:15] = rng.uniform(0, 1, (nrec, 6))
+    rec[:, 16:19] = rng.uniform(0, 2, (nrec, 3))
+    return Cache(ctx, bounds=(lo, hi)).time_kernels(rec, reps=reps)
+
+
 def cache_report(ctx, packed_c2, peak_tflops, peak_kind):
     """Radiance cache (cache query paths on the streaming wavefront) against plain path tracing:
     time to reach a plain image's RMSE (against a long plain reference, GPU time), the speed-up
@@ -400,19 +421,9 @@ def cache_report(ctx, packed_c2, peak_tflops, peak_kind):
         c2[label] = _cache_vs_plain(plains, curve, at)
     out["many_spheres_1080p"] = c2
     del acc, r
-    # MLP kernels on synthetic records (random positions in the scene box, unit directions).
-    rng = np.random.default_rng(5)
+    # MLP kernels on synthetic records.
     nrec = 1 << 20
-    lo, hi = ((-1.0,) * 3, (1.0,) * 3)
-    rec = np.zeros((nrec, 20), np.float32)
-    rec[:, 0:3] = rng.uniform(lo, hi, (nrec, 3))
-    for o in (3, 6):
-        d = rng.normal(size=(nrec, 3))
-        rec[:, o:o + 3] = d / np.linalg.norm(d, axis=1, keepdims=True)
-    rec[:, 9:15] = rng.uniform(0, 1, (nrec, 6))
-    rec[:, 16:19] = rng.uniform(0, 2, (nrec, 3))
-    kc = Cache(ctx, bounds=(lo, hi))
-    kt = kc.time_kernels(rec, reps=10)
+    kt = mlp_kernel_seconds(ctx, nrec, reps=10)
     infer_tf = CACHE_MLP_FLOP * nrec / kt["infer"] / 1e12
     train_tf = 3 * CACHE_MLP_FLOP * nrec / kt["train"] / 1e12
     out["mlp_kernels"] = {"records": nrec, "seconds_per_launch": kt,
@@ -583,6 +594,10 @@ def run_cuda(args):
     r.set_accum_precision(64)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     total = args.warmup + args.steps
+
+    if args.profile_mlp:
+        print(json.dumps(mlp_kernel_seconds(ctx, 1 << 20, reps=1)), flush=True)
+        return
 
     if args.profile_cache:
         from verion_gb300.backend import Cache
