@@ -760,6 +760,8 @@ def run_cuda(args):
     batch = None
     if rank == 0 and not args.no_batch:
         batch = batch_report(ctx, args.batch_spp_scale)
+        # Small requests (128-512 px square, 4-32 spp): the shared persistent launch's case.
+        batch["small_requests"] = batch_report(ctx, 1.0, side_range=(128, 512), spp_range=(4, 32))
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
