@@ -1,6 +1,6 @@
 """Benchmark of the CUDA path-tracing backend on the 1M-triangle wavefront workload.
 
-Workload (configs[1] of the benchmark plan): 64 subdivided spheres on a noise-displaced 512 x 512 grid
+Workload (the 1M-triangle benchmark configuration): 64 subdivided spheres on a noise-displaced 512 x 512 grid
 (1,014,274 triangles; GGX conductor / dielectric / Lambertian materials), a 2048 x 1024 float HDRI,
 1920 x 1080, max depth 16, wavefront integrator with adaptive sampling (threshold 0.02, 16 minimum
 samples), double-precision sums. All inputs are generated from seeds (`data: synthetic`).

@@ -1,6 +1,6 @@
 """The N > 1 paths of bench.py on CPU: two ranks over gloo (127.0.0.1). The per-rank numbers are
-combined as the driver expects (max of the times, sum of the paths), and under torchrun only rank 0
-runs the reference arm: the other ranks join the rendezvous and exit 0 without work."""
+combined as a multi-GPU run reports them (max of the times, sum of the paths), and under torchrun
+only rank 0 runs the reference arm: the other ranks join the rendezvous and exit 0 without work."""
 import multiprocessing as mp
 import os
 import socket

@@ -1,6 +1,6 @@
 """The CPU oracle against the reference's known answers (crates/verion-gpu-metal/tests/pathtrace.rs
 and trace.rs) and against itself (its BVH against brute force, wavefront against megakernel).
-These pin the oracle before it is used to judge the CUDA backend."""
+These pin the oracle before it is used to check the CUDA backend."""
 import math
 
 import numpy as np
