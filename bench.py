@@ -678,9 +678,13 @@ def run_cuda(args):
     for _ in range(args.warmup):
         r.accumulate(acc_s, SPP_STEP)
     s0 = acc_s.traversal_stats() if args.integrator == "wavefront" else None
+    sh0 = acc_s.shadow_rays() if args.integrator == "wavefront" else 0
     for _ in range(args.steps):
         r.accumulate(acc_s, SPP_STEP)
     s1 = acc_s.traversal_stats() if args.integrator == "wavefront" else None
+    sh1 = acc_s.shadow_rays() if args.integrator == "wavefront" else 0
+    # Rays (closest-hit + shadow) per camera path: the replay traces the timed steps' paths.
+    rays_per_path = ((s1["rays"] - s0["rays"] + sh1 - sh0) / max(paths, 1.0)) if s0 is not None else None
     r.set_traversal_stats(False)
     del acc_s
 
@@ -778,6 +782,8 @@ def run_cuda(args):
                 "clocks": clk.summary(),
                 "stage_seconds": {"extend": stage[0], "shade": stage[1]},
                 "paths_per_step": paths_all / args.steps,
+                "mrays_per_s": value * rays_per_path if rays_per_path else None,
+                "rays_per_path": rays_per_path,
                 "megakernel_value": mega, "radiance_cache": cache, "batched_serving": batch,
                 "restir_many_lights": restir}
         print(json.dumps(line), flush=True)

@@ -279,6 +279,9 @@ int vg_accum_read_queue_counts(const VgAccum* acc, uint32_t* out, size_t len);
 /* Extend-stage counters since the accumulation began (with traversal stats on): rays, BVH nodes
  * visited, triangles tested, rays past depth 0. */
 int vg_accum_traversal_stats(const VgAccum* acc, uint64_t out[4]);
+/* Shadow rays traced by the streaming wavefront's any-hit stage since the accumulation began (with
+ * traversal stats on; with the deferred shadow stage and dynamic fetch in opaque scenes). */
+int vg_accum_shadow_rays(const VgAccum* acc, uint64_t* out);
 /* Kernel launches made by vg_accumulate on this accumulation so far. */
 uint64_t vg_accum_launches(const VgAccum* acc);
 /* Average duration in seconds of one extend-kernel launch, from stage timing (0 if none). */

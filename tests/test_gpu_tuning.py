@@ -64,3 +64,20 @@ def test_autotune_keeps_the_sums(gpu_ctx):
     assert t["extend_blocks_per_sm"] >= 1
     fresh = wave_renderer(gpu_ctx, p)
     assert np.array_equal(render(r, 80, 45, 3), render(fresh, 80, 45, 3))
+
+
+def test_traversal_counters_count_and_change_nothing(gpu_ctx):
+    # The counting instantiations of the extend and shadow stages give the same sums; they count
+    # every closest-hit ray (one per path vertex reached, at least one per camera path) and the
+    # shadow rays of the deferred light samples (at most one per closest hit).
+    p = pack.pack(scenes.many_spheres(hdri=(256, 128)))
+    r = wave_renderer(gpu_ctx, p)
+    want = render(r, 96, 54, 2)
+    r.set_traversal_stats(True)
+    acc = r.new_accumulation(96, 54)
+    r.accumulate(acc, 2)
+    st = acc.traversal_stats()
+    shadow = acc.shadow_rays()
+    assert np.array_equal(acc.sums(), want)
+    assert st["rays"] >= 96 * 54 * 2 and st["nodes"] > st["rays"]
+    assert 0 < shadow <= st["rays"]

@@ -205,6 +205,7 @@ def lib() -> C.CDLL:
             "vg_set_bvh_traversal_cost": (i32, [vp, C.POINTER(_Packed), C.c_float]),
             "vg_autotune": (i32, [vp, C.POINTER(_Packed), u32, u32, u32, C.POINTER(_TuneResult)]),
             "vg_accum_traversal_stats": (i32, [vp, C.POINTER(C.c_uint64)]),
+            "vg_accum_shadow_rays": (i32, [vp, C.POINTER(C.c_uint64)]),
             "vg_set_accum_precision": (i32, [vp, i32]),
             "vg_accum_create": (i32, [vp, u32, u32, i32, C.POINTER(vp)]),
             "vg_accum_destroy": (None, [vp]),
@@ -408,6 +409,12 @@ class Accumulation:
         out = (C.c_uint64 * 4)()
         _check(lib().vg_accum_traversal_stats(self._h, out))
         return {"rays": out[0], "nodes": out[1], "tests": out[2], "rays_after_depth0": out[3]}
+
+    def shadow_rays(self) -> int:
+        """Rays traced by the any-hit shadow stage (traversal stats on)."""
+        out = C.c_uint64(0)
+        _check(lib().vg_accum_shadow_rays(self._h, C.byref(out)))
+        return out.value
 
     def launches(self) -> int:
         return lib().vg_accum_launches(self._h)

@@ -278,9 +278,13 @@ cudaError_t launch_stream_extend_dyn(bool stats, int blocks, cudaStream_t s, con
     return cudaGetLastError();
 }
 
-cudaError_t launch_stream_shadow_trace(int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w, uint32_t wave)
+cudaError_t launch_stream_shadow_trace(bool stats, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                                       uint32_t wave)
 {
-    vgk::wf_stream_shadow_trace<<<blocks, 128, 0, s>>>(c, w, wave);
+    if (stats)
+        vgk::wf_stream_shadow_trace<true><<<blocks, 128, 0, s>>>(c, w, wave);
+    else
+        vgk::wf_stream_shadow_trace<false><<<blocks, 128, 0, s>>>(c, w, wave);
     return cudaGetLastError();
 }
 

@@ -624,13 +624,16 @@ __global__ void __launch_bounds__(128, 8) wf_stream_extend_dyn(const __grid_cons
 }
 
 // Shadow rays of the deferred light samples, any hit (opaque scenes: one layer, no opacity roll).
-// The result goes to hits[p].x (1 occluded), which the finish stage reads.
-static __global__ void __launch_bounds__(128, 8) wf_stream_shadow_trace(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
+// The result goes to hits[p].x (1 occluded), which the finish stage reads. STATS: the rays traced
+// are counted into tstats[4].
+template <bool STATS>
+__global__ void __launch_bounds__(128, 8) wf_stream_shadow_trace(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
 {
     uint32_t in = wave & 1u;
     uint32_t count = w.counts[in];
     const uint32_t* qin = w.queue[in];
     uint32_t n = w.n;
+    uint32_t n_rays = 0;
     vgt::trace_queue<true, VG_SHADOW_REFILL, VG_SHADOW_STEPS>(
         c.s.nodes, c.s.tris, &w.fetch[4 + in], count, c.err,
         [&](uint32_t i, V3& o, V3& d, float& tmax) {
@@ -644,9 +647,13 @@ static __global__ void __launch_bounds__(128, 8) wf_stream_shadow_trace(const __
             o = v3(r0.x, r0.y, r0.z);
             d = v3(r1.x, r1.y, r1.z);
             tmax = r0.w;
+            if (STATS)
+                n_rays++;
             return true;
         },
         [&](uint32_t i, const vgt::TraceHit& q) { ((uint32_t*)w.hits)[4 * (size_t)qin[i]] = q.hit ? 1u : 0u; });
+    if (STATS)
+        warp_count(&w.tstats[4], n_rays);
 }
 
 // After the shadow trace: add the unoccluded light sample, then queue, finish or restart each slot

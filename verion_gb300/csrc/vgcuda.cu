@@ -231,7 +231,7 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
             if (ce == cudaSuccess && deferred) {
                 ce = (q ? vgx::launch_stream_cache_shade(v.f64, csb, s, c, w, i, *q) : vgx::launch_stream_shade_deferred(v.f64, dsb, s, c, w, i));
                 if (ce == cudaSuccess && r->dynamic_fetch && r->ds.shadow_any) {
-                    ce = vgx::launch_stream_shadow_trace(shb, s, c, w, i);
+                    ce = vgx::launch_stream_shadow_trace(r->traversal_stats, shb, s, c, w, i);
                     if (ce == cudaSuccess)
                         ce = vgx::launch_stream_finish(v.f64, shb, s, c, w, i);
                 } else if (ce == cudaSuccess)
@@ -317,7 +317,7 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
                 VG_CHECK(cudaEventRecord(qe, s), "event");
             }
             if (r->dynamic_fetch && r->ds.shadow_any) {
-                VG_CHECK(vgx::launch_stream_shadow_trace(shb, s, c, w, (uint32_t)wave), "shadow launch");
+                VG_CHECK(vgx::launch_stream_shadow_trace(r->traversal_stats, shb, s, c, w, (uint32_t)wave), "shadow launch");
                 VG_CHECK(vgx::launch_stream_finish(v.f64, shb, s, c, w, (uint32_t)wave), "finish launch");
                 acc->launches++;
             } else {
@@ -947,7 +947,7 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
             (st = alloc(acc->queue[1], px * 4, s, false)) != VG_OK ||
             (st = alloc(acc->counts, (max_depth_alloc + 1) * 4, s, true)) != VG_OK ||
             (st = alloc(acc->fetch, 2 * (max_depth_alloc + 1) * 4, s, true)) != VG_OK ||
-            (st = alloc(acc->tstats, 4 * 8, s, true)) != VG_OK ||
+            (st = alloc(acc->tstats, 8 * 8, s, true)) != VG_OK ||
             (st = alloc(acc->meta, px * 4, s, false)) != VG_OK ||
             (st = alloc(acc->sreq, acc->lighting ? 16 : px * 3 * 16, s, false)) != VG_OK)
             return st;
@@ -1178,6 +1178,19 @@ int vg_accum_traversal_stats(const VgAccum* acc, uint64_t out[4])
     if (!acc->tstats.p)
         return fail(VG_ERR_INVALID, "no wavefront sample has run on this accumulation");
     return read_dev(acc, acc->tstats, out, 4 * 8);
+}
+
+int vg_accum_shadow_rays(const VgAccum* acc, uint64_t* out)
+{
+    if (!acc || !out)
+        return fail(VG_ERR_INVALID, "null argument");
+    if (!acc->tstats.p)
+        return fail(VG_ERR_INVALID, "no wavefront sample has run on this accumulation");
+    uint64_t words[5];
+    int st = read_dev(acc, acc->tstats, words, sizeof(words));
+    if (st == VG_OK)
+        *out = words[4];
+    return st;
 }
 
 int vg_accum_read_queue_counts(const VgAccum* acc, uint32_t* out, size_t len)
