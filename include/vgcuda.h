@@ -410,7 +410,7 @@ typedef struct VgExrFrame {
 
 /* write_exr (exr_out.rs:103-293): one OpenEXR file with the reference's channel names (R, G, B,
  * N.X.., Albedo.*, DirectDiffuse.* .. Emission.*, Visibility.V, Z, and the 32-bit integer channels
- * ObjectId, MaterialId, SampleCount), the target's chromaticities and the `verion/*` metadata.
+ * ObjectId, MaterialId, SampleCount), the target's chromaticities and the `verion/` metadata.
  * Uncompressed scanlines. VG_ERR_INVALID for a zero size or an incomplete lighting split;
  * VG_ERR_RESOURCE when the file cannot be written. */
 int vg_write_exr(const char* path, const VgExrFrame* frame, const VgOutputTransform* transform);

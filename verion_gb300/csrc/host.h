@@ -376,7 +376,7 @@ vgk::Wave wave_of(const VgRenderer* r, const VgAccum* acc)
     return w;
 }
 
-vgx::Variant variant_of(const VgRenderer* r, const VgAccum* acc)
+vgx::Variant variant_of(const VgRenderer*, const VgAccum* acc)
 {
     vgx::Variant v;
     v.light = acc->lighting;
