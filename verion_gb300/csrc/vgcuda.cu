@@ -24,6 +24,7 @@
 #include "bvh_build.h"
 #include "launch.h"
 
+#include "env_guide.h"
 #include "host.h"
 
 // Sets the thread's error text for translation units compiled without the CUDA headers.
@@ -95,37 +96,18 @@ bool translucent_materials(const VgPacked* pk)
     return false;
 }
 
-// The environment CDF search (pt_core.slang:274-306): the first of the n entries >= u, the last
-// when none is.
-uint32_t cdf_search(const float* cdf, uint32_t n, float u)
-{
-    uint32_t lo = 0, hi = n - 1;
-    while (lo < hi) {
-        uint32_t mid = (lo + hi) / 2;
-        if (cdf[mid] >= u)
-            hi = mid;
-        else
-            lo = mid + 1;
-    }
-    return lo;
-}
-
-// Guide tables of the environment's CDF searches (vgd::ENV_GUIDE_M / ENV_GUIDE_C, ctx.h): entry k
-// of a table is the search's answer for u = k / K. The CDFs are non-decreasing, so the answer for
-// any u of bucket k lies between entries k and k + 1.
+// Guide tables of the environment's CDF searches (env_guide.h; sizes vgd::ENV_GUIDE_M / ENV_GUIDE_C):
+// the marginal's, then one per row of the conditional.
 std::vector<uint32_t> env_guide(const VgPacked* pk)
 {
     uint32_t w = pk->info.env_width, h = pk->info.env_height;
     if (w == 0 || h == 0)
         return std::vector<uint32_t>(vgd::ENV_GUIDE_M + 1, 0u);
     std::vector<uint32_t> g((vgd::ENV_GUIDE_M + 1) + (size_t)h * (vgd::ENV_GUIDE_C + 1));
-    for (uint32_t k = 0; k <= vgd::ENV_GUIDE_M; k++)
-        g[k] = cdf_search(pk->env_marginal, h, (float)k / (float)vgd::ENV_GUIDE_M);
-    for (uint32_t j = 0; j < h; j++) {
-        uint32_t* row = g.data() + (vgd::ENV_GUIDE_M + 1) + (size_t)j * (vgd::ENV_GUIDE_C + 1);
-        for (uint32_t k = 0; k <= vgd::ENV_GUIDE_C; k++)
-            row[k] = cdf_search(pk->env_conditional + (size_t)j * w, w, (float)k / (float)vgd::ENV_GUIDE_C);
-    }
+    envg::build_guide(pk->env_marginal, h, vgd::ENV_GUIDE_M, g.data());
+    for (uint32_t j = 0; j < h; j++)
+        envg::build_guide(pk->env_conditional + (size_t)j * w, w, vgd::ENV_GUIDE_C,
+                          g.data() + (vgd::ENV_GUIDE_M + 1) + (size_t)j * (vgd::ENV_GUIDE_C + 1));
     return g;
 }
 
