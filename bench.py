@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["cuda", "reference"], default="cuda")
     ap.add_argument("--integrator", choices=["wavefront", "megakernel"], default="wavefront")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--cpu-seconds", type=float, default=16.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-cache", action="store_true", help="skip the radiance-cache measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-serving measurement")
@@ -88,15 +88,44 @@ def config(args, extra=None):
     return c
 
 
-def dist_init(args):
+def dist_init(args, backend=None):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:
         import torch.distributed as dist
 
-        backend = "nccl" if args.impl == "cuda" else "gloo"
+        backend = backend or ("nccl" if args.impl == "cuda" else "gloo")
         dist.init_process_group(backend)
     return rank, world
+
+
+def select_device() -> int:
+    """CUDA ordinal of this process: LOCAL_RANK under torchrun (one process per GPU), else 0."""
+    return int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def open_device(args, set_device=None, make_context=None, backend=None):
+    """Makes this rank's GPU current (before the process group, so NCCL binds it), joins the
+    group, builds the library once per node (local rank 0; the others wait at a barrier) and opens
+    the backend's context on that GPU. Returns (rank, world, device, context)."""
+    dev = select_device()
+    if set_device is None:
+        import torch
+
+        set_device = torch.cuda.set_device
+    set_device(dev)
+    rank, world = dist_init(args, backend)
+    if make_context is None:
+        from verion_gb300 import build
+        from verion_gb300.backend import Context
+
+        if dev == 0:
+            build.build()
+        barrier(world)
+        if dev != 0:
+            build.build()  # finds the library up to date
+        make_context = Context
+    return rank, world, dev, make_context(device=dev)
 
 
 def barrier(world):
@@ -191,69 +220,68 @@ def traffic_per_ray():
     return None, None
 
 
-def cpu_baseline(packed, seconds: float, threads: int = 0):
-    """The oracle (single-precision restatement of the reference integrator) on a bounded row sample
-    of the same frame: 8 samples per pixel, every k-th row, all host threads."""
+def oracle_steps(packed, warmup: int, steps: int, step_seconds: float, threads: int = 0):
+    """The oracle (the reference's integrator restated in single precision) on a row sample of the
+    benchmark frame with the GPU arm's settings: adaptive sampling (0.02, 16), f64 sums, depth 16,
+    8 samples per step. `warmup` untimed steps, then `steps` timed ones on the same accumulation,
+    so the timed steps trace the pixels adaptive sampling left active, as the GPU arm's do (the
+    predicate reads a pixel's own statistics only, so a row sample evolves exactly like those rows
+    of the full frame). Every k-th row, k chosen so that a step with every pixel active takes about
+    `step_seconds`. Returns (Mpaths/s over the timed steps, seconds per timed step, sample text)."""
     import oracle
     from verion_gb300 import pack
+    from verion_gb300.readback import Adaptive
 
     o = oracle.OracleScene(packed)
     threads = threads or oracle.default_threads()
-    prm = pack.base_params(packed.info, packed.view, (WIDTH, HEIGHT), False, True, max_depth=DEPTH)
+    prm = pack.base_params(packed.info, packed.view, (WIDTH, HEIGHT), False, True, adaptive=Adaptive(*ADAPTIVE),
+                           max_depth=DEPTH)
+    probe = list(range(0, HEIGHT, 135))[:8]
+    acc = oracle.OracleAccumulation(WIDTH, HEIGHT, acc64=True, adaptive=True)
+    t0 = time.perf_counter()
+    oracle.render(o, prm, acc, SPP_STEP, threads=threads, rows=probe)
+    per_row = (time.perf_counter() - t0) / len(probe)
+    n = int(max(1, min(HEIGHT, step_seconds / max(per_row, 1e-6))))
+    stride = max(1, HEIGHT // n)
+    rows = list(range(stride // 2, HEIGHT, stride))[:n]
+    acc = oracle.OracleAccumulation(WIDTH, HEIGHT, acc64=True, adaptive=True)
 
-    def run(rows, spp):
-        acc = oracle.OracleAccumulation(WIDTH, HEIGHT)
-        t0 = time.perf_counter()
-        oracle.render(o, prm, acc, spp, threads=threads, rows=rows)
-        return time.perf_counter() - t0
+    def traced():
+        return float(acc.stats.reshape(-1, 3)[:, 0].sum())
 
-    probe_rows = list(range(0, HEIGHT, 135))[:8]
-    per_row = run(probe_rows, SPP_STEP) / len(probe_rows)
-    n = int(max(1, min(HEIGHT, seconds / max(per_row, 1e-6))))
-    step = max(1, HEIGHT // n)
-    rows = list(range(step // 2, HEIGHT, step))[:n]
-    # When the whole frame is faster than the target, trace more samples per pixel.
-    spp = SPP_STEP * max(1, int(round(seconds / max(len(rows) * per_row, 1e-6)))) if n == HEIGHT else SPP_STEP
-    dt = run(rows, spp)
-    paths = len(rows) * WIDTH * spp
-    return {"value": paths / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{len(rows)} of {HEIGHT} rows (every {step}th) x {WIDTH} px x {spp} spp, "
-                      f"single-precision oracle, {dt:.1f} s"}, dt
+    for _ in range(warmup):
+        oracle.render(o, prm, acc, SPP_STEP, threads=threads, rows=rows)
+    p0 = traced()
+    times = []
+    for _ in range(steps):
+        t = time.perf_counter()
+        oracle.render(o, prm, acc, SPP_STEP, threads=threads, rows=rows)
+        times.append(time.perf_counter() - t)
+    paths = traced() - p0
+    sample = (f"{len(rows)} of {HEIGHT} rows (every {stride}th) x {WIDTH} px, {warmup} untimed + {steps} timed "
+              f"steps of {SPP_STEP} spp with adaptive sampling {ADAPTIVE} and f64 sums, {paths:.0f} paths timed")
+    return paths / sum(times) / 1e6, times, sample, threads
+
+
+def cpu_baseline(packed, seconds: float, warmup: int, threads: int = 0):
+    """The oracle on a bounded row sample of the same workload (oracle_steps): the GPU arm's warm-up
+    steps, then two timed steps, about `seconds` of CPU work in all."""
+    per_step = seconds / (warmup + 2)
+    value, times, sample, threads = oracle_steps(packed, warmup, 2, per_step, threads)
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}, sum(times)
 
 
 def run_reference(args):
     rank, world = dist_init(args)
     if rank != 0:
         return 0
-    from verion_gb300 import pack
-    import oracle
-
     _, packed = workload()
-    o = oracle.OracleScene(packed)
-    threads = oracle.default_threads()
-    prm = pack.base_params(packed.info, packed.view, (WIDTH, HEIGHT), False, True, max_depth=DEPTH)
-    # Each step: a bounded sample of the frame (every k-th row) at 8 spp, sized to ~2 s.
-    t0 = time.perf_counter()
-    acc = oracle.OracleAccumulation(WIDTH, HEIGHT)
-    oracle.render(o, prm, acc, SPP_STEP, threads=threads, rows=list(range(0, HEIGHT, 135))[:8])
-    per_row = (time.perf_counter() - t0) / 8
-    n = int(max(1, min(HEIGHT, 2.0 / max(per_row, 1e-6))))
-    stride = max(1, HEIGHT // n)
-    rows = list(range(stride // 2, HEIGHT, stride))[:n]
-    times = []
-    for k in range(args.warmup + args.steps):
-        acc = oracle.OracleAccumulation(WIDTH, HEIGHT)
-        t = time.perf_counter()
-        oracle.render(o, prm, acc, SPP_STEP, threads=threads, rows=rows)
-        if k >= args.warmup:
-            times.append(time.perf_counter() - t)
-    paths = len(rows) * WIDTH * SPP_STEP * len(times)
-    value = paths / sum(times) / 1e6
-    sample = f"{len(rows)} of {HEIGHT} rows (every {stride}th) x {WIDTH} px x {SPP_STEP} spp per step"
+    # Each step: a bounded row sample of the frame at 8 spp, about 1.5 s with every pixel active.
+    value, times, sample, threads = oracle_steps(packed, args.warmup, args.steps, 1.5)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config(args, {"sums": "f32", "integrator": "megakernel (CPU)"}), "impl": "reference",
+            "config": config(args, {"integrator": "megakernel (CPU)"}), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -577,16 +605,13 @@ def restir_report(ctx):
 
 
 def run_cuda(args):
-    rank, world = dist_init(args)
+    rank, world, device, ctx = open_device(args)
     import torch
 
-    from verion_gb300 import build
-    from verion_gb300.backend import Context, Integrator, Renderer
+    from verion_gb300.backend import Integrator, Renderer
     from verion_gb300.readback import Adaptive
 
-    build.build()
     _, packed = workload()
-    ctx = Context()
     r = Renderer(ctx, packed)
     r.set_integrator(Integrator.WAVEFRONT if args.integrator == "wavefront" else Integrator.MEGAKERNEL)
     r.set_max_depth(DEPTH)
@@ -652,7 +677,7 @@ def run_cuda(args):
     launches0 = acc.launches()
     r.set_stage_timing(True)
     step_times = []
-    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+    with Clocks(device) as clk:
         for _ in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
@@ -769,7 +794,7 @@ def run_cuda(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu, _ = cpu_baseline(packed, args.cpu_seconds)
+        cpu, _ = cpu_baseline(packed, args.cpu_seconds, args.warmup)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -123,9 +123,16 @@ size_t vg_last_error(char* buf, size_t len);
 /* OutOfMemory details of the thread's last VG_ERR_OOM. */
 void vg_last_oom(uint64_t* needed, uint64_t* available);
 
-/* RayTracingBackend::context (lib.rs:18-19): opens device 0; VG_ERR_NO_DEVICE without a GPU,
- * VG_ERR_UNSUPPORTED unless it is an sm_103 device. */
+/* RayTracingBackend::context (lib.rs:18-19): opens the calling thread's current CUDA device (device
+ * 0 unless the caller selected another, e.g. one process per GPU under torchrun);
+ * VG_ERR_NO_DEVICE without a GPU, VG_ERR_UNSUPPORTED unless it is an sm_103 device. Every object
+ * made from a context belongs to its device: each call on it makes that device current for the
+ * call's duration and restores the caller's current device afterwards. */
 int vg_context_create(VgContext** out);
+/* The same on device `device` (an ordinal below cudaGetDeviceCount; VG_ERR_INVALID otherwise).
+ * The caller's current device is left as it was. No reference counterpart: the reference's
+ * backends open the system default device. */
+int vg_context_create_on(int device, VgContext** out);
 void vg_context_destroy(VgContext* ctx);
 /* RayTracingBackend::memory (lib.rs:20) */
 int vg_memory(VgContext* ctx, VgMemoryUsage* out);
@@ -319,6 +326,10 @@ int vg_trace_closest_device(VgRenderer* r, const float* d_rays, size_t n, uint32
  * it returns. Results are identical to vg_trace_closest's. */
 #define VG_TRACE_NOALLOC_MAX_RAYS 65536u
 int vg_trace_closest_noalloc(VgRenderer* r, const float* rays, size_t n, uint32_t* hits);
+
+/* Device allocations (cudaMalloc) and frees (cudaFree) this library has made since it was loaded,
+ * for tests of the allocation-free entry point. No reference counterpart. */
+void vg_debug_allocations(uint64_t* mallocs, uint64_t* frees);
 
 /* ---- Batched rendering (no reference counterpart) -----------------------------------------------
  * Many render requests in one persistent launch: the work items (16 x 8 pixel tiles with all of a

@@ -1,6 +1,6 @@
-"""Writes the golden fixtures of the test suite from the reference sources (run in a checkout
-that has the reference tree at REFERENCE_ROOT; the fixtures are committed, so the tests never
-read the reference).
+"""Writes the golden fixtures of the test suite from the reference sources. Run it with the
+environment variable REFERENCE_ROOT set to a checkout of the reference tree; the fixtures are
+committed, so the tests never read the reference.
 
 * albedo_sha256.json: sha256 of the reference's three albedo tables
   (crates/verion-gpu/tables/*.f32), which the in-tree generator must reproduce byte for byte.
@@ -13,11 +13,13 @@ import os
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REFERENCE_ROOT = Path(os.environ.get("REFERENCE_ROOT", "/root/reference"))
 
 
 def main() -> None:
-    tables = REFERENCE_ROOT / "crates" / "verion-gpu" / "tables"
+    root = os.environ.get("REFERENCE_ROOT")
+    if not root:
+        raise SystemExit("set REFERENCE_ROOT to the reference checkout")
+    tables = Path(root) / "crates" / "verion-gpu" / "tables"
     sums = {}
     for name in ("ggx_albedo.f32", "sheen_albedo.f32", "dielectric_albedo.f32"):
         data = (tables / name).read_bytes()

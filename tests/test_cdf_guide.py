@@ -1,8 +1,10 @@
-"""Guide tables of the environment map's CDF searches (verion_gb300/csrc/env_guide.h): the search
-started from a guide's range finds the entry the full search finds (pt_core.slang:274-306), for
-non-decreasing CDFs with flat runs, spikes, all-zero rows and a last entry below 1, and for u at
-the bucket edges, just below them, on the CDF's own values and at random. Compiled with g++ from
-the header the library uses."""
+"""Guide tables of the inverse-CDF searches (verion_gb300/csrc/cdf_guide.h): the search started
+from a guide's range finds the entry the full search finds (pt_core.slang:274-306, 1343-1352) for
+environment-sized guides (256 and 1024 buckets) and emitter-sized ones (the power of two at or
+above twice the entry count), for non-decreasing CDFs with flat runs, spikes, all-zero rows and a
+last entry below 1, for CDFs that decrease or hold NaN (negative or broken weights: the guide then
+falls back to the full search), and for u at the bucket edges, just below them, on the CDF's own
+values and at random. Compiled with g++ from the header the library uses."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -12,7 +14,7 @@ import pytest
 CSRC = Path(__file__).resolve().parent.parent / "verion_gb300" / "csrc"
 
 HARNESS = r"""
-#include "env_guide.h"
+#include "cdf_guide.h"
 #include <cmath>
 #include <cstdio>
 #include <random>
@@ -22,13 +24,12 @@ int main()
 {
     std::mt19937 rng(7);
     std::uniform_real_distribution<float> uni(0.0f, 1.0f);
-    const uint32_t sizes[] = {1, 2, 3, 17, 64, 1024, 2048};
-    const uint32_t buckets[] = {256, 1024};
-    long checked = 0;
-    for (int trial = 0; trial < 400; trial++) {
-        uint32_t n = sizes[rng() % 7];
+    const uint32_t sizes[] = {1, 2, 3, 17, 64, 1024, 2048, 4096};
+    long checked = 0, fallbacks = 0;
+    for (int trial = 0; trial < 560; trial++) {
+        uint32_t n = sizes[rng() % 8];
         std::vector<float> w(n);
-        int kind = trial % 5;
+        int kind = trial % 7;
         for (uint32_t i = 0; i < n; i++) {
             float x = uni(rng);
             if (kind == 0)
@@ -39,8 +40,12 @@ int main()
                 w[i] = ((i / 7) % 2) ? x : 0.0f;             // flat runs
             else if (kind == 3)
                 w[i] = 0.0f;                                 // an all-zero row
-            else
+            else if (kind == 4)
                 w[i] = x * x * x * x;                        // strongly skewed
+            else if (kind == 5)
+                w[i] = x - 0.3f;                             // negative weights: the CDF decreases
+            else
+                w[i] = (i == n / 2) ? NAN : x;               // a broken weight
         }
         std::vector<float> cdf(n);
         double total = 0.0;
@@ -50,14 +55,17 @@ int main()
         for (uint32_t i = 0; i < n; i++) {
             run += w[i];
             cdf[i] = total > 0.0 ? (float)(run / total) : 0.0f;
-            if (i > 0 && cdf[i] < cdf[i - 1])
+            if (kind < 5 && i > 0 && cdf[i] < cdf[i - 1])
                 cdf[i] = cdf[i - 1]; // keep it non-decreasing, as the packer's is
         }
         if (trial % 3 == 0 && n > 0 && total > 0.0)
             cdf[n - 1] = std::nextafter(1.0f, 0.0f); // last entry just below 1
+        const uint32_t buckets[] = {256, 1024, cdfg::emitter_guide_buckets(n)};
         for (uint32_t K : buckets) {
             std::vector<uint32_t> g(K + 1);
-            envg::build_guide(cdf.data(), n, K, g.data());
+            cdfg::build_guide(cdf.data(), n, K, g.data());
+            if (!cdfg::non_decreasing(cdf.data(), n))
+                fallbacks++;
             std::vector<float> us;
             for (uint32_t k = 0; k < K; k++) {
                 float e = (float)k / (float)K;
@@ -79,8 +87,8 @@ int main()
             for (float u : us) {
                 if (!(u >= 0.0f && u < 1.0f))
                     continue;
-                uint32_t a = envg::cdf_search(cdf.data(), n, u);
-                uint32_t b = envg::guided_search(cdf.data(), g.data(), K, u);
+                uint32_t a = cdfg::cdf_search(cdf.data(), n, u);
+                uint32_t b = cdfg::guided_search(cdf.data(), n, g.data(), K, u);
                 if (a != b) {
                     std::printf("mismatch n=%u K=%u u=%.9g full=%u guided=%u\n", n, K, u, a, b);
                     return 1;
@@ -88,6 +96,10 @@ int main()
                 checked++;
             }
         }
+    }
+    if (fallbacks == 0) {
+        std::printf("no CDF took the full-search fallback\n");
+        return 1;
     }
     std::printf("ok %ld\n", checked);
     return 0;

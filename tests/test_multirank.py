@@ -1,6 +1,7 @@
 """The N > 1 paths of bench.py on CPU: two ranks over gloo (127.0.0.1). The per-rank numbers are
-combined as a multi-GPU run reports them (max of the times, sum of the paths), and under torchrun
-only rank 0 runs the reference arm: the other ranks join the rendezvous and exit 0 without work."""
+combined as a multi-GPU run reports them (max of the times, sum of the paths), under torchrun
+only rank 0 runs the reference arm (the other ranks join the rendezvous and exit 0 without work),
+and each rank of the CUDA arm selects GPU LOCAL_RANK for torch and for the backend's context."""
 import multiprocessing as mp
 import os
 import socket
@@ -60,3 +61,44 @@ def test_two_gloo_ranks_combine_and_only_rank0_runs_the_reference():
     assert ("reference", 1, 0) in msgs
     reduces = {m[1]: m[2] for m in msgs if m[0] == "reduce"}
     assert reduces == {0: (2.5, 3.0), 1: (2.5, 3.0)}
+
+
+class _FakeContext:
+    def __init__(self, device=None):
+        self.device = device
+
+
+def _device_rank(rank: int, world: int, port: int, q):
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank), MASTER_ADDR="127.0.0.1",
+                      MASTER_PORT=str(port))
+    import torch.distributed as dist
+
+    import bench
+
+    chosen = []
+    args = SimpleNamespace(impl="cuda", gpus=world, steps=1, warmup=1)
+    r, w, dev, ctx = bench.open_device(args, set_device=chosen.append, make_context=_FakeContext, backend="gloo")
+    q.put(("device", rank, (r, w, dev, chosen, ctx.device)))
+    dist.destroy_process_group()
+
+
+def test_each_rank_opens_its_local_gpu():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_device_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    msgs = []
+    try:
+        for _ in range(2):
+            msgs.append(q.get(timeout=120))
+    finally:
+        for p in procs:
+            p.join(timeout=60)
+            if p.exitcode is None:
+                p.kill()
+    assert [p.exitcode for p in procs] == [0, 0], msgs
+    got = {m[1]: m[2] for m in msgs}
+    # rank, world, the ordinal given to torch.cuda.set_device, and the one the context was opened on
+    assert got == {0: (0, 2, 0, [0], 0), 1: (1, 2, 1, [1], 1)}

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from verion_gb300 import pack, scenes
-from verion_gb300.backend import VG_TRACE_NOALLOC_MAX_RAYS, Error, Renderer
+from verion_gb300.backend import VG_TRACE_NOALLOC_MAX_RAYS, Error, Renderer, device_allocations
 
 pytestmark = pytest.mark.gpu
 
@@ -29,10 +29,13 @@ def test_noalloc_matches_trace_closest_twice(gpu_ctx, scene):
     r = Renderer(gpu_ctx, p)
     for b in batches:
         want = r.trace_closest(b)
+        before = device_allocations()
         # Two calls in a row: the fetch counter and error flag are cleared per call.
         for call in range(2):
             got = r.trace_closest_noalloc(b)
             assert np.array_equal(got, want), f"{scene}: call {call}, {len(b)} rays"
+        # The property the entry point exists for: no cudaMalloc and no cudaFree in either call.
+        assert device_allocations() == before
         assert want[:, 0].any()
 
 

@@ -179,6 +179,8 @@ def lib() -> C.CDLL:
             "vg_last_error": (_S, [C.c_char_p, _S]),
             "vg_last_oom": (None, [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
             "vg_context_create": (i32, [C.POINTER(vp)]),
+            "vg_context_create_on": (i32, [i32, C.POINTER(vp)]),
+            "vg_debug_allocations": (None, [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
             "vg_context_destroy": (None, [vp]),
             "vg_memory": (i32, [vp, C.POINTER(MemoryUsage)]),
             "vg_renderer_create": (i32, [vp, C.POINTER(_Packed), C.POINTER(vp)]),
@@ -257,6 +259,13 @@ def lib() -> C.CDLL:
     return _lib
 
 
+def device_allocations() -> tuple:
+    """(cudaMalloc calls, cudaFree calls) the library has made since it was loaded."""
+    m, f = C.c_uint64(), C.c_uint64()
+    lib().vg_debug_allocations(C.byref(m), C.byref(f))
+    return m.value, f.value
+
+
 def _check(status: int) -> None:
     if status != VG_OK:
         L = lib()
@@ -292,12 +301,17 @@ class Aovs:
 
 
 class Context:
-    """The device and its stream (`RayTracingBackend::Context`)."""
+    """The device and its stream (`RayTracingBackend::Context`). `device` is a CUDA ordinal; None
+    opens the calling thread's current device (device 0 unless the caller selected another)."""
 
-    def __init__(self):
+    def __init__(self, device: Optional[int] = None):
         h = C.c_void_p()
-        _check(lib().vg_context_create(C.byref(h)))
+        if device is None:
+            _check(lib().vg_context_create(C.byref(h)))
+        else:
+            _check(lib().vg_context_create_on(int(device), C.byref(h)))
         self._h = h
+        self.device = device
 
     def memory(self) -> MemoryUsage:
         m = MemoryUsage()

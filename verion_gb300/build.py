@@ -9,6 +9,7 @@ with a CPU restatement possible.
 """
 from __future__ import annotations
 
+import fcntl
 import os
 import shutil
 import subprocess
@@ -30,7 +31,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", str(CSRC)]
 
 CU_SOURCES = ["kern_mk.cu", "kern_wf.cu", "kern_nrc.cu", "kern_batch.cu", "vgcuda.cu", "cache.cu", "batch.cu"]
 CXX_SOURCES = ["bvh_build.cpp", "exr.cpp"]
-DEPS = ["vg_math.h", "host.h", "env_guide.h", "tc.cuh", "nrc.cuh", "nrc_device.cuh", "vg_layout.h", "vec3.h", "bvh8.h", "traverse.cuh", "pt_device.cuh", "kernels.cuh",
+DEPS = ["vg_math.h", "host.h", "cdf_guide.h", "tc.cuh", "nrc.cuh", "nrc_device.cuh", "vg_layout.h", "vec3.h", "bvh8.h", "traverse.cuh", "pt_device.cuh", "kernels.cuh",
         "launch.h", "launch_nrc.h", "launch_batch.h", "batch.h", "cache_host.h", "bvh_build.h"]
 
 
@@ -57,11 +58,22 @@ def _run(cmd: list[str]) -> None:
 
 def build(force: bool = False, verbose: bool = False, defines=(), build_dir: Path = None) -> Path:
     """Compiles the library if any source is newer than it; returns its path. `defines` adds
-    preprocessor definitions (e.g. "VG_SHADE_MIN_BLOCKS=4") for a variant built in `build_dir`."""
+    preprocessor definitions (e.g. "VG_SHADE_MIN_BLOCKS=4") for a variant built in `build_dir`.
+    Processes that build into the same folder at once take turns (an exclusive lock on
+    `<build>/.lock`), so none of them loads a half-written library."""
     BUILD = Path(build_dir) if build_dir else globals()["BUILD"]
+    BUILD.mkdir(parents=True, exist_ok=True)
+    with open(BUILD / ".lock", "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            return _build_locked(BUILD, force, verbose, defines)
+        finally:
+            fcntl.flock(lock, fcntl.LOCK_UN)
+
+
+def _build_locked(BUILD: Path, force: bool, verbose: bool, defines) -> Path:
     LIB = BUILD / "libvgcuda.so"
     extra = [f"-D{d}" for d in defines]
-    BUILD.mkdir(parents=True, exist_ok=True)
     nvcc = _nvcc()
     cxx = shutil.which("g++") or "g++"
     jobs = []
@@ -83,7 +95,7 @@ def build(force: bool = False, verbose: bool = False, defines=(), build_dir: Pat
                     print(" ".join(cmd), file=sys.stderr)
             list(ex.map(_run, jobs))
     if force or jobs or not LIB.exists():
-        tmp = BUILD / "libvgcuda.so.tmp"
+        tmp = BUILD / f"libvgcuda.so.{os.getpid()}.tmp"
         _run([nvcc] + ARCH + ["-shared", "-o", str(tmp)] + [str(o) for o in objs])
         os.replace(tmp, LIB)
     return LIB

@@ -309,6 +309,7 @@ extern "C" {
 int vg_batch_render(VgContext* ctx, const VgBatchRequest* requests, size_t n, VgBatchResult* out,
                     double* total_seconds, int* graph_replayed)
 {
+    DevGuard device_guard(dev_of(ctx));
     if (!ctx)
         return fail(VG_ERR_INVALID, "null context");
     return batch_run(ctx, requests, n, ctx->batch_blocks_per_sm, ctx->batch_order, ctx->batch_wavefront_pixels, out,
@@ -317,6 +318,7 @@ int vg_batch_render(VgContext* ctx, const VgBatchRequest* requests, size_t n, Vg
 
 int vg_batch_kernel_info(VgContext* ctx, int out[5])
 {
+    DevGuard device_guard(dev_of(ctx));
     if (!ctx || !out)
         return fail(VG_ERR_INVALID, "null argument");
     out[0] = vgx::batch_kernel_info(&out[1], &out[2], &out[3], &out[4]);
@@ -335,6 +337,7 @@ int vg_set_batch_options(VgContext* ctx, int blocks_per_sm, int order, uint64_t 
 
 int vg_batch_tune(VgContext* ctx, const VgBatchRequest* requests, size_t n, VgBatchTune* out)
 {
+    DevGuard device_guard(dev_of(ctx));
     if (!ctx || !requests || n == 0 || !out)
         return fail(VG_ERR_INVALID, "null argument");
     // Scratch accumulations of the requests' sizes and precision, so theirs stay untouched.

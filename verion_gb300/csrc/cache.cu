@@ -320,6 +320,7 @@ int vg_renderer_bounds(const VgRenderer* r, float lo[3], float hi[3])
 
 int vg_cache_create(VgContext* ctx, const VgCacheConfig* cfg, VgCache** out)
 {
+    DevGuard device_guard(dev_of(ctx));
     if (!ctx || !cfg || !out)
         return fail(VG_ERR_INVALID, "null argument");
     *out = nullptr;
@@ -393,6 +394,7 @@ int vg_cache_create(VgContext* ctx, const VgCacheConfig* cfg, VgCache** out)
 
 int vg_cache_destroy(VgCache* cache)
 {
+    DevGuard device_guard(dev_of(cache));
     delete cache;
     return VG_OK;
 }
@@ -410,6 +412,7 @@ int vg_cache_param_counts(const VgCache* k, size_t* mlp, size_t* grid)
 
 int vg_cache_read_params(VgCache* k, float* mlp, float* grid)
 {
+    DevGuard device_guard(dev_of(k));
     if (!k)
         return fail(VG_ERR_INVALID, "null cache");
     cudaStream_t s = k->ctx->stream;
@@ -423,6 +426,7 @@ int vg_cache_read_params(VgCache* k, float* mlp, float* grid)
 
 int vg_cache_write_params(VgCache* k, const float* mlp, const float* grid)
 {
+    DevGuard device_guard(dev_of(k));
     if (!k)
         return fail(VG_ERR_INVALID, "null cache");
     cudaStream_t s = k->ctx->stream;
@@ -439,6 +443,7 @@ int vg_cache_write_params(VgCache* k, const float* mlp, const float* grid)
 
 int vg_cache_infer(VgCache* k, const float* records, size_t n, float* out)
 {
+    DevGuard device_guard(dev_of(k));
     if (!k || (n > 0 && (!records || !out)))
         return fail(VG_ERR_INVALID, "null argument");
     if (n > 0x7fffffffull)
@@ -466,6 +471,7 @@ int vg_cache_infer(VgCache* k, const float* records, size_t n, float* out)
 
 int vg_cache_gradients(VgCache* k, const float* records, size_t n, float* mlp_grad, float* grid_grad, double* loss)
 {
+    DevGuard device_guard(dev_of(k));
     if (!k || (n > 0 && !records))
         return fail(VG_ERR_INVALID, "null argument");
     if (n > 0x7fffffffull)
@@ -500,6 +506,7 @@ int vg_cache_gradients(VgCache* k, const float* records, size_t n, float* mlp_gr
 
 int vg_cache_train(VgCache* k, const float* records, size_t n, uint32_t batch, double* last_loss)
 {
+    DevGuard device_guard(dev_of(k));
     if (!k || (n > 0 && !records))
         return fail(VG_ERR_INVALID, "null argument");
     if (batch == 0 || n > 0x7fffffffull)
@@ -528,6 +535,7 @@ int vg_cache_train(VgCache* k, const float* records, size_t n, uint32_t batch, d
 
 int vg_cache_time(VgCache* k, const float* records, size_t n, uint32_t reps, double out[4])
 {
+    DevGuard device_guard(dev_of(k));
     if (!k || !records || !out || n == 0 || reps == 0)
         return fail(VG_ERR_INVALID, "null argument or empty input");
     if (n > 0x7fffffffull)

@@ -43,6 +43,10 @@ struct VgCache {
     }
 };
 
+namespace {
+int dev_of(const VgCache* k) { return k ? dev_of(k->ctx) : -1; }
+} // namespace
+
 namespace vgc {
 
 int cache_check(const VgCache* k);

@@ -10,10 +10,11 @@ namespace vgd {
 
 using namespace vgl;
 
-// Guide tables of the environment map's CDF searches (the cutpoint method): for a CDF of n entries
-// and K buckets (K a power of two, so u K is exact), entry k is the search's answer for u = k / K,
-// k = 0..K; every u with floor(u K) = k then has its answer between entries k and k + 1. Layout:
-// the marginal's K_M + 1 entries, then K_C + 1 entries per row of the conditional.
+// Guide tables of the CDF searches (the cutpoint method, cdf_guide.h): for a CDF of n entries and
+// K buckets (K a power of two, so u K is exact), entry k is the search's answer for u = k / K,
+// k = 0..K; every u with floor(u K) = k then has its answer between entries k and k + 1 (a bucket
+// whose entries are reversed, lo > hi, means "search all n entries"). Environment layout: the
+// marginal's K_M + 1 entries, then K_C + 1 entries per row of the conditional.
 constexpr uint32_t ENV_GUIDE_M = 1024;
 constexpr uint32_t ENV_GUIDE_C = 256;
 
@@ -30,6 +31,8 @@ struct DeviceScene {
     const float* env_marginal;
     const float* env_cond;
     const uint32_t* env_guide; // search ranges for env_marginal and env_cond (ENV_GUIDE_*)
+    const uint32_t* emit_guide; // search ranges for emit_cdf: emit_guide_k + 1 entries
+    uint32_t emit_guide_k;      // buckets of emit_guide (a power of two)
     const float* uvs;
     const float* texels;
     const uint32_t* tex_info;

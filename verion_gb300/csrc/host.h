@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstring>
 #include <string>
@@ -90,6 +91,16 @@ int wait_event(cudaEvent_t ev)
     }
 }
 
+} // namespace
+
+namespace vgh {
+// Device allocations and frees made by this library since it was loaded (all of them go through
+// alloc() and DevBuf), readable through vg_debug_allocations.
+inline std::atomic<uint64_t> g_mallocs{0}, g_frees{0};
+} // namespace vgh
+
+namespace {
+
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
@@ -99,11 +110,35 @@ struct DevBuf {
     ~DevBuf() { release(); }
     void release()
     {
-        if (p)
+        if (p) {
             cudaFree(p);
+            vgh::g_frees++;
+        }
         p = nullptr;
         bytes = 0;
     }
+};
+
+// Makes `device` the calling thread's current device for one entry-point call and restores the
+// caller's device when the call returns (a negative ordinal leaves everything as it is). Every
+// object of the C ABI belongs to its context's device; with this guard a caller that drives
+// several devices from one thread can interleave calls on their objects freely.
+struct DevGuard {
+    int prev = -1;
+    explicit DevGuard(int device)
+    {
+        int cur = -1;
+        if (device >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != device &&
+            cudaSetDevice(device) == cudaSuccess)
+            prev = cur;
+    }
+    ~DevGuard()
+    {
+        if (prev >= 0)
+            cudaSetDevice(prev);
+    }
+    DevGuard(const DevGuard&) = delete;
+    DevGuard& operator=(const DevGuard&) = delete;
 };
 
 } // namespace
@@ -139,7 +174,7 @@ constexpr uint32_t CACHE_WARMUP_SAMPLE = 0x40000000u; // first sample index of c
 
 struct VgRenderer {
     VgContext* ctx = nullptr;
-    DevBuf positions, indices, uvs, vnormals, instances, materials, lights, emitters, emit_cdf, env_pixels,
+    DevBuf positions, indices, uvs, vnormals, instances, materials, lights, emitters, emit_cdf, emit_guide, env_pixels,
         env_marginal, env_cond, env_guide, texels, tex_info, nodes, tris, err, scratch;
     vgd::DeviceScene ds{};
     VgSceneInfo info{};
@@ -220,6 +255,11 @@ struct VgAccum {
 
 namespace {
 
+// The device an object of the C ABI belongs to (-1 for a null handle).
+int dev_of(const VgContext* ctx) { return ctx ? ctx->device : -1; }
+int dev_of(const VgRenderer* r) { return r && r->ctx ? r->ctx->device : -1; }
+int dev_of(const VgAccum* acc) { return acc ? dev_of(acc->owner) : -1; }
+
 int check_fits(size_t bytes)
 {
     size_t free_b = 0, total_b = 0;
@@ -247,6 +287,7 @@ int alloc(DevBuf& b, size_t bytes, cudaStream_t s, bool zero)
         b.p = nullptr;
         return cuda_fail(e, "cudaMalloc");
     }
+    vgh::g_mallocs++;
     b.bytes = n;
     if (zero) {
         e = cudaMemsetAsync(b.p, 0, n, s);

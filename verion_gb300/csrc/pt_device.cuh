@@ -235,36 +235,39 @@ static __device__ __forceinline__ float envPdf(const Ctx& c, V3 d)
     return lum(envTexel(c, i, j)) * pf(c, P_ENV_PDF_SCALE);
 }
 
-// pt_core.slang:274-306. Each CDF search is the reference's: the first entry >= u (the last entry
-// when none is); it starts from the guide table's range for u's bucket, which holds that entry, so
-// it ends at the same one after a few steps instead of log2(n).
+// The reference's inverse-CDF search (pt_core.slang:274-306, 1343-1352): the first of the n entries
+// of `cdf` that is >= u, the last when none is. It starts from the guide table's range for u's
+// bucket (K buckets, cdf_guide.h), which holds that entry, so it ends at the same one after a few
+// steps instead of log2(n) dependent loads; a reversed range (lo > hi) marks a CDF that is not
+// non-decreasing, searched over all n entries.
+static __device__ __forceinline__ uint32_t guidedCdf(const float* cdf, uint32_t n, const uint32_t* guide, uint32_t K,
+                                                     float u)
+{
+    uint32_t k = min((uint32_t)(u * (float)K), K - 1);
+    uint32_t lo = __ldg(guide + k), hi = __ldg(guide + k + 1);
+    if (lo > hi) {
+        lo = 0;
+        hi = n - 1;
+    }
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) / 2;
+        if (fget(cdf, mid) >= u)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    return lo;
+}
+
+// pt_core.slang:274-306, each CDF search through its guide table.
 static __device__ __noinline__ V3 envSample(const Ctx& c, float u1, float u2, float u3, float u4, float& pdf, V3& le)
 {
     uint32_t w = c.p[P_ENV_W];
     uint32_t h = c.p[P_ENV_H];
     const uint32_t* g = c.s.env_guide;
-    uint32_t k = min((uint32_t)(u1 * (float)ENV_GUIDE_M), ENV_GUIDE_M - 1);
-    uint32_t lo = g[k], hi = g[k + 1];
-    while (lo < hi) {
-        uint32_t mid = (lo + hi) / 2;
-        if (fget(c.s.env_marginal, mid) >= u1)
-            hi = mid;
-        else
-            lo = mid + 1;
-    }
-    uint32_t j = lo;
-    const uint32_t* gr = g + (ENV_GUIDE_M + 1) + j * (ENV_GUIDE_C + 1);
-    k = min((uint32_t)(u2 * (float)ENV_GUIDE_C), ENV_GUIDE_C - 1);
-    lo = gr[k];
-    hi = gr[k + 1];
-    while (lo < hi) {
-        uint32_t mid = (lo + hi) / 2;
-        if (fget(c.s.env_cond, j * w + mid) >= u2)
-            hi = mid;
-        else
-            lo = mid + 1;
-    }
-    uint32_t i = lo;
+    uint32_t j = guidedCdf(c.s.env_marginal, h, g, ENV_GUIDE_M, u1);
+    uint32_t i = guidedCdf(c.s.env_cond + (size_t)j * w, w, g + (ENV_GUIDE_M + 1) + j * (ENV_GUIDE_C + 1), ENV_GUIDE_C,
+                           u2);
     float phi = (((float)i + u3) / (float)w - 0.5f) * 2.0f * PI;
     float theta = (((float)j + u4) / (float)h) * PI;
     float st = vgm::sinf_(theta);
@@ -685,14 +688,7 @@ static __device__ __noinline__ RestirPick restirDI(const Ctx& c, uint32_t pixel,
         float ue = rng.next();
         float ua = rng.next();
         float ub = rng.next();
-        uint32_t lo = 0, hi = emitterCount - 1;
-        while (lo < hi) {
-            uint32_t mid = (lo + hi) / 2;
-            if (fget(c.s.emit_cdf, mid) >= ue)
-                hi = mid;
-            else
-                lo = mid + 1;
-        }
+        uint32_t lo = guidedCdf(c.s.emit_cdf, emitterCount, c.s.emit_guide, c.s.emit_guide_k, ue);
         uint32_t o = lo * 16;
         V3 a = v3(fget(E, o), fget(E, o + 1), fget(E, o + 2));
         V3 b = v3(fget(E, o + 3), fget(E, o + 4), fget(E, o + 5));
@@ -1329,14 +1325,7 @@ __device__ bool shadePath(const Ctx& c, PathState<LIGHT>& st, Hit hq, uint32_t d
             float ue = rng.next();
             float ua = rng.next();
             float ub = rng.next();
-            uint32_t lo = 0, hi = emitterCount - 1;
-            while (lo < hi) {
-                uint32_t mid = (lo + hi) / 2;
-                if (fget(c.s.emit_cdf, mid) >= ue)
-                    hi = mid;
-                else
-                    lo = mid + 1;
-            }
+            uint32_t lo = guidedCdf(c.s.emit_cdf, emitterCount, c.s.emit_guide, c.s.emit_guide_k, ue);
             uint32_t e = lo * 16;
             const float* E = c.s.emitters;
             V3 a = v3(fget(E, e), fget(E, e + 1), fget(E, e + 2));

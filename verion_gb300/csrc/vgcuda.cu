@@ -24,7 +24,7 @@
 #include "bvh_build.h"
 #include "launch.h"
 
-#include "env_guide.h"
+#include "cdf_guide.h"
 #include "host.h"
 
 // Sets the thread's error text for translation units compiled without the CUDA headers.
@@ -96,7 +96,7 @@ bool translucent_materials(const VgPacked* pk)
     return false;
 }
 
-// Guide tables of the environment's CDF searches (env_guide.h; sizes vgd::ENV_GUIDE_M / ENV_GUIDE_C):
+// Guide tables of the environment's CDF searches (cdf_guide.h; sizes vgd::ENV_GUIDE_M / ENV_GUIDE_C):
 // the marginal's, then one per row of the conditional.
 std::vector<uint32_t> env_guide(const VgPacked* pk)
 {
@@ -104,10 +104,22 @@ std::vector<uint32_t> env_guide(const VgPacked* pk)
     if (w == 0 || h == 0)
         return std::vector<uint32_t>(vgd::ENV_GUIDE_M + 1, 0u);
     std::vector<uint32_t> g((vgd::ENV_GUIDE_M + 1) + (size_t)h * (vgd::ENV_GUIDE_C + 1));
-    envg::build_guide(pk->env_marginal, h, vgd::ENV_GUIDE_M, g.data());
+    cdfg::build_guide(pk->env_marginal, h, vgd::ENV_GUIDE_M, g.data());
     for (uint32_t j = 0; j < h; j++)
-        envg::build_guide(pk->env_conditional + (size_t)j * w, w, vgd::ENV_GUIDE_C,
+        cdfg::build_guide(pk->env_conditional + (size_t)j * w, w, vgd::ENV_GUIDE_C,
                           g.data() + (vgd::ENV_GUIDE_M + 1) + (size_t)j * (vgd::ENV_GUIDE_C + 1));
+    return g;
+}
+
+// Guide table of the emitter CDF's searches (cdf_guide.h): cdfg::emitter_guide_buckets(n) + 1
+// entries.
+std::vector<uint32_t> emitter_guide(const VgPacked* pk)
+{
+    uint32_t n = pk->info.emitter_count;
+    uint32_t K = cdfg::emitter_guide_buckets(n);
+    std::vector<uint32_t> g(K + 1, 0u);
+    if (n > 0)
+        cdfg::build_guide(pk->emit_cdf, n, K, g.data());
     return g;
 }
 
@@ -144,6 +156,8 @@ void bind_tables(VgRenderer* r)
     r->ds.env_marginal = (const float*)r->env_marginal.p;
     r->ds.env_cond = (const float*)r->env_cond.p;
     r->ds.env_guide = (const uint32_t*)r->env_guide.p;
+    r->ds.emit_guide = (const uint32_t*)r->emit_guide.p;
+    r->ds.emit_guide_k = cdfg::emitter_guide_buckets(r->info.emitter_count);
     r->ds.uvs = (const float*)r->uvs.p;
     r->ds.texels = (const float*)r->texels.p;
     r->ds.tex_info = (const uint32_t*)r->tex_info.p;
@@ -384,7 +398,7 @@ void vg_last_oom(uint64_t* needed, uint64_t* available)
         *available = g_oom_available;
 }
 
-int vg_context_create(VgContext** out)
+int vg_context_create_on(int device, VgContext** out)
 {
     if (!out)
         return fail(VG_ERR_INVALID, "null output pointer");
@@ -394,13 +408,16 @@ int vg_context_create(VgContext** out)
         cudaGetLastError();
         return fail(VG_ERR_NO_DEVICE, "no CUDA device");
     }
+    if (device < 0 || device >= n)
+        return fail(VG_ERR_INVALID, "device ordinal " + std::to_string(device) + " out of range (" +
+                                        std::to_string(n) + " devices)");
     cudaDeviceProp prop;
-    VG_CHECK(cudaGetDeviceProperties(&prop, 0), "cudaGetDeviceProperties");
+    VG_CHECK(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
     if (prop.major != 10 || prop.minor != 3)
         return fail(VG_ERR_UNSUPPORTED, std::string("device ") + prop.name + " is not sm_103 (GB300)");
-    VG_CHECK(cudaSetDevice(0), "cudaSetDevice");
+    DevGuard device_guard(device);
     VgContext* ctx = new VgContext();
-    ctx->device = 0;
+    ctx->device = device;
     ctx->sms = prop.multiProcessorCount;
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -411,8 +428,27 @@ int vg_context_create(VgContext** out)
     return VG_OK;
 }
 
+int vg_context_create(VgContext** out)
+{
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) {
+        cudaGetLastError();
+        device = 0;
+    }
+    return vg_context_create_on(device, out);
+}
+
+void vg_debug_allocations(uint64_t* mallocs, uint64_t* frees)
+{
+    if (mallocs)
+        *mallocs = vgh::g_mallocs.load();
+    if (frees)
+        *frees = vgh::g_frees.load();
+}
+
 void vg_context_destroy(VgContext* ctx)
 {
+    DevGuard device_guard(dev_of(ctx));
     if (!ctx)
         return;
     cudaStreamSynchronize(ctx->stream);
@@ -430,6 +466,7 @@ void vg_context_destroy(VgContext* ctx)
 
 int vg_memory(VgContext* ctx, VgMemoryUsage* out)
 {
+    DevGuard device_guard(dev_of(ctx));
     if (!ctx || !out)
         return fail(VG_ERR_INVALID, "null argument");
     size_t free_b = 0, total_b = 0;
@@ -442,6 +479,7 @@ int vg_memory(VgContext* ctx, VgMemoryUsage* out)
 
 int vg_renderer_create(VgContext* ctx, const VgPacked* pk, VgRenderer** out)
 {
+    DevGuard device_guard(dev_of(ctx));
     if (!ctx || !pk || !out)
         return fail(VG_ERR_INVALID, "null argument");
     *out = nullptr;
@@ -477,6 +515,10 @@ int vg_renderer_create(VgContext* ctx, const VgPacked* pk, VgRenderer** out)
     UP(lights, pk->lights, pk->lights_len * 4);
     UP(emitters, pk->emitters, pk->emitters_len * 4);
     UP(emit_cdf, pk->emit_cdf, pk->emit_cdf_len * 4);
+    {
+        std::vector<uint32_t> guide = emitter_guide(pk);
+        UP(emit_guide, guide.data(), guide.size() * 4);
+    }
     UP(env_pixels, pk->env_pixels, pk->env_pixels_len * 4);
     UP(env_marginal, pk->env_marginal, pk->env_marginal_len * 4);
     UP(env_cond, pk->env_conditional, pk->env_conditional_len * 4);
@@ -510,12 +552,14 @@ int vg_renderer_create(VgContext* ctx, const VgPacked* pk, VgRenderer** out)
 
 void vg_renderer_destroy(VgRenderer* r)
 {
+    DevGuard device_guard(dev_of(r));
     // As vg_accum_destroy: frees device memory only, independent of the context's lifetime.
     delete r;
 }
 
 int vg_renderer_update(VgRenderer* r, const VgPacked* pk, const VgUpdatePlan* plan, VgUpdateReport* out)
 {
+    DevGuard device_guard(dev_of(r));
     if (!r || !pk || !plan || !out)
         return fail(VG_ERR_INVALID, "null argument");
     memset(out, 0, sizeof(*out));
@@ -530,10 +574,10 @@ int vg_renderer_update(VgRenderer* r, const VgPacked* pk, const VgUpdatePlan* pl
         if ((st = vg_renderer_create(ctx, pk, &f)) != VG_OK)
             return st;
         DevBuf* mine[] = {&r->positions, &r->indices, &r->uvs, &r->vnormals, &r->instances, &r->materials,
-                          &r->lights, &r->emitters, &r->emit_cdf, &r->env_pixels, &r->env_marginal, &r->env_cond,
+                          &r->lights, &r->emitters, &r->emit_cdf, &r->emit_guide, &r->env_pixels, &r->env_marginal, &r->env_cond,
                           &r->env_guide, &r->texels, &r->tex_info, &r->nodes, &r->tris};
         DevBuf* theirs[] = {&f->positions, &f->indices, &f->uvs, &f->vnormals, &f->instances, &f->materials,
-                            &f->lights, &f->emitters, &f->emit_cdf, &f->env_pixels, &f->env_marginal, &f->env_cond,
+                            &f->lights, &f->emitters, &f->emit_cdf, &f->emit_guide, &f->env_pixels, &f->env_marginal, &f->env_cond,
                             &f->env_guide, &f->texels, &f->tex_info, &f->nodes, &f->tris};
         uint64_t bytes = 0;
         for (size_t i = 0; i < sizeof(mine) / sizeof(mine[0]); i++) {
@@ -629,7 +673,10 @@ int vg_renderer_update(VgRenderer* r, const VgPacked* pk, const VgUpdatePlan* pl
         if ((st = upload(ctx, r->emitters, pk->emitters, pk->emitters_len * 4)) != VG_OK ||
             (st = upload(ctx, r->emit_cdf, pk->emit_cdf, pk->emit_cdf_len * 4)) != VG_OK)
             return st;
-        bytes += (pk->emitters_len + pk->emit_cdf_len) * 4;
+        std::vector<uint32_t> guide = emitter_guide(pk);
+        if ((st = upload(ctx, r->emit_guide, guide.data(), guide.size() * 4)) != VG_OK)
+            return st;
+        bytes += (pk->emitters_len + pk->emit_cdf_len + guide.size()) * 4;
         r->info.emitter_count = pk->info.emitter_count;
     }
     if (plan->instances) {
@@ -657,6 +704,7 @@ int vg_renderer_update(VgRenderer* r, const VgPacked* pk, const VgUpdatePlan* pl
 
 int vg_set_bvh_traversal_cost(VgRenderer* r, const VgPacked* pk, float cost)
 {
+    DevGuard device_guard(dev_of(r));
     if (!r || !pk)
         return fail(VG_ERR_INVALID, "null argument");
     if (!(cost > 0.0f && cost <= 16.0f))
@@ -828,6 +876,7 @@ int vg_set_accum_precision(VgRenderer* r, int bits)
 
 int vg_accum_create(VgRenderer* r, uint32_t width, uint32_t height, int lighting, VgAccum** out)
 {
+    DevGuard device_guard(dev_of(r));
     if (!r || !out)
         return fail(VG_ERR_INVALID, "null argument");
     *out = nullptr;
@@ -861,6 +910,7 @@ int vg_accum_create(VgRenderer* r, uint32_t width, uint32_t height, int lighting
 
 void vg_accum_destroy(VgAccum* acc)
 {
+    DevGuard device_guard(dev_of(acc));
     // Frees device memory only (cudaFree waits for work in flight); it does not touch the
     // renderer or context, so handles may be destroyed in any order.
     delete acc;
@@ -868,6 +918,7 @@ void vg_accum_destroy(VgAccum* acc)
 
 int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
 {
+    DevGuard device_guard(dev_of(r));
     if (!r || !acc || acc->owner != r)
         return fail(VG_ERR_INVALID, "accumulation does not belong to this renderer");
     cudaStream_t s = r->ctx->stream;
@@ -1083,6 +1134,7 @@ static int read_dev(const VgAccum* acc, const DevBuf& b, void* out, size_t bytes
 
 int vg_accum_read_sums(const VgAccum* acc, float* out, size_t len)
 {
+    DevGuard device_guard(dev_of(acc));
     if (!acc || !out)
         return fail(VG_ERR_INVALID, "null argument");
     size_t n = (size_t)acc->width * acc->height * 3;
@@ -1105,6 +1157,7 @@ int vg_accum_read_sums(const VgAccum* acc, float* out, size_t len)
 
 int vg_accum_read_sums_f64(const VgAccum* acc, double* out, size_t len)
 {
+    DevGuard device_guard(dev_of(acc));
     if (!acc || !out)
         return fail(VG_ERR_INVALID, "null argument");
     size_t n = (size_t)acc->width * acc->height * 3;
@@ -1123,6 +1176,7 @@ int vg_accum_read_sums_f64(const VgAccum* acc, double* out, size_t len)
 
 int vg_accum_read_lighting(const VgAccum* acc, float* out, size_t len)
 {
+    DevGuard device_guard(dev_of(acc));
     if (!acc || !out)
         return fail(VG_ERR_INVALID, "null argument");
     if (!acc->lighting)
@@ -1135,6 +1189,7 @@ int vg_accum_read_lighting(const VgAccum* acc, float* out, size_t len)
 
 int vg_accum_read_stats(const VgAccum* acc, float* out, size_t len)
 {
+    DevGuard device_guard(dev_of(acc));
     if (!acc || !out)
         return fail(VG_ERR_INVALID, "null argument");
     if (!acc->stats.p)
@@ -1155,6 +1210,7 @@ int vg_accum_read_stats(const VgAccum* acc, float* out, size_t len)
 
 int vg_accum_traversal_stats(const VgAccum* acc, uint64_t out[4])
 {
+    DevGuard device_guard(dev_of(acc));
     if (!acc || !out)
         return fail(VG_ERR_INVALID, "null argument");
     if (!acc->tstats.p)
@@ -1164,6 +1220,7 @@ int vg_accum_traversal_stats(const VgAccum* acc, uint64_t out[4])
 
 int vg_accum_shadow_rays(const VgAccum* acc, uint64_t* out)
 {
+    DevGuard device_guard(dev_of(acc));
     if (!acc || !out)
         return fail(VG_ERR_INVALID, "null argument");
     if (!acc->tstats.p)
@@ -1177,6 +1234,7 @@ int vg_accum_shadow_rays(const VgAccum* acc, uint64_t* out)
 
 int vg_accum_read_queue_counts(const VgAccum* acc, uint32_t* out, size_t len)
 {
+    DevGuard device_guard(dev_of(acc));
     if (!acc || !out)
         return fail(VG_ERR_INVALID, "null argument");
     if (!acc->counts.p || acc->samples == 0 || acc->last_depth == 0)
@@ -1216,6 +1274,7 @@ static double tune_trial(VgRenderer* r, uint32_t w, uint32_t h, uint32_t spp, in
 
 int vg_autotune(VgRenderer* r, const VgPacked* pk, uint32_t width, uint32_t height, uint32_t samples, VgTuneResult* out)
 {
+    DevGuard device_guard(dev_of(r));
     if (!r || !out || width == 0 || height == 0 || samples == 0)
         return fail(VG_ERR_INVALID, "null argument or empty trial");
     memset(out, 0, sizeof(*out));
@@ -1321,6 +1380,7 @@ int vg_autotune(VgRenderer* r, const VgPacked* pk, uint32_t width, uint32_t heig
 
 int vg_render_normals(VgRenderer* r, uint32_t width, uint32_t height, float* out)
 {
+    DevGuard device_guard(dev_of(r));
     if (!r || !out)
         return fail(VG_ERR_INVALID, "null argument");
     if (width == 0 || height == 0)
@@ -1344,6 +1404,7 @@ int vg_render_normals(VgRenderer* r, uint32_t width, uint32_t height, float* out
 int vg_render_aovs(VgRenderer* r, uint32_t width, uint32_t height, float* albedo_depth, uint32_t* object_id,
                    uint32_t* material_id, float* coverage)
 {
+    DevGuard device_guard(dev_of(r));
     if (!r || !albedo_depth || !object_id || !material_id || !coverage)
         return fail(VG_ERR_INVALID, "null argument");
     if (width == 0 || height == 0)
@@ -1371,6 +1432,7 @@ int vg_render_aovs(VgRenderer* r, uint32_t width, uint32_t height, float* albedo
 
 int vg_trace_closest_device(VgRenderer* r, const float* d_rays, size_t n, uint32_t* d_hits, double* seconds)
 {
+    DevGuard device_guard(dev_of(r));
     if (!r || (n > 0 && (!d_rays || !d_hits)))
         return fail(VG_ERR_INVALID, "null argument");
     if (n > 0xffffffffull)
@@ -1401,6 +1463,7 @@ int vg_trace_closest_device(VgRenderer* r, const float* d_rays, size_t n, uint32
 
 int vg_trace_closest(VgRenderer* r, const float* rays, size_t n, uint32_t* hits)
 {
+    DevGuard device_guard(dev_of(r));
     if (!r || (n > 0 && (!rays || !hits)))
         return fail(VG_ERR_INVALID, "null argument");
     DevBuf dr, dh;
@@ -1442,7 +1505,7 @@ static int noalloc_scratch(int device, unsigned char** out)
         return fail(VG_ERR_INVALID, "device ordinal out of range for the static scratch table");
     std::lock_guard<std::mutex> lock(g_na_mu);
     if (!g_na_addr[device]) {
-        VG_CHECK(cudaSetDevice(device), "cudaSetDevice");
+        DevGuard on(device); // restores the caller's current device on return
         void* p = nullptr;
         VG_CHECK(cudaGetSymbolAddress(&p, g_trace_noalloc_scratch), "cudaGetSymbolAddress");
         g_na_addr[device] = (unsigned char*)p;
@@ -1455,6 +1518,7 @@ extern "C" {
 
 int vg_trace_closest_noalloc(VgRenderer* r, const float* rays, size_t n, uint32_t* hits)
 {
+    DevGuard device_guard(dev_of(r));
     if (!r || (n > 0 && (!rays || !hits)))
         return fail(VG_ERR_INVALID, "null argument");
     if (n > VG_TRACE_NOALLOC_MAX_RAYS)
@@ -1490,6 +1554,7 @@ int vg_trace_closest_noalloc(VgRenderer* r, const float* rays, size_t n, uint32_
 
 int vg_trace_occluded(VgRenderer* r, const float* rays, size_t n, uint32_t* out)
 {
+    DevGuard device_guard(dev_of(r));
     if (!r || (n > 0 && (!rays || !out)))
         return fail(VG_ERR_INVALID, "null argument");
     if (n > 0xffffffffull)
