@@ -289,7 +289,10 @@ def run_reference(args):
 
 
 CACHE_W = CACHE_H = 512
+C2_ORACLE = "many_spheres_1080p_d16_rows476_507"  # converged FP64 oracle rows of the 1M-triangle frame
 CACHE_REF_SPP = 8192
+C2_REF_SPP = 2048
+REF_FIRST_SAMPLE = 1 << 24  # reference images start here: no sample shared with a measured curve
 CACHE_MLP_FLOP = 2 * (4 * 64 * 64 + 64 * 3)  # per record, inference (algorithmic, 3 outputs)
 
 
@@ -297,9 +300,37 @@ def _rmse(a, b):
     return float(np.sqrt(np.mean((a - b) ** 2)))
 
 
+_CONVERGED = None
+
+
+def converged(name):
+    """A converged image of the CPU oracle in double precision (tests/golden/make_converged.py):
+    (float64 (rows, width, 3) pixel means, its settings), or (None, None) if absent."""
+    global _CONVERGED
+    if _CONVERGED is None:
+        npz, js = ROOT / "tests" / "golden" / "converged_fp64.npz", ROOT / "tests" / "golden" / "converged_fp64.json"
+        _CONVERGED = (dict(np.load(npz)), json.loads(js.read_text())) if npz.exists() and js.exists() else ({}, {})
+    img, meta = _CONVERGED[0].get(name), _CONVERGED[1].get(name)
+    return (None, None) if img is None else (img.astype(np.float64), meta)
+
+
+def rmse_vs_fp64(img, width, height, name):
+    """RMSE of a (pixels, 3) mean image of `width` x `height` against the converged FP64 oracle image
+    `name`, over that image's rows; with the oracle image's own noise (the floor of any such RMSE)."""
+    ref, meta = converged(name)
+    if ref is None or (meta["width"], meta["height"]) != (width, height):
+        return None
+    r0, r1 = meta["rows"]
+    a = np.asarray(img, np.float64).reshape(height, width, 3)[r0:r1]
+    return {"rmse": _rmse(a, ref), "oracle_image": name, "oracle_spp": meta["spp"],
+            "oracle_noise_rmse": meta["noise_rmse"], "rows": [r0, r1],
+            "mean_rel_error": float(a.mean() / ref.mean() - 1.0)}
+
+
 def _time_at(curve, target):
-    """First time (log-log interpolation between points) at which the curve's RMSE reaches target."""
-    for (t0, e0), (t1, e1) in zip(curve, curve[1:]):
+    """First time (log-log interpolation between points) at which the curve's RMSE reaches target.
+    Curve points are (seconds, rmse, samples)."""
+    for (t0, e0, *_), (t1, e1, *_) in zip(curve, curve[1:]):
         if e1 <= target < e0 or (e0 <= target and t0 == curve[0][0]):
             if e0 <= target:
                 return t0
@@ -308,36 +339,69 @@ def _time_at(curve, target):
     return None
 
 
-def _rmse_at(curve, t):
-    for (t0, e0), (t1, e1) in zip(curve, curve[1:]):
-        if t0 <= t <= t1:
-            f = (math.log(t) - math.log(t0)) / (math.log(t1) - math.log(t0))
-            return math.exp(math.log(e0) + f * (math.log(e1) - math.log(e0)))
-    return None
-
-
 def _cache_curve(r, acc, ref, chunks, limit_s=None):
     curve, n = [], 0
     for k in chunks:
         r.accumulate(acc, k)
         n += k
-        curve.append((acc.gpu_seconds(), _rmse(acc.mean(), ref)))
+        curve.append((acc.gpu_seconds(), _rmse(acc.mean(), ref), n))
         if limit_s is not None and acc.gpu_seconds() > limit_s:
             break
     return curve, n
 
 
-def _cache_vs_plain(plains, curve, target_at):
-    """Each plain curve's time to the RMSE the first plain curve has at point `target_at`, the
-    cache curve's time to it, and the speed-up against the fastest plain integrator."""
-    first = next(iter(plains.values()))
-    target = first[target_at][1]
+def _speedup(plains, curve, target):
+    """Each plain curve's time to `target` RMSE, the cache curve's, and the speed-up against the
+    fastest plain integrator."""
     t_plain = {name: _time_at(c, target) or c[-1][0] for name, c in plains.items()}
     best = min(t_plain, key=t_plain.get)
     t_cache = _time_at(curve, target)
     return {"target_rmse": target, "time_to_target_s": {**{"plain_" + k: v for k, v in t_plain.items()},
                                                          "cache": t_cache},
-            "speedup": (t_plain[best] / t_cache) if t_cache else None, "speedup_against": "plain " + best}
+            "speedup": (t_plain[best] / t_cache) if t_cache else None, "speedup_against": "plain " + best,
+            "reached": t_cache is not None}
+
+
+def _cache_vs_plain(plains, curve, target_at):
+    """_speedup at the RMSE the first plain curve has at its point `target_at`."""
+    first = next(iter(plains.values()))
+    return _speedup(plains, curve, first[target_at][1])
+
+
+def _fit_noise(curve, points=3):
+    """Least-squares fit of rmse^2 = B + S / N to a curve's last `points` points (N = samples): an
+    unbiased estimate's squared error falls as S / N, so B is the floor (bias energy and the
+    reference's own noise) and S the per-sample variance."""
+    pts = curve[-points:]
+    A = np.array([[1.0, 1.0 / n] for _, _, n in pts])
+    y = np.array([e * e for _, e, _ in pts])
+    (B, S), *_ = np.linalg.lstsq(A, y, rcond=None)
+    return float(B), float(S)
+
+
+def _at_spp_by_fit(plains, curve, spp, ref_spp):
+    """Time to reach the RMSE plain path tracing has at `spp` samples, from the curves' noise fits:
+    plain is unbiased, so against a reference of ref_spp independent plain samples its measured
+    error is rmse^2 = S_p (1 / N + 1 / ref_spp) (S_p fitted to the fastest plain curve's last
+    points), and at `spp` samples it is S_p (1 / spp + 1 / ref_spp); plain takes spp times its time
+    per sample. The cache's fit rmse^2 = B + S / N gives the samples it needs, N = S / (target^2 - B),
+    or none when its floor B is at or above the target (bias the network does not lose)."""
+    best = min(plains, key=lambda k: plains[k][-1][0] / plains[k][-1][2])
+    pc = plains[best]
+    pts = pc[-3:]
+    S_p = float(np.mean([e * e / (1.0 / n + 1.0 / ref_spp) for _, e, n in pts]))
+    target2 = S_p * (1.0 / spp + 1.0 / ref_spp)
+    t_plain = spp * pc[-1][0] / pc[-1][2]
+    B, S = _fit_noise(curve)
+    t_per = curve[-1][0] / curve[-1][2]
+    n_cache = S / (target2 - B) if target2 > B and S > 0 else None
+    t_cache = n_cache * t_per if n_cache else None
+    return {"target_rmse": math.sqrt(target2), "plain_spp": spp, "method": "fit (see bench.py _at_spp_by_fit)",
+            "time_to_target_s": {"plain_" + best: t_plain, "cache": t_cache},
+            "cache_fit": {"floor_rmse": math.sqrt(max(B, 0.0)), "per_sample_sigma": math.sqrt(max(S, 0.0)),
+                          "reference_noise_rmse": math.sqrt(S_p / ref_spp)},
+            "cache_spp_needed": n_cache, "speedup": (t_plain / t_cache) if t_cache else None,
+            "speedup_against": "plain " + best, "reached": t_cache is not None}
 
 
 def mlp_kernel_seconds(ctx, nrec, reps):
@@ -370,41 +434,48 @@ def cache_report(ctx, packed_c2, peak_tflops, peak_kind):
     from verion_gb300.readback import Adaptive
 
     out = {}
-    # C4.
+    # C4: the Cornell box with the stated cache (2^19 entries, 2^16 training records per frame).
     p = pack.pack(scenes.cornell())
     ref_r = Renderer(ctx, p)
     ref_r.set_integrator(Integrator.WAVEFRONT)
     acc = ref_r.new_accumulation(CACHE_W, CACHE_H)
+    acc.set_first_sample(REF_FIRST_SAMPLE)
     for _ in range(CACHE_REF_SPP // 512):
         ref_r.accumulate(acc, 512)
     ref = acc.mean()
     del acc, ref_r
-    plains, plain_ms = {}, {}
-    for name, integ in (("megakernel", Integrator.MEGAKERNEL), ("wavefront", Integrator.WAVEFRONT)):
+    plains, plain_ms, plain_fp64 = {}, {}, {}
+    for name, integ, chunks in (("megakernel", Integrator.MEGAKERNEL, (32, 32, 64, 128, 256, 512)),
+                                ("wavefront", Integrator.WAVEFRONT, (32, 32, 64, 128, 256, 512, 1024, 2048))):
         plain_r = Renderer(ctx, p)
         plain_r.set_integrator(integ)
         acc = plain_r.new_accumulation(CACHE_W, CACHE_H)
-        plains[name], n = _cache_curve(plain_r, acc, ref, (32, 32, 64, 128, 256, 512))
+        plains[name], n = _cache_curve(plain_r, acc, ref, chunks)
         plain_ms[name] = 1e3 * acc.gpu_seconds() / n
+        plain_fp64[name] = rmse_vs_fp64(acc.mean(), CACHE_W, CACHE_H, "cornell_512_d8")
         del acc, plain_r
     r = Renderer(ctx, p)
     r.set_integrator(Integrator.WAVEFRONT)
     r.set_cache_frame(8)
-    cache = Cache(ctx, bounds=r.bounds(), log2_entries=17)
+    cache = Cache(ctx, bounds=r.bounds())
     r.set_cache(cache, spread=0.01, train_paths=8192, train_steps=2, train_batch=32768)
     r.set_stage_timing(True)
     acc = r.new_accumulation(CACHE_W, CACHE_H)
-    curve, n = _cache_curve(r, acc, ref, (32, 32, 64, 128, 256, 512, 1024))
+    curve, n = _cache_curve(r, acc, ref, (32, 32, 64, 128, 256, 512, 1024, 2048))
     st = acc.cache_stats()
-    c4 = {"config": "Cornell box 512x512, depth 8; cache 16 levels x 2^17 entries x 2 fp16, MLP 64 x 4 hidden bf16; "
-                    "frames of 8 samples, ~8192 training pixels, 2 Adam steps of 32768 records per frame; "
-                    f"reference {CACHE_REF_SPP} spp plain; target: plain megakernel RMSE at 1024 spp",
+    c4 = {"config": "Cornell box 512x512, depth 8; cache 16 levels x 2^19 entries x 2 fp16, MLP 64 x 4 hidden bf16; "
+                    "frames of 8 samples, ~8192 training pixels, 2 Adam steps of 32768 records (2^16 per frame); "
+                    f"reference {CACHE_REF_SPP} spp plain from sample index 2^24 (no sample shared with the curves); "
+                    "targets: plain megakernel RMSE at 1024 spp, plain wavefront RMSE at 4096 spp (measured)",
           "plain_ms_per_spp": plain_ms, "cache_ms_per_spp": 1e3 * acc.gpu_seconds() / n,
           "cache_split_seconds": {"paths": st.path_seconds, "encode_and_infer": st.infer_seconds,
                                   "train": st.train_seconds},
           "bias_rel_mean": float((acc.mean().mean() - ref.mean()) / ref.mean()),
           "cache_curve": curve, "plain_curves": plains}
-    c4.update(_cache_vs_plain(plains, curve, -1))
+    c4.update(_cache_vs_plain({"megakernel": plains["megakernel"], "wavefront": plains["wavefront"]}, curve, -1))
+    c4["at_4096spp"] = _speedup({"wavefront": plains["wavefront"]}, curve, plains["wavefront"][-1][1])
+    c4["rmse_vs_fp64_oracle"] = {"cache": rmse_vs_fp64(acc.mean(), CACHE_W, CACHE_H, "cornell_512_d8"),
+                                 **{"plain_" + k: v for k, v in plain_fp64.items()}}
     out["cornell_512"] = c4
     del acc, r
     # C2.
@@ -418,15 +489,17 @@ def cache_report(ctx, packed_c2, peak_tflops, peak_kind):
 
     ref_r = c2_renderer()
     acc = ref_r.new_accumulation(WIDTH, HEIGHT)
-    for _ in range(16):
+    acc.set_first_sample(REF_FIRST_SAMPLE)
+    for _ in range(C2_REF_SPP // 128):
         ref_r.accumulate(acc, 128)
     ref = acc.mean()
     del acc, ref_r
-    plains = {}
+    plains, plain_fp64 = {}, {}
     for name, adaptive in (("wavefront", False), ("wavefront_adaptive", True)):
         rr = c2_renderer(adaptive)
         acc = rr.new_accumulation(WIDTH, HEIGHT)
         plains[name], _ = _cache_curve(rr, acc, ref, (8, 8, 16, 32, 64, 128))
+        plain_fp64[name] = rmse_vs_fp64(acc.mean(), WIDTH, HEIGHT, C2_ORACLE)
         del acc, rr
     r = c2_renderer()
     cache = Cache(ctx, bounds=r.bounds())
@@ -435,11 +508,12 @@ def cache_report(ctx, packed_c2, peak_tflops, peak_kind):
     r.set_cache(cache, spread=0.002)
     r.set_stage_timing(True)
     acc = r.new_accumulation(WIDTH, HEIGHT)
-    curve, n = _cache_curve(r, acc, ref, (8, 8, 16, 32, 64, 128))
+    curve, n = _cache_curve(r, acc, ref, (8, 8, 16, 32, 64, 128, 256))
     st = acc.cache_stats()
     c2 = {"config": "1M-triangle workload 1920x1080, depth 16; cache 16 levels x 2^19 entries, spread threshold "
                     "0.002, frames of 4 samples, ~16384 training pixels, 4 Adam steps of 16384 records per frame; "
-                    "reference 2048 spp plain",
+                    f"reference {C2_REF_SPP} spp plain from sample index 2^24; the 4096-spp target is fitted "
+                    "(plain: error^2 = S (1/N + 1/reference spp); cache: error^2 = B + S/N over its last points)",
           "cache_ms_per_spp": 1e3 * acc.gpu_seconds() / n,
           "cache_split_seconds": {"paths": st.path_seconds, "encode_and_infer": st.infer_seconds,
                                   "train": st.train_seconds},
@@ -447,6 +521,9 @@ def cache_report(ctx, packed_c2, peak_tflops, peak_kind):
           "cache_curve": curve, "plain_curves": plains}
     for label, at in (("at_64spp", 3), ("at_256spp", 5)):
         c2[label] = _cache_vs_plain(plains, curve, at)
+    c2["at_4096spp"] = _at_spp_by_fit(plains, curve, 4096, C2_REF_SPP)
+    c2["rmse_vs_fp64_oracle"] = {"cache": rmse_vs_fp64(acc.mean(), WIDTH, HEIGHT, C2_ORACLE),
+                                 **{"plain_" + k: v for k, v in plain_fp64.items()}}
     out["many_spheres_1080p"] = c2
     del acc, r
     # MLP kernels on synthetic records.
@@ -593,6 +670,8 @@ def restir_report(ctx):
                 r.accumulate(acc, 1)
             img = acc.mean()
             out[f"rmse_8_frames{tag}_{'restir' if on else 'plain'}"] = _rmse(img, ref)
+            out[f"rmse_vs_fp64_oracle_8_frames{tag}_{'restir' if on else 'plain'}"] = rmse_vs_fp64(
+                img, w, h, f"many_lights_480x270_d{depth}")
             # Without the pixels that see an emitter (reference luminance above its 95th percentile):
             # their error is edge aliasing of the bright triangles, which no light sampling changes.
             lum = ref @ np.array([0.2126, 0.7152, 0.0722])
@@ -689,6 +768,9 @@ def run_cuda(args):
         barrier(world)
     paths = paths_of(acc) - p0
     gpu_launches = acc.launches() - launches0
+    fp64 = rmse_vs_fp64(acc.mean(), WIDTH, HEIGHT, C2_ORACLE)
+    if fp64 is not None:
+        fp64["mean_spp"] = paths_of(acc) / (WIDTH * HEIGHT)
     stage = acc.stage_seconds() or (0.0, 0.0)
     extend_launch_s = acc.extend_launch_seconds()
     t_local = sum(step_times)
@@ -809,6 +891,7 @@ def run_cuda(args):
                 "paths_per_step": paths_all / args.steps,
                 "mrays_per_s": value * rays_per_path if rays_per_path else None,
                 "rays_per_path": rays_per_path,
+                "rmse_vs_fp64_oracle": fp64,
                 "megakernel_value": mega, "radiance_cache": cache, "batched_serving": batch,
                 "restir_many_lights": restir}
         print(json.dumps(line), flush=True)

@@ -212,6 +212,17 @@ int vg_set_deferred_shadows(VgRenderer* r, int on);
 /* Streaming mode: the extend and shadow stages refill a warp's idle lanes with queued rays
  * (default on) or give each warp 32 rays at a time (off). Same results either way. */
 int vg_set_dynamic_fetch(VgRenderer* r, int on);
+/* Streaming mode with dynamic fetch: the extend and shadow stages test the triangles of the leaves
+ * their warp's rays reached together, one (ray, triangle) pair per lane (default on), or each lane
+ * its own (off). Same results either way. No reference counterpart: the reference's hardware ray
+ * queries have no such choice. */
+int vg_set_coop_triangles(VgRenderer* r, int on);
+/* Streaming mode with dynamic fetch: a warp of the extend stage takes new rays once at least
+ * `refill` of its 32 lanes are idle (1-32, default 8) and visits at most `steps` nodes per lane
+ * between refills (1-64, default 4); shadow_refill and shadow_steps set the same for the shadow
+ * stage. Same results for every setting. No reference counterpart. */
+int vg_set_traversal_fetch(VgRenderer* r, uint32_t refill, uint32_t steps, uint32_t shadow_refill,
+                           uint32_t shadow_steps);
 /* Streaming mode: capture `waves` waves (an even count, 0 = off) of the bounce loop in a CUDA graph
  * once per call and replay it until the slots drain (without stage timing), instead of launching
  * every wave's kernels from the host. Same sums. */
@@ -237,6 +248,8 @@ typedef struct VgTuneResult {
     double mpaths_before, mpaths_after; /* camera paths per second, first and best trial */
     uint32_t trials;
     int extend_blocks_per_sm;
+    int coop_triangles;                /* vg_set_coop_triangles */
+    uint32_t fetch_refill, fetch_steps; /* vg_set_traversal_fetch, extend stage */
 } VgTuneResult;
 int vg_autotune(VgRenderer* r, const VgPacked* packed, uint32_t width, uint32_t height, uint32_t samples,
                 VgTuneResult* out);
@@ -264,6 +277,13 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples);
 
 /* Accumulation getters (lib.rs:76-92). */
 uint32_t vg_accum_samples(const VgAccum* acc);
+/* Per-pixel sample indices of this accumulation start at `first` (default 0) instead of 0: its
+ * samples then share no random sequence with another accumulation's samples below `first` (each
+ * sample's sequence is seeded from the pixel and the sample index, pt_core.slang:645-682), e.g.
+ * for an independent reference image or for replicas that split one image's samples. Set before
+ * the first sample; plain path tracing only (an accumulation with ReSTIR or the radiance cache
+ * fails with VG_ERR_SCENE). No reference counterpart. */
+int vg_accum_set_first_sample(VgAccum* acc, uint32_t first);
 double vg_accum_gpu_seconds(const VgAccum* acc);
 /* Stage seconds {extend, shade}; returns 0 when stage timing never ran (None). */
 int vg_accum_stage_seconds(const VgAccum* acc, double out[2]);

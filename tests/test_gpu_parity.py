@@ -315,10 +315,12 @@ def test_wavefront_modes_match_the_oracle(gpu_ctx, mode, tail, adaptive):
         assert 0 < acc.last_waves() <= 7 * 16 + 3
 
 
-@pytest.mark.parametrize("deferred,dynamic", [(False, False), (True, False), (True, True)])
-def test_streaming_shadow_stage_matches_the_oracle(gpu_ctx, deferred, dynamic):
+@pytest.mark.parametrize("deferred,dynamic,coop", [(False, False, False), (True, False, False), (True, True, False),
+                                                  (True, True, True)])
+def test_streaming_shadow_stage_matches_the_oracle(gpu_ctx, deferred, dynamic, coop):
     # The emitter / environment shadow ray traced inline in shade, or in the separate shadow stage;
-    # with dynamic fetch the extend and shadow traversals refill idle lanes from the queue.
+    # with dynamic fetch the extend and shadow traversals refill idle lanes from the queue, with
+    # coop their warps test the leaves' triangles one (ray, triangle) pair per lane.
     from . import analytic as an
 
     for s, depth in ((scenes.many_spheres(hdri=(256, 128)), 16), (an.feature_zoo(), 8)):
@@ -328,6 +330,7 @@ def test_streaming_shadow_stage_matches_the_oracle(gpu_ctx, deferred, dynamic):
         r.set_integrator(Integrator.WAVEFRONT)
         r.set_deferred_shadows(deferred)
         r.set_dynamic_fetch(dynamic)
+        r.set_coop_triangles(coop)
         r.set_stream_tail(0)
         r.set_max_depth(depth)
         acc = r.new_accumulation(40, 30)
@@ -368,3 +371,58 @@ def test_transparent_background_bit_exact(gpu_ctx):
     _, acc = gpu_render(gpu_ctx, p, 48, 36, 4, integrator=Integrator.WAVEFRONT)
     ref = oracle_render(p, 48, 36, 4)
     assert_same(acc.sums(), ref.sums, "transparent background sums")
+
+
+def test_coop_leaf_testing_keeps_hits_and_counters(gpu_ctx):
+    # Warp-cooperative leaf testing against each lane testing its own triangles: the same sums,
+    # the same nodes visited and triangles tested (the walk's order is unchanged), the same number
+    # of shadow rays, on the 1M-triangle scene with adaptive sampling.
+    p = pack.pack(scenes.many_spheres(hdri=(256, 128)))
+    out = {}
+    for coop in (False, True):
+        r = Renderer(gpu_ctx, p)
+        r.set_accum_precision(32)
+        r.set_integrator(Integrator.WAVEFRONT)
+        r.set_max_depth(16)
+        r.set_adaptive(Adaptive(threshold=0.05, min_spp=4))
+        r.set_coop_triangles(coop)
+        r.set_stream_tail(0)  # waves only: the tail launch traces each slot's path in one thread
+        r.set_traversal_stats(True)
+        acc = r.new_accumulation(160, 90)
+        for n in (4, 4):
+            r.accumulate(acc, n)
+        out[coop] = (acc.sums(), acc.traversal_stats(), acc.shadow_rays())
+    assert_same(out[True][0], out[False][0], "sums")
+    assert out[True][1] == out[False][1]
+    assert out[True][2] == out[False][2]
+    assert out[True][1]["tests"] > 0
+
+
+@pytest.mark.parametrize("integrator", [Integrator.MEGAKERNEL, Integrator.WAVEFRONT])
+def test_first_sample_index_bit_exact(gpu_ctx, integrator):
+    # An accumulation whose sample indices start at 1000 traces the oracle's samples 1000..1006
+    # (per-pixel sequences seeded from the sample index), over two calls.
+    p = pack.pack(scenes.cornell())
+    r = Renderer(gpu_ctx, p)
+    r.set_accum_precision(32)
+    r.set_integrator(integrator)
+    acc = r.new_accumulation(64, 48)
+    acc.set_first_sample(1000)
+    r.accumulate(acc, 4)
+    r.accumulate(acc, 3)
+    o = oracle.OracleScene(p)
+    ref = oracle.OracleAccumulation(64, 48)
+    ref.samples = 1000
+    oracle.render(o, params(p, 64, 48), ref, 7)
+    assert_same(acc.sums(), ref.sums, "sums from sample 1000")
+    zero = r.new_accumulation(64, 48)
+    r.accumulate(zero, 7)
+    assert not np.array_equal(zero.sums(), acc.sums())
+    with pytest.raises(Error):
+        acc.set_first_sample(5)  # after the first sample
+    r.set_restir(Restir(di=True, gi=False))
+    other = r.new_accumulation(16, 16)
+    other.set_first_sample(8)
+    with pytest.raises(Error) as e:
+        r.accumulate(other, 1)
+    assert e.value.kind == "Scene"

@@ -62,8 +62,30 @@ def test_autotune_keeps_the_sums(gpu_ctx):
     assert t["trials"] >= 6 and t["mpaths_after"] >= t["mpaths_before"] > 0
     assert t["graph_waves"] in (0, 8) and t["bvh_traversal_cost"] in (0.25, 0.5, 1.0, 2.0)
     assert t["extend_blocks_per_sm"] >= 1
+    assert t["coop_triangles"] in (0, 1) and t["fetch_refill"] in (4, 8, 16) and t["fetch_steps"] in (2, 4, 8)
     fresh = wave_renderer(gpu_ctx, p)
     assert np.array_equal(render(r, 80, 45, 3), render(fresh, 80, 45, 3))
+
+
+@pytest.mark.parametrize("refill,steps", [(1, 1), (4, 2), (16, 8), (32, 64)])
+def test_traversal_fetch_settings_keep_the_sums(gpu_ctx, refill, steps):
+    p = pack.pack(scenes.many_spheres(hdri=(256, 128)))
+    want = render(wave_renderer(gpu_ctx, p), 64, 36, 2)
+    for coop in (False, True):
+        r = wave_renderer(gpu_ctx, p)
+        r.set_stream_tail(0)  # waves only: small frames would otherwise go straight to the tail launch
+        r.set_coop_triangles(coop)
+        r.set_traversal_fetch(refill, steps)
+        assert np.array_equal(render(r, 64, 36, 2), want), (refill, steps, coop)
+
+
+def test_traversal_fetch_rejects_out_of_range(gpu_ctx):
+    from verion_gb300.backend import Error
+
+    r = Renderer(gpu_ctx, scenes.cornell())
+    for bad in ((0, 4), (33, 4), (8, 0), (8, 65)):
+        with pytest.raises(Error):
+            r.set_traversal_fetch(*bad)
 
 
 def test_traversal_counters_count_and_change_nothing(gpu_ctx):

@@ -111,7 +111,8 @@ class CacheStats(C.Structure):
 class _TuneResult(C.Structure):
     _fields_ = [("dynamic_fetch", C.c_int), ("deferred_shadows", C.c_int), ("stream_tail", C.c_uint32),
                 ("graph_waves", C.c_uint32), ("bvh_traversal_cost", C.c_float), ("mpaths_before", C.c_double),
-                ("mpaths_after", C.c_double), ("trials", C.c_uint32), ("extend_blocks_per_sm", C.c_int)]
+                ("mpaths_after", C.c_double), ("trials", C.c_uint32), ("extend_blocks_per_sm", C.c_int),
+                ("coop_triangles", C.c_int), ("fetch_refill", C.c_uint32), ("fetch_steps", C.c_uint32)]
 
 
 class _BatchRequest(C.Structure):
@@ -203,6 +204,8 @@ def lib() -> C.CDLL:
             "vg_accum_tail_seconds": (f64, [vp]),
             "vg_set_deferred_shadows": (i32, [vp, i32]),
             "vg_set_dynamic_fetch": (i32, [vp, i32]),
+            "vg_set_coop_triangles": (i32, [vp, i32]),
+            "vg_set_traversal_fetch": (i32, [vp, u32, u32, u32, u32]),
             "vg_set_wavefront_graph": (i32, [vp, u32]),
             "vg_set_bvh_traversal_cost": (i32, [vp, C.POINTER(_Packed), C.c_float]),
             "vg_autotune": (i32, [vp, C.POINTER(_Packed), u32, u32, u32, C.POINTER(_TuneResult)]),
@@ -213,6 +216,7 @@ def lib() -> C.CDLL:
             "vg_accum_destroy": (None, [vp]),
             "vg_accumulate": (i32, [vp, vp, u32]),
             "vg_accum_samples": (u32, [vp]),
+            "vg_accum_set_first_sample": (i32, [vp, u32]),
             "vg_accum_gpu_seconds": (f64, [vp]),
             "vg_accum_stage_seconds": (i32, [vp, C.POINTER(f64)]),
             "vg_accum_wavefront_bytes": (_S, [vp]),
@@ -433,6 +437,10 @@ class Accumulation:
     def launches(self) -> int:
         return lib().vg_accum_launches(self._h)
 
+    def set_first_sample(self, first: int) -> None:
+        """Sample indices start at `first` (before the first sample; plain path tracing only)."""
+        _check(lib().vg_accum_set_first_sample(self._h, first))
+
     def extend_launch_seconds(self) -> float:
         return lib().vg_accum_extend_launch_seconds(self._h)
 
@@ -616,6 +624,17 @@ class Renderer:
 
     def set_dynamic_fetch(self, on: bool) -> None:
         _check(lib().vg_set_dynamic_fetch(self._h, int(on)))
+
+    def set_coop_triangles(self, on: bool) -> None:
+        """Warp-cooperative leaf testing in the streaming traversal stages (same results)."""
+        _check(lib().vg_set_coop_triangles(self._h, int(on)))
+
+    def set_traversal_fetch(self, refill: int = 8, steps: int = 4, shadow_refill: int = None,
+                            shadow_steps: int = None) -> None:
+        """Dynamic fetch of the streaming traversal stages: idle lanes per refill, node visits
+        between refills (the shadow stage's default to the extend stage's)."""
+        _check(lib().vg_set_traversal_fetch(self._h, refill, steps, refill if shadow_refill is None else shadow_refill,
+                                            steps if shadow_steps is None else shadow_steps))
 
     def set_deferred_shadows(self, on: bool) -> None:
         _check(lib().vg_set_deferred_shadows(self._h, int(on)))

@@ -339,6 +339,7 @@ int vg_cache_create(VgContext* ctx, const VgCacheConfig* cfg, VgCache** out)
     vgx::nrc_prepare();
     VgCache* k = new VgCache();
     k->ctx = ctx;
+    k->device = ctx->device;
     k->cfg = c;
     double growth = c.levels > 1 ? std::exp((std::log((double)c.max_resolution) - std::log((double)c.base_resolution)) /
                                             (double)(c.levels - 1))

@@ -8,6 +8,7 @@
 
 struct VgCache {
     VgContext* ctx = nullptr;
+    int device = -1; // the context's device
     VgCacheConfig cfg{};
     uint32_t res[vgn::MAX_LEVELS] = {};
     uint32_t dense_mask = 0;
@@ -44,7 +45,7 @@ struct VgCache {
 };
 
 namespace {
-int dev_of(const VgCache* k) { return k ? dev_of(k->ctx) : -1; }
+int dev_of(const VgCache* k) { return k ? k->device : -1; }
 } // namespace
 
 namespace vgc {

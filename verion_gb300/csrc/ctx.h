@@ -88,6 +88,8 @@ struct Wave {
     uint32_t* meta;    // streaming mode: per path slot, depth (bits 0-7) and sample within the batch (8+)
     uint32_t n;        // paths: one per pixel
     uint32_t depth;    // max depth
+    uint32_t refill, steps;               // dynamic fetch of the extend stage: idle lanes per refill, visits between refills
+    uint32_t shadow_refill, shadow_steps; // the same for the shadow stage
 };
 
 // Radiance-cache frames on the streaming wavefront: the path spread (a0, a) of every slot,

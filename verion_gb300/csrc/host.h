@@ -128,9 +128,18 @@ struct DevGuard {
     explicit DevGuard(int device)
     {
         int cur = -1;
-        if (device >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != device &&
-            cudaSetDevice(device) == cudaSuccess)
+        if (device < 0)
+            return;
+        if (cudaGetDevice(&cur) != cudaSuccess) {
+            cudaGetLastError(); // leave no error behind for the call's own launch checks
+            return;
+        }
+        if (cur == device)
+            return;
+        if (cudaSetDevice(device) == cudaSuccess)
             prev = cur;
+        else
+            cudaGetLastError();
     }
     ~DevGuard()
     {
@@ -174,6 +183,7 @@ constexpr uint32_t CACHE_WARMUP_SAMPLE = 0x40000000u; // first sample index of c
 
 struct VgRenderer {
     VgContext* ctx = nullptr;
+    int device = -1; // the context's device, kept here so no call dereferences a destroyed context
     DevBuf positions, indices, uvs, vnormals, instances, materials, lights, emitters, emit_cdf, emit_guide, env_pixels,
         env_marginal, env_cond, env_guide, texels, tex_info, nodes, tris, err, scratch;
     vgd::DeviceScene ds{};
@@ -200,6 +210,9 @@ struct VgRenderer {
     int shadow_blocks[2] = {};
     bool defer_shadows = true; // streaming: shadow rays of the light sample in their own stage
     bool dynamic_fetch = true; // streaming: traversal stages refill idle lanes from the queue
+    bool coop_tris = true;     // streaming, dynamic fetch: warp-cooperative leaf testing
+    uint32_t fetch_refill = 8, fetch_steps = 4;               // dynamic fetch, extend stage
+    uint32_t shadow_fetch_refill = 8, shadow_fetch_steps = 4; // dynamic fetch, shadow stage
     uint32_t graph_waves = 0;  // streaming: waves per captured CUDA graph (0: launched one by one)
     float bvh_traversal_cost = 0.5f; // SAH node-visit cost the BVH8 was built with (0.5: the fastest measured on the 1M-triangle scene)
     float bounds_lo[3] = {0, 0, 0}, bounds_hi[3] = {0, 0, 0}; // world box of the triangles
@@ -216,10 +229,12 @@ struct VgRenderer {
 
 struct VgAccum {
     VgRenderer* owner = nullptr;
+    int device = -1; // the owner's device (destroying the accumulation must not read the owner)
     uint32_t width = 0, height = 0;
     bool lighting = false;
     int precision = 64;
     uint32_t samples = 0;
+    uint32_t first_sample = 0; // sample index of the first sample (vg_accum_set_first_sample)
     double gpu_seconds = 0.0;
     bool stage_ran = false;
     double stage_seconds[2] = {0.0, 0.0};
@@ -257,8 +272,8 @@ namespace {
 
 // The device an object of the C ABI belongs to (-1 for a null handle).
 int dev_of(const VgContext* ctx) { return ctx ? ctx->device : -1; }
-int dev_of(const VgRenderer* r) { return r && r->ctx ? r->ctx->device : -1; }
-int dev_of(const VgAccum* acc) { return acc ? dev_of(acc->owner) : -1; }
+int dev_of(const VgRenderer* r) { return r ? r->device : -1; }
+int dev_of(const VgAccum* acc) { return acc ? acc->device : -1; }
 
 int check_fits(size_t bytes)
 {
@@ -414,6 +429,10 @@ vgk::Wave wave_of(const VgRenderer* r, const VgAccum* acc)
     w.meta = (uint32_t*)acc->meta.p;
     w.n = acc->width * acc->height;
     w.depth = r->max_depth;
+    w.refill = r->fetch_refill;
+    w.steps = r->fetch_steps;
+    w.shadow_refill = r->shadow_fetch_refill;
+    w.shadow_steps = r->shadow_fetch_steps;
     return w;
 }
 

@@ -268,24 +268,42 @@ int stream_deferred_blocks_per_sm(bool f64, int* shadow)
 
 namespace vgx {
 
-cudaError_t launch_stream_extend_dyn(bool stats, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
-                                     uint32_t wave)
+cudaError_t launch_stream_extend_dyn(bool stats, bool coop, int blocks, cudaStream_t s, const vgd::Ctx& c,
+                                     const vgk::Wave& w, uint32_t wave)
 {
-    if (stats)
-        vgk::wf_stream_extend_dyn<true><<<blocks, 128, 0, s>>>(c, w, wave);
+    if (stats && coop)
+        vgk::wf_stream_extend_dyn<true, true><<<blocks, 128, 0, s>>>(c, w, wave);
+    else if (stats)
+        vgk::wf_stream_extend_dyn<true, false><<<blocks, 128, 0, s>>>(c, w, wave);
+    else if (coop)
+        vgk::wf_stream_extend_dyn<false, true><<<blocks, 128, 0, s>>>(c, w, wave);
     else
-        vgk::wf_stream_extend_dyn<false><<<blocks, 128, 0, s>>>(c, w, wave);
+        vgk::wf_stream_extend_dyn<false, false><<<blocks, 128, 0, s>>>(c, w, wave);
     return cudaGetLastError();
 }
 
-cudaError_t launch_stream_shadow_trace(bool stats, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
-                                       uint32_t wave)
+cudaError_t launch_stream_shadow_trace(bool stats, bool coop, int blocks, cudaStream_t s, const vgd::Ctx& c,
+                                       const vgk::Wave& w, uint32_t wave)
 {
-    if (stats)
-        vgk::wf_stream_shadow_trace<true><<<blocks, 128, 0, s>>>(c, w, wave);
+    if (stats && coop)
+        vgk::wf_stream_shadow_trace<true, true><<<blocks, 128, 0, s>>>(c, w, wave);
+    else if (stats)
+        vgk::wf_stream_shadow_trace<true, false><<<blocks, 128, 0, s>>>(c, w, wave);
+    else if (coop)
+        vgk::wf_stream_shadow_trace<false, true><<<blocks, 128, 0, s>>>(c, w, wave);
     else
-        vgk::wf_stream_shadow_trace<false><<<blocks, 128, 0, s>>>(c, w, wave);
+        vgk::wf_stream_shadow_trace<false, false><<<blocks, 128, 0, s>>>(c, w, wave);
     return cudaGetLastError();
+}
+
+int stream_trace_blocks_per_sm(bool coop)
+{
+    int n = 0;
+    if (coop)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, vgk::wf_stream_extend_dyn<false, true>, 128, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, vgk::wf_stream_extend_dyn<false, false>, 128, 0);
+    return n > 0 ? n : 1;
 }
 
 cudaError_t launch_stream_finish(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,

@@ -59,6 +59,52 @@ static __device__ __forceinline__ uint32_t warp_fetch(uint32_t* counter)
     return __shfl_sync(FULL, base, 0);
 }
 
+// Block-level compaction: appends the `pred` threads of a block of WARPS warps to `queue` with one
+// atomic per block. Every thread of the block calls it. A block-wide exclusive scan over the warps'
+// ballot counts (warp 0 scans them with shuffles) gives each warp its offset in the block's range;
+// each lane writes at its warp's offset plus its rank in the ballot. `slot` is WARPS words of
+// shared memory. Each warp writes and reads only its own word outside the scan, so calls in a loop
+// need no barrier after the writes.
+template <uint32_t WARPS>
+__device__ __forceinline__ void block_append(uint32_t* count, uint32_t* queue, bool pred, uint32_t value, uint32_t* slot)
+{
+    uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    uint32_t b = __ballot_sync(FULL, pred);
+    if (lane == 0)
+        slot[warp] = __popc(b);
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t v = lane < WARPS ? slot[lane] : 0u;
+        uint32_t incl = v;
+#pragma unroll
+        for (uint32_t o = 1; o < WARPS; o <<= 1) {
+            uint32_t t = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o)
+                incl += t;
+        }
+        uint32_t total = __shfl_sync(FULL, incl, WARPS - 1);
+        uint32_t base = 0;
+        if (lane == 0 && total)
+            base = atomicAdd(count, total);
+        base = __shfl_sync(FULL, base, 0);
+        if (lane < WARPS)
+            slot[lane] = base + incl - v;
+    }
+    __syncthreads();
+    if (pred)
+        queue[slot[warp] + __popc(b & ((1u << lane) - 1u))] = value;
+}
+
+// Block-wide work fetch: blockDim.x consecutive items per atomic (thread 0 takes them, a barrier
+// hands them out). `word` is one word of shared memory.
+static __device__ __forceinline__ uint32_t block_fetch(uint32_t* counter, uint32_t* word)
+{
+    if (threadIdx.x == 0)
+        *word = atomicAdd(counter, blockDim.x);
+    __syncthreads();
+    return *word;
+}
+
 template <bool LIGHT>
 __device__ __forceinline__ void storePath(const Wave& w, const PathState<LIGHT>& s, uint32_t p)
 {
@@ -155,13 +201,15 @@ static __global__ void wf_begin(const __grid_constant__ Ctx c, Wave w)
     }
 }
 
-// wf_select.slang:7-18: queues the pixels that still take samples, warp aggregated.
+// wf_select.slang:7-18: queues the pixels that still take samples; one atomic per block of 256
+// (the reference takes one per pixel).
 template <typename A>
 __global__ void __launch_bounds__(256) wf_select(const __grid_constant__ Ctx c, Wave w)
 {
+    __shared__ uint32_t slot[8];
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     bool active = p < w.n && pixelActive<A>(c, p);
-    warp_append(&w.counts[0], w.queue[0], active, p);
+    block_append<8>(&w.counts[0], w.queue[0], active, p, slot);
 }
 
 // Sums a per-lane counter over the warp and adds it to a global 64-bit counter (lane 0).
@@ -312,6 +360,7 @@ __device__ __forceinline__ PathState<LIGHT> loadState(const Wave& w, uint32_t p)
 template <bool LIGHT, typename A, bool CACHE = false>
 __global__ void __launch_bounds__(256) wf_stream_start(const __grid_constant__ Ctx c, Wave w, CacheWave q)
 {
+    __shared__ uint32_t slot[8];
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     bool live = false;
     if (p < w.n && c.p[P_SAMPLES_PER_DISPATCH] > 0 && (c.p[P_ADAPTIVE] == 0 || pixelActive<A>(c, p)) &&
@@ -321,7 +370,7 @@ __global__ void __launch_bounds__(256) wf_stream_start(const __grid_constant__ C
         w.meta[p] = 0;
         live = true;
     }
-    warp_append(&w.counts[0], w.queue[0], live, p);
+    block_append<8>(&w.counts[0], w.queue[0], live, p, slot);
 }
 
 template <bool STATS>
@@ -539,11 +588,12 @@ __global__ void __launch_bounds__(128, 8) wf_stream_shadow(const __grid_constant
     const uint32_t* qin = w.queue[in];
     uint32_t* qout = w.queue[out];
     uint32_t n = w.n;
+    __shared__ uint32_t slot[4], fetched;
     for (;;) {
-        uint32_t base = warp_fetch(&w.fetch[4 + in]);
+        uint32_t base = block_fetch(&w.fetch[4 + in], &fetched);
         if (base >= count)
             break;
-        uint32_t i = base + lane_id();
+        uint32_t i = base + threadIdx.x;
         bool live = false;
         uint32_t p = 0;
         if (i < count) {
@@ -556,31 +606,33 @@ __global__ void __launch_bounds__(128, 8) wf_stream_shadow(const __grid_constant
             }
             live = finishSlot<A>(c, w, p, occ);
         }
-        __syncwarp();
-        warp_append(&w.counts[out], qout, live, p);
+        block_append<4>(&w.counts[out], qout, live, p, slot);
     }
 }
 
-// Dynamic-fetch forms of the streaming extend and shadow stages (vgt::trace_queue). Refill when
-// at least VG_REFILL lanes of a warp are idle; at most VG_STEPS node visits between refills.
-// Measured on the 1M-triangle workload (BVH8 with SAH node cost 0.5): refills of 4 to 10 lanes
-// are within 0.5% of one another and 2% faster than 16; 24 is 3% slower; 2 or 8 steps are slower
-// than 4.
-#ifndef VG_REFILL
-#define VG_REFILL 8
-#endif
-#ifndef VG_STEPS
-#define VG_STEPS 4
-#endif
-// The same for the any-hit shadow stage.
-#ifndef VG_SHADOW_REFILL
-#define VG_SHADOW_REFILL VG_REFILL
-#endif
-#ifndef VG_SHADOW_STEPS
-#define VG_SHADOW_STEPS VG_STEPS
-#endif
+// Dynamic-fetch forms of the streaming extend and shadow stages (vgt::trace_queue). A warp refills
+// when at least w.refill of its lanes are idle and runs at most w.steps node visits between refills
+// (w.shadow_refill, w.shadow_steps for the shadow stage; vg_set_traversal_fetch). Measured on the
+// 1M-triangle workload (BVH8 with SAH node cost 0.5, each lane testing its own triangles): refills
+// of 4 to 10 lanes are within 0.5% of one another and 2% faster than 16; 24 is 3% slower; 2 or 8
+// steps are slower than 4.
 
-template <bool STATS>
+// Runs trace_queue, or with COOP trace_queue_coop (warp-cooperative leaf testing; blocks of 128
+// threads, the launchers' size): the same hits either way.
+template <bool ANY, bool COOP, typename GetRay, typename PutHit>
+__device__ __forceinline__ void trace_queue_any(const Ctx& c, uint32_t* fetch, uint32_t count, uint32_t refill,
+                                                uint32_t steps, GetRay get, PutHit put)
+{
+    if (COOP) {
+        __shared__ vgt::CoopWarp coop[vgt::COOP_WARPS];
+        vgt::trace_queue_coop<ANY>(c.s.nodes, c.s.tris, fetch, count, c.err, refill, steps, coop[threadIdx.x >> 5],
+                                   get, put);
+    } else {
+        vgt::trace_queue<ANY>(c.s.nodes, c.s.tris, fetch, count, c.err, refill, steps, get, put);
+    }
+}
+
+template <bool STATS, bool COOP>
 __global__ void __launch_bounds__(128, 8) wf_stream_extend_dyn(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
 {
     uint32_t in = wave & 1u, out = in ^ 1u;
@@ -593,8 +645,8 @@ __global__ void __launch_bounds__(128, 8) wf_stream_extend_dyn(const __grid_cons
     uint32_t count = w.counts[in];
     const uint32_t* qin = w.queue[in];
     uint32_t n_rays = 0, n_nodes = 0, n_tests = 0, n_later = 0;
-    vgt::trace_queue<false, VG_REFILL, VG_STEPS>(
-        c.s.nodes, c.s.tris, &w.fetch[in], count, c.err,
+    trace_queue_any<false, COOP>(
+        c, &w.fetch[in], count, w.refill, w.steps,
         [&](uint32_t i, V3& o, V3& d, float& tmax) {
             uint32_t p = qin[i];
             float4 a = w.state[p];
@@ -626,7 +678,7 @@ __global__ void __launch_bounds__(128, 8) wf_stream_extend_dyn(const __grid_cons
 // Shadow rays of the deferred light samples, any hit (opaque scenes: one layer, no opacity roll).
 // The result goes to hits[p].x (1 occluded), which the finish stage reads. STATS: the rays traced
 // are counted into tstats[4].
-template <bool STATS>
+template <bool STATS, bool COOP>
 __global__ void __launch_bounds__(128, 8) wf_stream_shadow_trace(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
 {
     uint32_t in = wave & 1u;
@@ -634,8 +686,8 @@ __global__ void __launch_bounds__(128, 8) wf_stream_shadow_trace(const __grid_co
     const uint32_t* qin = w.queue[in];
     uint32_t n = w.n;
     uint32_t n_rays = 0;
-    vgt::trace_queue<true, VG_SHADOW_REFILL, VG_SHADOW_STEPS>(
-        c.s.nodes, c.s.tris, &w.fetch[4 + in], count, c.err,
+    trace_queue_any<true, COOP>(
+        c, &w.fetch[4 + in], count, w.shadow_refill, w.shadow_steps,
         [&](uint32_t i, V3& o, V3& d, float& tmax) {
             uint32_t p = qin[i];
             float4 r1 = w.sreq[n + p];
@@ -667,19 +719,19 @@ __global__ void __launch_bounds__(128, 8) wf_stream_finish(const __grid_constant
     uint32_t count = w.counts[in];
     const uint32_t* qin = w.queue[in];
     uint32_t* qout = w.queue[out];
+    __shared__ uint32_t slot[4], fetched;
     for (;;) {
-        uint32_t base = warp_fetch(&w.fetch[6 + in]);
+        uint32_t base = block_fetch(&w.fetch[6 + in], &fetched);
         if (base >= count)
             break;
-        uint32_t i = base + lane_id();
+        uint32_t i = base + threadIdx.x;
         bool live = false;
         uint32_t p = 0;
         if (i < count) {
             p = qin[i];
             live = finishSlot<A>(c, w, p, ((const uint32_t*)w.hits)[4 * (size_t)p] != 0u);
         }
-        __syncwarp();
-        warp_append(&w.counts[out], qout, live, p);
+        block_append<4>(&w.counts[out], qout, live, p, slot);
     }
 }
 

@@ -45,10 +45,12 @@ cudaError_t launch_stream_shadow(bool f64, int blocks, cudaStream_t s, const vgd
                                  uint32_t wave);
 int stream_deferred_blocks_per_sm(bool f64, int* shadow);
 // Dynamic-fetch traversal stages: extend, the shadow trace of opaque scenes, then finish.
-cudaError_t launch_stream_extend_dyn(bool stats, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
-                                     uint32_t wave);
-cudaError_t launch_stream_shadow_trace(bool stats, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
-                                       uint32_t wave);
+// With `coop` the warp-cooperative leaf testing of traverse.cuh (the same hits).
+cudaError_t launch_stream_extend_dyn(bool stats, bool coop, int blocks, cudaStream_t s, const vgd::Ctx& c,
+                                     const vgk::Wave& w, uint32_t wave);
+cudaError_t launch_stream_shadow_trace(bool stats, bool coop, int blocks, cudaStream_t s, const vgd::Ctx& c,
+                                       const vgk::Wave& w, uint32_t wave);
+int stream_trace_blocks_per_sm(bool coop);
 cudaError_t launch_stream_finish(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
                                  uint32_t wave);
 // Finishes every slot still live after `wave` (at most max_slots of them) in one launch.

@@ -222,12 +222,12 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
         VG_CHECK(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed), "graph capture");
         cudaError_t ce = cudaSuccess;
         for (uint32_t i = 0; i < K && ce == cudaSuccess; i++) {
-            ce = r->dynamic_fetch ? vgx::launch_stream_extend_dyn(r->traversal_stats, eb, s, c, w, i)
+            ce = r->dynamic_fetch ? vgx::launch_stream_extend_dyn(r->traversal_stats, r->coop_tris, eb, s, c, w, i)
                                   : vgx::launch_stream_extend(r->traversal_stats, eb, s, c, w, i);
             if (ce == cudaSuccess && deferred) {
                 ce = (q ? vgx::launch_stream_cache_shade(v.f64, csb, s, c, w, i, *q) : vgx::launch_stream_shade_deferred(v.f64, dsb, s, c, w, i));
                 if (ce == cudaSuccess && r->dynamic_fetch && r->ds.shadow_any) {
-                    ce = vgx::launch_stream_shadow_trace(r->traversal_stats, shb, s, c, w, i);
+                    ce = vgx::launch_stream_shadow_trace(r->traversal_stats, r->coop_tris, shb, s, c, w, i);
                     if (ce == cudaSuccess)
                         ce = vgx::launch_stream_finish(v.f64, shb, s, c, w, i);
                 } else if (ce == cudaSuccess)
@@ -298,7 +298,7 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
             VG_CHECK(cudaEventRecord(a, s), "event");
         }
         if (r->dynamic_fetch)
-            VG_CHECK(vgx::launch_stream_extend_dyn(r->traversal_stats, eb, s, c, w, (uint32_t)wave),
+            VG_CHECK(vgx::launch_stream_extend_dyn(r->traversal_stats, r->coop_tris, eb, s, c, w, (uint32_t)wave),
                      "extend launch");
         else
             VG_CHECK(vgx::launch_stream_extend(r->traversal_stats, eb, s, c, w, (uint32_t)wave),
@@ -313,7 +313,7 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
                 VG_CHECK(cudaEventRecord(qe, s), "event");
             }
             if (r->dynamic_fetch && r->ds.shadow_any) {
-                VG_CHECK(vgx::launch_stream_shadow_trace(r->traversal_stats, shb, s, c, w, (uint32_t)wave), "shadow launch");
+                VG_CHECK(vgx::launch_stream_shadow_trace(r->traversal_stats, r->coop_tris, shb, s, c, w, (uint32_t)wave), "shadow launch");
                 VG_CHECK(vgx::launch_stream_finish(v.f64, shb, s, c, w, (uint32_t)wave), "finish launch");
                 acc->launches++;
             } else {
@@ -488,6 +488,7 @@ int vg_renderer_create(VgContext* ctx, const VgPacked* pk, VgRenderer** out)
         return st;
     VgRenderer* r = new VgRenderer();
     r->ctx = ctx;
+    r->device = ctx->device;
     r->info = pk->info;
     r->view = pk->view;
     r->instance_count = (uint32_t)pk->instance_count;
@@ -806,6 +807,29 @@ int vg_set_dynamic_fetch(VgRenderer* r, int on)
     return VG_OK;
 }
 
+int vg_set_coop_triangles(VgRenderer* r, int on)
+{
+    if (!r)
+        return fail(VG_ERR_INVALID, "null renderer");
+    r->coop_tris = on != 0;
+    return VG_OK;
+}
+
+int vg_set_traversal_fetch(VgRenderer* r, uint32_t refill, uint32_t steps, uint32_t shadow_refill,
+                           uint32_t shadow_steps)
+{
+    if (!r)
+        return fail(VG_ERR_INVALID, "null renderer");
+    if (refill < 1 || refill > 32 || shadow_refill < 1 || shadow_refill > 32 || steps < 1 || steps > 64 ||
+        shadow_steps < 1 || shadow_steps > 64)
+        return fail(VG_ERR_INVALID, "refill must be 1-32 lanes and steps 1-64 node visits");
+    r->fetch_refill = refill;
+    r->fetch_steps = steps;
+    r->shadow_fetch_refill = shadow_refill;
+    r->shadow_fetch_steps = shadow_steps;
+    return VG_OK;
+}
+
 int vg_set_deferred_shadows(VgRenderer* r, int on)
 {
     if (!r)
@@ -886,6 +910,7 @@ int vg_accum_create(VgRenderer* r, uint32_t width, uint32_t height, int lighting
         return fail(VG_ERR_INVALID, "image too large");
     VgAccum* acc = new VgAccum();
     acc->owner = r;
+    acc->device = r->device;
     acc->width = width;
     acc->height = height;
     acc->lighting = lighting != 0;
@@ -970,6 +995,11 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
     }
     if (!(acc->restir == r->restir))
         return fail(VG_ERR_SCENE, "ReSTIR was switched mid-accumulation; start a new accumulation");
+    if (acc->first_sample != 0 && (acc->restir.on || r->cache))
+        return fail(VG_ERR_SCENE, "a first sample index other than 0 needs plain path tracing (no ReSTIR, no cache)");
+    if ((uint64_t)acc->first_sample + acc->samples + samples > 0xffffffffull)
+        return fail(VG_ERR_INVALID, "sample index beyond 2^32 - 1");
+    const uint32_t sample0 = acc->first_sample + acc->samples; // index of this call's first sample
     bool wavefront = r->integrator == VG_WAVEFRONT && !r->cache;
     const uint32_t max_depth_alloc = 64;
     if (r->integrator == VG_WAVEFRONT && !acc->state.p) {
@@ -1010,7 +1040,7 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
         dim3 grid((acc->width + 15) / 16, (acc->height + 7) / 8);
         uint32_t k = 0;
         while (k < samples) {
-            c.p[P_SAMPLE] = acc->samples + k;
+            c.p[P_SAMPLE] = sample0 + k;
             c.p[P_SAMPLES_PER_DISPATCH] = std::min<uint32_t>(samples - k, acc->restir.on ? 1u : 8u);
             k += c.p[P_SAMPLES_PER_DISPATCH];
             VG_CHECK(vgx::launch_megakernel(v, grid, s, c), "megakernel launch");
@@ -1027,11 +1057,11 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
         bool streaming = r->wavefront_mode == VG_WAVEFRONT_STREAMING && !acc->restir.on;
         if (streaming && samples > 0) {
             streamed = true;
-            if ((st = stream_samples(r, acc, c, v, w, acc->samples, samples, timed, pool, stages, nullptr)) != VG_OK)
+            if ((st = stream_samples(r, acc, c, v, w, sample0, samples, timed, pool, stages, nullptr)) != VG_OK)
                 return st;
         }
         for (uint32_t k = 0; k < (streaming ? 0u : samples); k++) {
-            c.p[P_SAMPLE] = acc->samples + k;
+            c.p[P_SAMPLE] = sample0 + k;
             VG_CHECK(vgx::launch_wf_begin(s, c, w), "wf_begin launch");
             acc->launches++;
             if (acc->adaptive) {
@@ -1093,6 +1123,16 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
 }
 
 uint32_t vg_accum_samples(const VgAccum* acc) { return acc ? acc->samples : 0; }
+
+int vg_accum_set_first_sample(VgAccum* acc, uint32_t first)
+{
+    if (!acc)
+        return fail(VG_ERR_INVALID, "null accumulation");
+    if (acc->samples != 0)
+        return fail(VG_ERR_INVALID, "the first sample index is set before the first sample");
+    acc->first_sample = first;
+    return VG_OK;
+}
 double vg_accum_gpu_seconds(const VgAccum* acc) { return acc ? acc->gpu_seconds : 0.0; }
 
 int vg_accum_stage_seconds(const VgAccum* acc, double out[2])
@@ -1336,6 +1376,34 @@ int vg_autotune(VgRenderer* r, const VgPacked* pk, uint32_t width, uint32_t heig
             return o;
         },
         std::vector<uint32_t>{r->graph_waves == 0 ? 8u : 0u});
+    try_setting(
+        [&](bool v, bool) {
+            bool o = r->coop_tris;
+            r->coop_tris = v;
+            return o;
+        },
+        std::vector<bool>{!r->coop_tris});
+    std::vector<uint32_t> refills, steps;
+    for (uint32_t v : {4u, 8u, 16u})
+        if (v != r->fetch_refill)
+            refills.push_back(v);
+    try_setting(
+        [&](uint32_t v, bool) {
+            uint32_t o = r->fetch_refill;
+            r->fetch_refill = r->shadow_fetch_refill = v;
+            return o;
+        },
+        refills);
+    for (uint32_t v : {2u, 4u, 8u})
+        if (v != r->fetch_steps)
+            steps.push_back(v);
+    try_setting(
+        [&](uint32_t v, bool) {
+            uint32_t o = r->fetch_steps;
+            r->fetch_steps = r->shadow_fetch_steps = v;
+            return o;
+        },
+        steps);
     int most = vgx::wf_extend_blocks_per_sm();
     std::vector<int> extend_blocks;
     for (int b : {most, (3 * most) / 4, most / 2})
@@ -1373,6 +1441,9 @@ int vg_autotune(VgRenderer* r, const VgPacked* pk, uint32_t width, uint32_t heig
     out->graph_waves = r->graph_waves;
     out->bvh_traversal_cost = r->bvh_traversal_cost;
     out->extend_blocks_per_sm = r->extend_blocks;
+    out->coop_triangles = r->coop_tris;
+    out->fetch_refill = r->fetch_refill;
+    out->fetch_steps = r->fetch_steps;
     out->mpaths_after = best;
     out->trials = trials;
     return VG_OK;
