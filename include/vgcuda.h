@@ -213,9 +213,10 @@ int vg_set_deferred_shadows(VgRenderer* r, int on);
  * (default on) or give each warp 32 rays at a time (off). Same results either way. */
 int vg_set_dynamic_fetch(VgRenderer* r, int on);
 /* Streaming mode with dynamic fetch: the extend and shadow stages test the triangles of the leaves
- * their warp's rays reached together, one (ray, triangle) pair per lane (default on), or each lane
- * its own (off). Same results either way. No reference counterpart: the reference's hardware ray
- * queries have no such choice. */
+ * their warp's rays reached together, one (ray, triangle) pair per lane (on), or each lane its own
+ * (off, the default: on the 1M-triangle workload the cooperative form's scan, shuffles and
+ * shared-memory reductions cost more than the idle lanes they save). Same results either way. No
+ * reference counterpart: the reference's hardware ray queries have no such choice. */
 int vg_set_coop_triangles(VgRenderer* r, int on);
 /* Streaming mode with dynamic fetch: a warp of the extend stage takes new rays once at least
  * `refill` of its 32 lanes are idle (1-32, default 8) and visits at most `steps` nodes per lane

@@ -261,6 +261,11 @@ struct QHit {
     R t = 0, b1 = 0, b2 = 0;
 };
 
+// The far side is widened by the slab test's rounding bound (robust_far). The closest hit so far
+// (tmax) is widened by 2^-18 relative as well: the triangle test computes its t with roundings of
+// its own, so a triangle whose computed t is below the best one can sit in a box whose computed
+// entry is a few ulps above it (a flat box in the plane of the hit, e.g. a floor made of many
+// triangles). Culling is only a shortcut here, so the margin costs speed, never a hit.
 template <class R>
 bool box_hit(const Ray<R>& r, const float* lo, const float* hi, R tmax)
 {
@@ -273,7 +278,7 @@ bool box_hit(const Ray<R>& r, const float* lo, const float* hi, R tmax)
         tn = mmax(tn, t0);
         tf = mmin(tf, t1);
     }
-    tf = mmin(tf * robust_far<R>(), tmax);
+    tf = mmin(tf * robust_far<R>(), tmax * R(1.0 + 1.0 / 262144.0));
     return tn <= tf;
 }
 

@@ -301,3 +301,25 @@ def test_opacity_lets_rays_and_shadows_through(oracle_lib):
     assert abs(lit(0.0) - full) < 0.02 * full
     assert lit(1.0) < 0.02 * full
     assert abs(lit(0.5) - 0.5 * full) < 0.08 * full
+
+
+def test_oracle_bvh_finds_the_brute_force_hits_on_a_floor_grid(oracle_lib):
+    # The many-light scene's floor is a grid of coplanar triangles: the computed t of two
+    # neighbours sharing an edge can differ by an ulp, and the box test must not cull the nearer
+    # one's flat box against the farther one's t. The ray below once hit triangle 141917 at
+    # t = 0x41380a7b instead of 142548 at 0x41380a7a through the oracle's BVH.
+    import struct
+
+    p = pack.pack(scenes.many_lights())
+    o = oracle.OracleScene(p)
+    f = lambda h: struct.unpack("<f", struct.pack("<I", h))[0]  # noqa: E731
+    one = np.array([[0.0, 6.0, 14.0, f(0x3DB768F6), f(0xBF058916), f(0xBF5934DC)]], np.float32)
+    assert o.trace_closest(one)[0].tolist() == [1, 0, 142548, 0x41380A7A]
+    rng = np.random.default_rng(3)
+    n = 20000
+    org = np.array([0.0, 6.0, 14.0]) + rng.normal(scale=0.5, size=(n, 3))
+    d = rng.normal(size=(n, 3))
+    d[:, 1] = -np.abs(d[:, 1])
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.concatenate([org, d], 1).astype(np.float32)
+    assert np.array_equal(o.trace_closest(rays), o.trace_closest(rays, brute=True))

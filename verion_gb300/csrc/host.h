@@ -210,7 +210,7 @@ struct VgRenderer {
     int shadow_blocks[2] = {};
     bool defer_shadows = true; // streaming: shadow rays of the light sample in their own stage
     bool dynamic_fetch = true; // streaming: traversal stages refill idle lanes from the queue
-    bool coop_tris = true;     // streaming, dynamic fetch: warp-cooperative leaf testing
+    bool coop_tris = false;    // streaming, dynamic fetch: warp-cooperative leaf testing (measured slower)
     uint32_t fetch_refill = 8, fetch_steps = 4;               // dynamic fetch, extend stage
     uint32_t shadow_fetch_refill = 8, shadow_fetch_steps = 4; // dynamic fetch, shadow stage
     uint32_t graph_waves = 0;  // streaming: waves per captured CUDA graph (0: launched one by one)

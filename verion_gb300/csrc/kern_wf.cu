@@ -139,6 +139,8 @@ cudaError_t launch_stream_extend(bool stats, int blocks, cudaStream_t s, const v
 cudaError_t launch_stream_shade(Variant v, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
                                 uint32_t wave)
 {
+    if (v.restir)
+        return launch_stream_shade_restir(v, blocks, s, c, w, wave);
     if (v.light && v.f64)
         return sshade<true, double>(blocks, s, c, w, wave);
     if (v.light)
@@ -150,6 +152,8 @@ cudaError_t launch_stream_shade(Variant v, int blocks, cudaStream_t s, const vgd
 
 int stream_shade_blocks_per_sm(Variant v)
 {
+    if (v.restir)
+        return stream_shade_restir_blocks_per_sm(v);
     if (v.light && v.f64)
         return sshade_occ<true, double>();
     if (v.light)
@@ -166,6 +170,8 @@ namespace vgx {
 cudaError_t launch_stream_tail(Variant v, uint32_t max_slots, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
                                uint32_t wave)
 {
+    if (v.restir)
+        return launch_stream_tail_restir(v, max_slots, s, c, w, wave);
     unsigned blocks = (max_slots + 127) / 128;
     if (blocks == 0)
         return cudaSuccess;

@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(128, 8) wf_stream_extend(const __grid_constant
     }
 }
 
-template <bool LIGHT, typename A>
+template <bool LIGHT, typename A, bool RESTIR = false>
 __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
 {
     uint32_t in = wave & 1u, out = in ^ 1u;
@@ -443,12 +443,12 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade(cons
             h.inst = hr.y;
             h.prim = hr.z;
             h.t = __uint_as_float(hr.w);
-            if (shadePath<LIGHT, false>(c, st, h, depth, p) && depth + 1 < w.depth) {
+            if (shadePath<LIGHT, RESTIR>(c, st, h, depth, p) && depth + 1 < w.depth) {
                 storePath<LIGHT>(w, st, p);
                 w.meta[p] = (depth + 1) | (k << 8);
                 live = true;
             } else {
-                finishPath<LIGHT, A>(c, st, p);
+                finishPath<LIGHT, A, RESTIR>(c, st, p);
                 if (k + 1 < batch && (c.p[P_ADAPTIVE] == 0 || pixelActive<A>(c, p))) {
                     PathState<LIGHT> nx =
                         generatePathFor<LIGHT>(c, p % c.p[P_WIDTH], p / c.p[P_WIDTH], c.p[P_SAMPLE] + k + 1);
@@ -470,7 +470,7 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade(cons
 // flags: bit 0 a request is present, bit 1 the path goes on to the next depth.
 // With CACHE a path also ends where its spread passes the cache threshold (shadePath's cache
 // hook); it then leaves a query record (one atomic per warp) and finishes like any other.
-template <typename A, bool CACHE = false>
+template <typename A, bool CACHE = false, bool RESTIR = false>
 __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade_deferred(const __grid_constant__ Ctx c,
                                                                                     Wave w, uint32_t wave,
                                                                                     CacheWave q)
@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade_defe
                 hk.a0 = sp.x;
                 hk.a = sp.y;
             }
-            bool alive = shadePath<false, false, true, CACHE>(c, st, h, depth, p, &req, &hk) && depth + 1 < w.depth;
+            bool alive = shadePath<false, RESTIR, true, CACHE>(c, st, h, depth, p, &req, &hk) && depth + 1 < w.depth;
             if (CACHE) {
                 query = hk.query && !bad3(st.parts.total);
                 if (alive)
@@ -545,7 +545,7 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade_defe
 // Finish of one slot after its shadow ray (or with no light sample): add the unoccluded sample,
 // then queue the path for its next depth, or finish it and restart the slot with the batch's next
 // sample. Returns whether the slot goes to the next wave's queue.
-template <typename A>
+template <typename A, bool RESTIR = false>
 __device__ __forceinline__ bool finishSlot(const Ctx& c, const Wave& w, uint32_t p, bool blocked)
 {
     uint32_t n = w.n;
@@ -568,7 +568,7 @@ __device__ __forceinline__ bool finishSlot(const Ctx& c, const Wave& w, uint32_t
     st.parts.zero();
     st.parts.total = total;
     st.visLit = st.visTotal = 0.0f;
-    finishPath<false, A>(c, st, p);
+    finishPath<false, A, RESTIR>(c, st, p);
     if (k + 1 < c.p[P_SAMPLES_PER_DISPATCH] && (c.p[P_ADAPTIVE] == 0 || pixelActive<A>(c, p))) {
         PathState<false> nx = generatePathFor<false>(c, p % c.p[P_WIDTH], p / c.p[P_WIDTH], c.p[P_SAMPLE] + k + 1);
         storePath<false>(w, nx, p);
@@ -578,7 +578,7 @@ __device__ __forceinline__ bool finishSlot(const Ctx& c, const Wave& w, uint32_t
     return false;
 }
 
-template <typename A>
+template <typename A, bool RESTIR = false>
 __global__ void __launch_bounds__(128, 8) wf_stream_shadow(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
 {
     uint32_t in = wave & 1u, out = in ^ 1u;
@@ -604,7 +604,7 @@ __global__ void __launch_bounds__(128, 8) wf_stream_shadow(const __grid_constant
                 float4 r0 = w.sreq[p];
                 occ = occluded(c, v3(r0.x, r0.y, r0.z), v3(r1.x, r1.y, r1.z), r0.w);
             }
-            live = finishSlot<A>(c, w, p, occ);
+            live = finishSlot<A, RESTIR>(c, w, p, occ);
         }
         block_append<4>(&w.counts[out], qout, live, p, slot);
     }
@@ -632,8 +632,14 @@ __device__ __forceinline__ void trace_queue_any(const Ctx& c, uint32_t* fetch, u
     }
 }
 
+// Minimum resident 128-thread blocks per SM requested for the dynamic-fetch traversal stages (a
+// register cap: 8 blocks leave 64 registers per thread).
+#ifndef VG_TRACE_MIN_BLOCKS
+#define VG_TRACE_MIN_BLOCKS 8
+#endif
+
 template <bool STATS, bool COOP>
-__global__ void __launch_bounds__(128, 8) wf_stream_extend_dyn(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
+__global__ void __launch_bounds__(128, VG_TRACE_MIN_BLOCKS) wf_stream_extend_dyn(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
 {
     uint32_t in = wave & 1u, out = in ^ 1u;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -679,7 +685,7 @@ __global__ void __launch_bounds__(128, 8) wf_stream_extend_dyn(const __grid_cons
 // The result goes to hits[p].x (1 occluded), which the finish stage reads. STATS: the rays traced
 // are counted into tstats[4].
 template <bool STATS, bool COOP>
-__global__ void __launch_bounds__(128, 8) wf_stream_shadow_trace(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
+__global__ void __launch_bounds__(128, VG_TRACE_MIN_BLOCKS) wf_stream_shadow_trace(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
 {
     uint32_t in = wave & 1u;
     uint32_t count = w.counts[in];
@@ -710,7 +716,7 @@ __global__ void __launch_bounds__(128, 8) wf_stream_shadow_trace(const __grid_co
 
 // After the shadow trace: add the unoccluded light sample, then queue, finish or restart each slot
 // (the second half of wf_stream_shadow).
-template <typename A>
+template <typename A, bool RESTIR = false>
 __global__ void __launch_bounds__(128, 8) wf_stream_finish(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
 {
     uint32_t in = wave & 1u, out = in ^ 1u;
@@ -729,7 +735,7 @@ __global__ void __launch_bounds__(128, 8) wf_stream_finish(const __grid_constant
         uint32_t p = 0;
         if (i < count) {
             p = qin[i];
-            live = finishSlot<A>(c, w, p, ((const uint32_t*)w.hits)[4 * (size_t)p] != 0u);
+            live = finishSlot<A, RESTIR>(c, w, p, ((const uint32_t*)w.hits)[4 * (size_t)p] != 0u);
         }
         block_append<4>(&w.counts[out], qout, live, p, slot);
     }
@@ -739,7 +745,7 @@ __global__ void __launch_bounds__(128, 8) wf_stream_finish(const __grid_constant
 // path and the rest of its samples to the end, trace and shade in a loop as the megakernel does,
 // instead of one half-empty wave per bounce. Same functions, same order per pixel, same sums.
 // With CACHE (lighting split off) paths end at the cache as in wf_stream_shade_deferred.
-template <bool LIGHT, typename A, bool CACHE = false>
+template <bool LIGHT, typename A, bool CACHE = false, bool RESTIR = false>
 __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_tail(const __grid_constant__ Ctx c, Wave w,
                                                                           uint32_t wave, CacheWave q)
 {
@@ -762,7 +768,7 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_tail(const
         hk.a = sp.y;
     }
     for (;;) {
-        if (shadePath<LIGHT, false, false, CACHE>(c, st, traceClosest(c, st.org, st.dir), depth, p, nullptr, &hk) &&
+        if (shadePath<LIGHT, RESTIR, false, CACHE>(c, st, traceClosest(c, st.org, st.dir), depth, p, nullptr, &hk) &&
             depth + 1 < w.depth) {
             depth++;
             continue;
@@ -772,7 +778,7 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_tail(const
             if (slot < q.qcap)
                 cacheQueryRecord(q.qrec + ((size_t)k * q.qcap + slot) * CACHE_REC_WORDS, hk, p);
         }
-        finishPath<LIGHT, A>(c, st, p);
+        finishPath<LIGHT, A, RESTIR>(c, st, p);
         if (k + 1 < batch && (c.p[P_ADAPTIVE] == 0 || pixelActive<A>(c, p))) {
             k++;
             depth = 0;

@@ -53,6 +53,19 @@ cudaError_t launch_stream_shadow_trace(bool stats, bool coop, int blocks, cudaSt
 int stream_trace_blocks_per_sm(bool coop);
 cudaError_t launch_stream_finish(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
                                  uint32_t wave);
+// The same streaming stages compiled with ReSTIR (kern_wf_restir.cu); the host runs them one
+// sample per launch sequence.
+cudaError_t launch_stream_shade_restir(Variant v, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                                       uint32_t wave);
+int stream_shade_restir_blocks_per_sm(Variant v);
+cudaError_t launch_stream_tail_restir(Variant v, uint32_t max_slots, cudaStream_t s, const vgd::Ctx& c,
+                                      const vgk::Wave& w, uint32_t wave);
+cudaError_t launch_stream_shade_deferred_restir(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c,
+                                                const vgk::Wave& w, uint32_t wave);
+cudaError_t launch_stream_shadow_restir(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                                        uint32_t wave);
+cudaError_t launch_stream_finish_restir(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
+                                        uint32_t wave);
 // Finishes every slot still live after `wave` (at most max_slots of them) in one launch.
 cudaError_t launch_stream_tail(Variant v, uint32_t max_slots, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
                                uint32_t wave);

@@ -98,8 +98,8 @@ static __device__ __forceinline__ void grid_backward(const CacheDev& cd, const f
             float w = ((k & 1u) ? fx : 1.0f - fx) * ((k & 2u) ? fy : 1.0f - fy);
             w = w * ((k & 4u) ? fz : 1.0f - fz);
             uint32_t e = grid_index(ix + (k & 1u), iy + ((k >> 1) & 1u), iz + ((k >> 2) & 1u), res, dense, mask);
-            atomicAdd(gg + 2 * (size_t)e, w * g0);
-            atomicAdd(gg + 2 * (size_t)e + 1, w * g1);
+            // Both features of the entry in one 8-byte atomic (an entry's pair is 8-byte aligned).
+            atomicAdd(reinterpret_cast<float2*>(gg + 2 * (size_t)e), make_float2(w * g0, w * g1));
         }
     }
 }

@@ -186,7 +186,9 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
         r->stream_shade_blocks[svi] = vgx::stream_shade_blocks_per_sm(v);
     int ssb = blocks_for(r, r->stream_shade_blocks[svi]);
     // Lighting split off: three-stage waves with the shadow rays in their own kernel.
-    bool deferred = (!acc->lighting && r->defer_shadows) || q;
+    // ReSTIR GI records the second vertex's direct light while shading it, so with GI the light
+    // sample's shadow ray is traced inside shade.
+    bool deferred = (!acc->lighting && r->defer_shadows && !(v.restir && acc->restir.gi)) || q;
     if (deferred && r->deferred_blocks[v.f64 ? 1 : 0] == 0)
         r->deferred_blocks[v.f64 ? 1 : 0] =
             vgx::stream_deferred_blocks_per_sm(v.f64, &r->shadow_blocks[v.f64 ? 1 : 0]);
@@ -225,13 +227,13 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
             ce = r->dynamic_fetch ? vgx::launch_stream_extend_dyn(r->traversal_stats, r->coop_tris, eb, s, c, w, i)
                                   : vgx::launch_stream_extend(r->traversal_stats, eb, s, c, w, i);
             if (ce == cudaSuccess && deferred) {
-                ce = (q ? vgx::launch_stream_cache_shade(v.f64, csb, s, c, w, i, *q) : vgx::launch_stream_shade_deferred(v.f64, dsb, s, c, w, i));
+                ce = (q ? vgx::launch_stream_cache_shade(v.f64, csb, s, c, w, i, *q) : (v.restir ? vgx::launch_stream_shade_deferred_restir : vgx::launch_stream_shade_deferred)(v.f64, dsb, s, c, w, i));
                 if (ce == cudaSuccess && r->dynamic_fetch && r->ds.shadow_any) {
                     ce = vgx::launch_stream_shadow_trace(r->traversal_stats, r->coop_tris, shb, s, c, w, i);
                     if (ce == cudaSuccess)
-                        ce = vgx::launch_stream_finish(v.f64, shb, s, c, w, i);
+                        ce = (v.restir ? vgx::launch_stream_finish_restir : vgx::launch_stream_finish)(v.f64, shb, s, c, w, i);
                 } else if (ce == cudaSuccess)
-                    ce = vgx::launch_stream_shadow(v.f64, shb, s, c, w, i);
+                    ce = (v.restir ? vgx::launch_stream_shadow_restir : vgx::launch_stream_shadow)(v.f64, shb, s, c, w, i);
             } else if (ce == cudaSuccess)
                 ce = vgx::launch_stream_shade(v, ssb, s, c, w, i);
         }
@@ -306,7 +308,7 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
         if (timed)
             VG_CHECK(cudaEventRecord(m, s), "event");
         if (deferred) {
-            VG_CHECK((q ? vgx::launch_stream_cache_shade(v.f64, csb, s, c, w, (uint32_t)wave, *q) : vgx::launch_stream_shade_deferred(v.f64, dsb, s, c, w, (uint32_t)wave)), "shade launch");
+            VG_CHECK((q ? vgx::launch_stream_cache_shade(v.f64, csb, s, c, w, (uint32_t)wave, *q) : (v.restir ? vgx::launch_stream_shade_deferred_restir : vgx::launch_stream_shade_deferred)(v.f64, dsb, s, c, w, (uint32_t)wave)), "shade launch");
             cudaEvent_t qe = nullptr;
             if (timed) {
                 qe = pool.get();
@@ -314,10 +316,10 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
             }
             if (r->dynamic_fetch && r->ds.shadow_any) {
                 VG_CHECK(vgx::launch_stream_shadow_trace(r->traversal_stats, r->coop_tris, shb, s, c, w, (uint32_t)wave), "shadow launch");
-                VG_CHECK(vgx::launch_stream_finish(v.f64, shb, s, c, w, (uint32_t)wave), "finish launch");
+                VG_CHECK((v.restir ? vgx::launch_stream_finish_restir : vgx::launch_stream_finish)(v.f64, shb, s, c, w, (uint32_t)wave), "finish launch");
                 acc->launches++;
             } else {
-                VG_CHECK(vgx::launch_stream_shadow(v.f64, shb, s, c, w, (uint32_t)wave), "shadow launch");
+                VG_CHECK((v.restir ? vgx::launch_stream_shadow_restir : vgx::launch_stream_shadow)(v.f64, shb, s, c, w, (uint32_t)wave), "shadow launch");
             }
             if (timed) {
                 VG_CHECK(cudaEventRecord(b, s), "event");
@@ -1054,11 +1056,15 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
             r->shade_blocks[vi] = vgx::wf_shade_blocks_per_sm(v);
         int eb = blocks_for(r, r->extend_blocks);
         int sb = blocks_for(r, r->shade_blocks[vi]);
-        bool streaming = r->wavefront_mode == VG_WAVEFRONT_STREAMING && !acc->restir.on;
+        bool streaming = r->wavefront_mode == VG_WAVEFRONT_STREAMING;
         if (streaming && samples > 0) {
             streamed = true;
-            if ((st = stream_samples(r, acc, c, v, w, sample0, samples, timed, pool, stages, nullptr)) != VG_OK)
-                return st;
+            // Under ReSTIR one sample per launch sequence: a sample's paths read the reservoirs the
+            // previous sample left (the other frame parity), which must be complete by then.
+            uint32_t per = acc->restir.on ? 1u : samples;
+            for (uint32_t k = 0; k < samples; k += per)
+                if ((st = stream_samples(r, acc, c, v, w, sample0 + k, per, timed, pool, stages, nullptr)) != VG_OK)
+                    return st;
         }
         for (uint32_t k = 0; k < (streaming ? 0u : samples); k++) {
             c.p[P_SAMPLE] = sample0 + k;
