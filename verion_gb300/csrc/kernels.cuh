@@ -568,6 +568,10 @@ __device__ __forceinline__ bool finishSlot(const Ctx& c, const Wave& w, uint32_t
     st.parts.zero();
     st.parts.total = total;
     st.visLit = st.visTotal = 0.0f;
+    // The deferred stages never carry ReSTIR GI (the host traces the light sample inside shade
+    // when GI is on), so the path's GI flag is false here.
+    st.gi = false;
+    st.chan = -1;
     finishPath<false, A, RESTIR>(c, st, p);
     if (k + 1 < c.p[P_SAMPLES_PER_DISPATCH] && (c.p[P_ADAPTIVE] == 0 || pixelActive<A>(c, p))) {
         PathState<false> nx = generatePathFor<false>(c, p % c.p[P_WIDTH], p / c.p[P_WIDTH], c.p[P_SAMPLE] + k + 1);

@@ -128,56 +128,6 @@ __device__ __forceinline__ float byte_f(uint32_t lo, uint32_t hi, int i)
 }
 
 
-// The byte as the float bits of 2^23 + byte (one byte permute); minus 2^23 it is the byte exactly.
-__device__ __forceinline__ float byte_biased(uint32_t lo, uint32_t hi, int i)
-{
-    uint32_t w = i < 4 ? lo : hi;
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u + (uint32_t)(i & 3)));
-}
-
-// Packed pairs of f32 (sm_100 and later): each half is the IEEE single-precision operation of its
-// own, so results are those of the scalar forms.
-__device__ __forceinline__ unsigned long long f2_pack(float lo, float hi)
-{
-    unsigned long long r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ void f2_unpack(unsigned long long v, float& lo, float& hi)
-{
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b)
-{
-    unsigned long long d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b, unsigned long long c)
-{
-    unsigned long long d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-// Three-input max / min (sm_100 and later): the result of fmaxf(fmaxf(a, b), c) (NaN inputs are
-// ignored in both, and no rounding happens).
-__device__ __forceinline__ float max3f(float a, float b, float c)
-{
-    float d;
-    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
-    return d;
-}
-__device__ __forceinline__ float min3f(float a, float b, float c)
-{
-    float d;
-    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
-    return d;
-}
-
-#ifndef VG_NODE_PAIRED
-#define VG_NODE_PAIRED 1
-#endif
-
 // Child-box tests of one BVH8 node (words w0..w4, bvh8.h) for ray r with the closest hit so far at
 // best_t: the hit internal children as bits (slot XOR octant, the visiting order) and the triangles
 // of the hit leaf slots as bits from the node's triangle base.
@@ -186,9 +136,9 @@ __device__ __forceinline__ float min3f(float a, float b, float c)
 // S = 2^e / d, one FMA per plane. The plane p + q 2^e is exact; A and S carry at most a few
 // roundings, so every t is moved outwards by err = 2^-21 (|A| + 255 |S|), a bound on that error:
 // the test never rejects a box the ray enters, and the hits stay those of brute force.
-// With VG_NODE_PAIRED each axis's near and far planes go through one packed f32x2 add (the byte
-// bias) and one packed FMA, and the slab maxima / minima are three-input: the same values from
-// fewer instructions.
+// (Tried: each axis's near and far planes through one packed f32x2 add and FMA, with three-input
+// max / min for the slab bounds. Same values, 0.408 against 0.407 ms per extend launch on the
+// 1M-triangle workload: the traversal is not limited by these instructions' count.)
 __device__ __forceinline__ void node_test(const TRay& r, uint4 w0, uint4 w2, uint4 w3, uint4 w4, uint32_t imask,
                                           uint32_t meta_lo, uint32_t meta_hi, float best_t, uint32_t& inner_hits,
                                           uint32_t& tri_bits)
@@ -215,30 +165,16 @@ __device__ __forceinline__ void node_test(const TRay& r, uint4 w0, uint4 w2, uin
     float anx = ax - ex, afx = ax + ex, any_ = ay - ey, afy = ay + ey, anz = az - ez, afz = az + ez;
     inner_hits = 0;
     tri_bits = 0;
-#if VG_NODE_PAIRED
-    const unsigned long long bias = f2_pack(-8388608.0f, -8388608.0f);
-    const unsigned long long SX = f2_pack(sx, sx), SY = f2_pack(sy, sy), SZ = f2_pack(sz, sz);
-    const unsigned long long AX = f2_pack(anx, afx), AY = f2_pack(any_, afy), AZ = f2_pack(anz, afz);
-#endif
 #pragma unroll
     for (int i = 0; i < 8; i++) {
-        float tnx, tny, tnz, tfx, tfy, tfz;
-#if VG_NODE_PAIRED
-        f2_unpack(f2_fma(f2_add(f2_pack(byte_biased(nxl, nxh, i), byte_biased(fxl, fxh, i)), bias), SX, AX), tnx, tfx);
-        f2_unpack(f2_fma(f2_add(f2_pack(byte_biased(nyl, nyh, i), byte_biased(fyl, fyh, i)), bias), SY, AY), tny, tfy);
-        f2_unpack(f2_fma(f2_add(f2_pack(byte_biased(nzl, nzh, i), byte_biased(fzl, fzh, i)), bias), SZ, AZ), tnz, tfz);
-        float tn = fmaxf(max3f(tnx, tny, tnz), 0.0f);
-        float tf = fminf(min3f(tfx, tfy, tfz), best_t);
-#else
-        tnx = fmaf(byte_f(nxl, nxh, i), sx, anx);
-        tny = fmaf(byte_f(nyl, nyh, i), sy, any_);
-        tnz = fmaf(byte_f(nzl, nzh, i), sz, anz);
-        tfx = fmaf(byte_f(fxl, fxh, i), sx, afx);
-        tfy = fmaf(byte_f(fyl, fyh, i), sy, afy);
-        tfz = fmaf(byte_f(fzl, fzh, i), sz, afz);
+        float tnx = fmaf(byte_f(nxl, nxh, i), sx, anx);
+        float tny = fmaf(byte_f(nyl, nyh, i), sy, any_);
+        float tnz = fmaf(byte_f(nzl, nzh, i), sz, anz);
+        float tfx = fmaf(byte_f(fxl, fxh, i), sx, afx);
+        float tfy = fmaf(byte_f(fyl, fyh, i), sy, afy);
+        float tfz = fmaf(byte_f(fzl, fzh, i), sz, afz);
         float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
         float tf = fminf(fminf(tfx, tfy), fminf(tfz, best_t));
-#endif
         if (tn <= tf) {
             if ((imask >> i) & 1u) {
                 inner_hits |= 1u << (i ^ r.oct);
