@@ -64,6 +64,12 @@ def parse():
     ap.add_argument("--profile-mlp", action="store_true",
                     help="profiling helper: the cache's kernels on 2^20 synthetic records, one untimed and one "
                          "timed launch of each (encode, inference, training pass, scatter); prints their times")
+    ap.add_argument("--profile-batch", action="store_true",
+                    help="profiling helper: one small batch (16 requests of 128-256 px square, 4-16 spp, plain and "
+                         "cached, scenes of the 1M-triangle kind), rendered twice through vg_batch_render")
+    ap.add_argument("--profile-restir", action="store_true",
+                    help="profiling helper: the many-light scene with ReSTIR DI (32 candidates) at 480x270 on the "
+                         "streaming wavefront, four frames of one sample")
     ap.add_argument("--width", type=int, default=WIDTH, help="smaller frames are for profiling runs only")
     ap.add_argument("--height", type=int, default=HEIGHT)
     a = ap.parse_args()
@@ -698,6 +704,43 @@ def run_cuda(args):
     r.set_accum_precision(64)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     total = args.warmup + args.steps
+
+    if args.profile_batch:
+        from verion_gb300 import pack, scenes
+        from verion_gb300.backend import BatchRequest, Cache
+
+        pb = pack.pack(scenes.many_spheres(spheres=16, sphere_n=21, grid=160))
+        rb, rcb = Renderer(ctx, pb), Renderer(ctx, pb)
+        for x in (rb, rcb):
+            x.set_max_depth(DEPTH)
+            x.set_accum_precision(32)
+        cb = Cache(ctx, bounds=rcb.bounds(), log2_entries=17)
+        rcb.set_cache(cb, spread=0.01)
+        rng = np.random.default_rng(7)
+        for _ in range(2):
+            reqs = []
+            for i in range(16):
+                side, spp = int(rng.integers(128, 257)), int(rng.integers(4, 17))
+                rr = rcb if i % 2 else rb
+                reqs.append(BatchRequest(rr, rr.new_accumulation(side, side), spp, cb if i % 2 else None))
+            out = ctx.batch_render(reqs)
+        print(json.dumps({"batch_total_s": out.total_seconds}), flush=True)
+        return
+
+    if args.profile_restir:
+        from verion_gb300 import pack, scenes
+        from verion_gb300.readback import Restir
+
+        pr = pack.pack(scenes.many_lights())
+        rr = Renderer(ctx, pr)
+        rr.set_integrator(Integrator.WAVEFRONT)
+        rr.set_accum_precision(32)
+        rr.set_restir(Restir(di=True, gi=False, candidates=32, history=20))
+        acc_r = rr.new_accumulation(480, 270)
+        for _ in range(4):
+            rr.accumulate(acc_r, 1)
+        print(json.dumps({"restir_ms_per_frame": 1e3 * acc_r.gpu_seconds() / 4}), flush=True)
+        return
 
     if args.profile_mlp:
         print(json.dumps(mlp_kernel_seconds(ctx, 1 << 20, reps=1)), flush=True)
