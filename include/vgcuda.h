@@ -218,6 +218,11 @@ int vg_set_dynamic_fetch(VgRenderer* r, int on);
  * shared-memory reductions cost more than the idle lanes they save). Same results either way. No
  * reference counterpart: the reference's hardware ray queries have no such choice. */
 int vg_set_coop_triangles(VgRenderer* r, int on);
+/* Streaming mode with deferred shadows: between the extend and shade stages each wave's slots are
+ * regrouped by shading class (missed ray, diffuse, conductor, dielectric) so that the shade stage's
+ * warps mostly run one BSDF's code (default on), or shaded in queue order (off). Same sums either
+ * way. No reference counterpart. */
+int vg_set_material_sort(VgRenderer* r, int on);
 /* Streaming mode with dynamic fetch: a warp of the extend stage takes new rays once at least
  * `refill` of its 32 lanes are idle (1-32, default 8) and visits at most `steps` nodes per lane
  * between refills (1-64, default 4); shadow_refill and shadow_steps set the same for the shadow
@@ -251,6 +256,7 @@ typedef struct VgTuneResult {
     int extend_blocks_per_sm;
     int coop_triangles;                /* vg_set_coop_triangles */
     uint32_t fetch_refill, fetch_steps; /* vg_set_traversal_fetch, extend stage */
+    int material_sort;                  /* vg_set_material_sort */
 } VgTuneResult;
 int vg_autotune(VgRenderer* r, const VgPacked* packed, uint32_t width, uint32_t height, uint32_t samples,
                 VgTuneResult* out);

@@ -373,6 +373,30 @@ def test_transparent_background_bit_exact(gpu_ctx):
     assert_same(acc.sums(), ref.sums, "transparent background sums")
 
 
+@pytest.mark.parametrize("restir", [None, Restir(di=True, gi=False, candidates=8, history=8)])
+def test_material_sorted_shading_matches_the_oracle(gpu_ctx, restir):
+    # Deferred shade stage with the wave's slots regrouped by shading class (missed, diffuse,
+    # conductor, dielectric) and in queue order: the same sums as the oracle, waves only (tail off).
+    s = scenes.many_spheres(hdri=(256, 128))
+    p = pack.pack(s)
+    out = {}
+    for sort in (True, False):
+        r = Renderer(gpu_ctx, p)
+        r.set_accum_precision(32)
+        r.set_integrator(Integrator.WAVEFRONT)
+        r.set_max_depth(16)
+        r.set_restir(restir)
+        r.set_stream_tail(0)
+        r.set_material_sort(sort)
+        acc = r.new_accumulation(64, 36)
+        for n in (2, 3):
+            r.accumulate(acc, n)
+        out[sort] = acc.sums()
+    ref = oracle_render(p, 64, 36, 5, depth=16, restir=restir)
+    assert_same(out[True], ref.sums, "material-sorted shading")
+    assert_same(out[False], ref.sums, "queue-order shading")
+
+
 def test_coop_leaf_testing_keeps_hits_and_counters(gpu_ctx):
     # Warp-cooperative leaf testing against each lane testing its own triangles: the same sums,
     # the same nodes visited and triangles tested (the walk's order is unchanged), the same number

@@ -63,6 +63,7 @@ def test_autotune_keeps_the_sums(gpu_ctx):
     assert t["graph_waves"] in (0, 8) and t["bvh_traversal_cost"] in (0.25, 0.5, 1.0, 2.0)
     assert t["extend_blocks_per_sm"] >= 1
     assert t["coop_triangles"] in (0, 1) and t["fetch_refill"] in (4, 8, 16) and t["fetch_steps"] in (2, 4, 8)
+    assert t["material_sort"] in (0, 1)
     fresh = wave_renderer(gpu_ctx, p)
     assert np.array_equal(render(r, 80, 45, 3), render(fresh, 80, 45, 3))
 

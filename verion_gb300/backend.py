@@ -112,7 +112,8 @@ class _TuneResult(C.Structure):
     _fields_ = [("dynamic_fetch", C.c_int), ("deferred_shadows", C.c_int), ("stream_tail", C.c_uint32),
                 ("graph_waves", C.c_uint32), ("bvh_traversal_cost", C.c_float), ("mpaths_before", C.c_double),
                 ("mpaths_after", C.c_double), ("trials", C.c_uint32), ("extend_blocks_per_sm", C.c_int),
-                ("coop_triangles", C.c_int), ("fetch_refill", C.c_uint32), ("fetch_steps", C.c_uint32)]
+                ("coop_triangles", C.c_int), ("fetch_refill", C.c_uint32), ("fetch_steps", C.c_uint32),
+                ("material_sort", C.c_int)]
 
 
 class _BatchRequest(C.Structure):
@@ -205,6 +206,7 @@ def lib() -> C.CDLL:
             "vg_set_deferred_shadows": (i32, [vp, i32]),
             "vg_set_dynamic_fetch": (i32, [vp, i32]),
             "vg_set_coop_triangles": (i32, [vp, i32]),
+            "vg_set_material_sort": (i32, [vp, i32]),
             "vg_set_traversal_fetch": (i32, [vp, u32, u32, u32, u32]),
             "vg_set_wavefront_graph": (i32, [vp, u32]),
             "vg_set_bvh_traversal_cost": (i32, [vp, C.POINTER(_Packed), C.c_float]),
@@ -624,6 +626,10 @@ class Renderer:
 
     def set_dynamic_fetch(self, on: bool) -> None:
         _check(lib().vg_set_dynamic_fetch(self._h, int(on)))
+
+    def set_material_sort(self, on: bool) -> None:
+        """Streaming wavefront: shade each wave's slots class by class (same sums)."""
+        _check(lib().vg_set_material_sort(self._h, int(on)))
 
     def set_coop_triangles(self, on: bool) -> None:
         """Warp-cooperative leaf testing in the streaming traversal stages (same results)."""

@@ -74,6 +74,7 @@ struct Ctx {
 namespace vgk {
 
 constexpr uint32_t BASE_PLANES = 4;  // 16-byte state planes per path
+constexpr uint32_t SHADE_CLASSES = 4; // material-sorted shading: missed, diffuse, conductor, dielectric
 constexpr uint32_t SPLIT_PLANES = 5; // more planes with the lighting split
 
 // Wavefront buffers of one accumulation.
@@ -90,6 +91,10 @@ struct Wave {
     uint32_t depth;    // max depth
     uint32_t refill, steps;               // dynamic fetch of the extend stage: idle lanes per refill, visits between refills
     uint32_t shadow_refill, shadow_steps; // the same for the shadow stage
+    // Material-sorted shading (streaming, deferred shadows): the wave's slots by shading class,
+    // class k in squeue[k * n ...], counts scount[parity * 4 + k] (null when off).
+    uint32_t* squeue;
+    uint32_t* scount;
 };
 
 // Radiance-cache frames on the streaming wavefront: the path spread (a0, a) of every slot,

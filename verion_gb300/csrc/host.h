@@ -211,6 +211,7 @@ struct VgRenderer {
     bool defer_shadows = true; // streaming: shadow rays of the light sample in their own stage
     bool dynamic_fetch = true; // streaming: traversal stages refill idle lanes from the queue
     bool coop_tris = false;    // streaming, dynamic fetch: warp-cooperative leaf testing (measured slower)
+    bool material_sort = true; // streaming, deferred shadows: shade the wave's slots class by class
     uint32_t fetch_refill = 8, fetch_steps = 4;               // dynamic fetch, extend stage
     uint32_t shadow_fetch_refill = 8, shadow_fetch_steps = 4; // dynamic fetch, shadow stage
     uint32_t graph_waves = 0;  // streaming: waves per captured CUDA graph (0: launched one by one)
@@ -247,7 +248,7 @@ struct VgAccum {
     Restir restir;               // captured at the first sample
     DevBuf re_g[2], re_n[2], re_x[2], re_m[2];
     DevBuf re_gx[2], re_gn[2], re_gl[2], re_s[7]; // ReSTIR GI planes
-    DevBuf state, hits, queue[2], counts, fetch, tstats, meta, sreq;
+    DevBuf state, hits, queue[2], counts, fetch, tstats, meta, sreq, squeue, scount;
     uint32_t* host_counts = nullptr; // pinned ring of wave output counts (streaming wavefront)
     uint32_t last_waves = 0;
     std::vector<uint32_t> wave_live; // last streaming accumulate: live slots after each wave
@@ -433,6 +434,8 @@ vgk::Wave wave_of(const VgRenderer* r, const VgAccum* acc)
     w.steps = r->fetch_steps;
     w.shadow_refill = r->shadow_fetch_refill;
     w.shadow_steps = r->shadow_fetch_steps;
+    w.squeue = (uint32_t*)acc->squeue.p;
+    w.scount = (uint32_t*)acc->scount.p;
     return w;
 }
 

@@ -190,13 +190,23 @@ cudaError_t launch_stream_tail(Variant v, uint32_t max_slots, cudaStream_t s, co
 
 namespace vgx {
 
-cudaError_t launch_stream_shade_deferred(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
-                                         uint32_t wave)
+cudaError_t launch_stream_shade_deferred(bool f64, bool sorted, int blocks, cudaStream_t s, const vgd::Ctx& c,
+                                         const vgk::Wave& w, uint32_t wave)
 {
-    if (f64)
+    if (f64 && sorted)
+        vgk::wf_stream_shade_deferred<double, false, false, true><<<blocks, 128, 0, s>>>(c, w, wave, vgk::CacheWave{});
+    else if (f64)
         vgk::wf_stream_shade_deferred<double><<<blocks, 128, 0, s>>>(c, w, wave, vgk::CacheWave{});
+    else if (sorted)
+        vgk::wf_stream_shade_deferred<float, false, false, true><<<blocks, 128, 0, s>>>(c, w, wave, vgk::CacheWave{});
     else
         vgk::wf_stream_shade_deferred<float><<<blocks, 128, 0, s>>>(c, w, wave, vgk::CacheWave{});
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_classify(int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w, uint32_t wave)
+{
+    vgk::wf_stream_classify<<<blocks, 256, 0, s>>>(c, w, wave);
     return cudaGetLastError();
 }
 

@@ -58,11 +58,15 @@ cudaError_t launch_stream_tail_restir(Variant v, uint32_t max_slots, cudaStream_
     return cudaGetLastError();
 }
 
-cudaError_t launch_stream_shade_deferred_restir(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c,
+cudaError_t launch_stream_shade_deferred_restir(bool f64, bool sorted, int blocks, cudaStream_t s, const vgd::Ctx& c,
                                                 const vgk::Wave& w, uint32_t wave)
 {
-    if (f64)
+    if (f64 && sorted)
+        vgk::wf_stream_shade_deferred<double, false, true, true><<<blocks, 128, 0, s>>>(c, w, wave, vgk::CacheWave{});
+    else if (f64)
         vgk::wf_stream_shade_deferred<double, false, true><<<blocks, 128, 0, s>>>(c, w, wave, vgk::CacheWave{});
+    else if (sorted)
+        vgk::wf_stream_shade_deferred<float, false, true, true><<<blocks, 128, 0, s>>>(c, w, wave, vgk::CacheWave{});
     else
         vgk::wf_stream_shade_deferred<float, false, true><<<blocks, 128, 0, s>>>(c, w, wave, vgk::CacheWave{});
     return cudaGetLastError();

@@ -463,6 +463,42 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade(cons
     }
 }
 
+// Shading classes of material-sorted shading (SHADE_CLASSES, ctx.h): a missed ray (environment or
+// sky), a diffuse surface, a conductor, a dielectric. Only the order in which slots are shaded
+// changes (each slot adds to its own pixel), so the sums stay bit-identical.
+
+static __device__ __forceinline__ uint32_t shadeClass(const Ctx& c, uint4 hr)
+{
+    if (hr.x == 0)
+        return 0;
+    uint32_t mi = uget(c.s.instances, hr.y * 16 + 2) * 24;
+    if (fget(c.s.materials, mi + 8) > 0.0f)
+        return 3;
+    return fget(c.s.materials, mi + 6) >= 0.5f ? 2u : 1u;
+}
+
+// Between extend and shade: every slot of the wave's queue goes to the queue of its shading class
+// (one atomic per class present in a warp), so the deferred shade stage's warps mostly run one
+// BSDF's code. Clears the other parity's class counts for the next wave (the shade stage of the
+// previous wave, their last reader, has finished).
+static __global__ void __launch_bounds__(256) wf_stream_classify(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
+{
+    uint32_t in = wave & 1u, out = in ^ 1u;
+    if (blockIdx.x == 0 && threadIdx.x < SHADE_CLASSES)
+        w.scount[out * SHADE_CLASSES + threadIdx.x] = 0;
+    uint32_t count = w.counts[in];
+    const uint32_t* qin = w.queue[in];
+    uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += stride) {
+        uint32_t i = base + threadIdx.x;
+        bool have = i < count;
+        uint32_t p = have ? qin[i] : 0u;
+        uint32_t k = have ? shadeClass(c, w.hits[p]) : SHADE_CLASSES;
+        for (uint32_t cls = 0; cls < SHADE_CLASSES; cls++)
+            warp_append(&w.scount[in * SHADE_CLASSES + cls], w.squeue + (size_t)cls * w.n, k == cls, p);
+    }
+}
+
 // Streaming wave in three stages (lighting split off): extend, then shade without any traversal,
 // then shadow. Shade leaves its emitter / environment light sample as a request per slot
 // (w.sreq planes: origin + tmax, direction + flags, contribution); the shadow stage traces it,
@@ -470,7 +506,8 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade(cons
 // flags: bit 0 a request is present, bit 1 the path goes on to the next depth.
 // With CACHE a path also ends where its spread passes the cache threshold (shadePath's cache
 // hook); it then leaves a query record (one atomic per warp) and finishes like any other.
-template <typename A, bool CACHE = false, bool RESTIR = false>
+// With SORTED the wave's slots are taken class by class from the classify stage's queues.
+template <typename A, bool CACHE = false, bool RESTIR = false, bool SORTED = false>
 __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade_deferred(const __grid_constant__ Ctx c,
                                                                                     Wave w, uint32_t wave,
                                                                                     CacheWave q)
@@ -479,6 +516,10 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade_defe
     uint32_t count = w.counts[in];
     const uint32_t* qin = w.queue[in];
     uint32_t n = w.n;
+    uint32_t seg[SHADE_CLASSES + 1] = {0, 0, 0, 0, 0};
+    if (SORTED)
+        for (uint32_t k = 0; k < SHADE_CLASSES; k++)
+            seg[k + 1] = seg[k] + w.scount[in * SHADE_CLASSES + k];
     for (;;) {
         uint32_t base = warp_fetch(&w.fetch[2 + in]);
         if (base >= count)
@@ -488,7 +529,12 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade_defe
         uint32_t p = 0, kq = 0;
         CacheHook hk;
         if (i < count) {
-            p = qin[i];
+            if (SORTED) {
+                uint32_t k = i >= seg[1] ? (i >= seg[2] ? (i >= seg[3] ? 3u : 2u) : 1u) : 0u;
+                p = w.squeue[(size_t)k * n + (i - seg[k])];
+            } else {
+                p = qin[i];
+            }
             uint32_t meta = w.meta[p];
             uint32_t depth = meta & 0xffu;
             kq = meta >> 8;

@@ -39,8 +39,10 @@ cudaError_t launch_stream_cache_shade(bool f64, int blocks, cudaStream_t s, cons
 int stream_cache_shade_blocks_per_sm(bool f64);
 cudaError_t launch_stream_cache_tail(bool f64, uint32_t max_slots, cudaStream_t s, const vgd::Ctx& c,
                                      const vgk::Wave& w, uint32_t wave, const vgk::CacheWave& q);
-cudaError_t launch_stream_shade_deferred(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
-                                         uint32_t wave);
+// With `sorted` the shade stage takes the wave's slots class by class (launch_stream_classify first).
+cudaError_t launch_stream_shade_deferred(bool f64, bool sorted, int blocks, cudaStream_t s, const vgd::Ctx& c,
+                                         const vgk::Wave& w, uint32_t wave);
+cudaError_t launch_stream_classify(int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w, uint32_t wave);
 cudaError_t launch_stream_shadow(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
                                  uint32_t wave);
 int stream_deferred_blocks_per_sm(bool f64, int* shadow);
@@ -60,7 +62,7 @@ cudaError_t launch_stream_shade_restir(Variant v, int blocks, cudaStream_t s, co
 int stream_shade_restir_blocks_per_sm(Variant v);
 cudaError_t launch_stream_tail_restir(Variant v, uint32_t max_slots, cudaStream_t s, const vgd::Ctx& c,
                                       const vgk::Wave& w, uint32_t wave);
-cudaError_t launch_stream_shade_deferred_restir(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c,
+cudaError_t launch_stream_shade_deferred_restir(bool f64, bool sorted, int blocks, cudaStream_t s, const vgd::Ctx& c,
                                                 const vgk::Wave& w, uint32_t wave);
 cudaError_t launch_stream_shadow_restir(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
                                         uint32_t wave);

@@ -200,11 +200,17 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
         csb = blocks_for(r, r->cache_shade_blocks[v.f64 ? 1 : 0]);
     }
     int shb = blocks_for(r, r->shadow_blocks[v.f64 ? 1 : 0]);
+    // Material-sorted shading: deferred plain (or ReSTIR) waves, not the cache's shade stage.
+    bool sorted = deferred && !q && r->material_sort && acc->squeue.p != nullptr && acc->scount.p != nullptr &&
+                  acc->squeue.bytes >= (size_t)w.n * 4 * vgk::SHADE_CLASSES;
+    int clb = r->ctx->sms * 4;
     acc->wave_stages = deferred ? 3 : 2;
     c.p[P_SAMPLE] = sample0;
     c.p[P_SAMPLES_PER_DISPATCH] = samples;
     VG_CHECK(cudaMemsetAsync(acc->counts.p, 0, 2 * 4, s), "counters");
     VG_CHECK(cudaMemsetAsync(acc->fetch.p, 0, 4 * 4, s), "counters");
+    if (sorted)
+        VG_CHECK(cudaMemsetAsync(acc->scount.p, 0, 2 * vgk::SHADE_CLASSES * 4, s), "counters");
     VG_CHECK((q ? vgx::launch_stream_cache_start(v.f64, s, c, w, *q) : vgx::launch_stream_start(v, s, c, w)), "stream start launch");
     acc->launches++;
     // Waves until no slot is live. The host reads each wave's output count LAG waves later,
@@ -226,8 +232,10 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
         for (uint32_t i = 0; i < K && ce == cudaSuccess; i++) {
             ce = r->dynamic_fetch ? vgx::launch_stream_extend_dyn(r->traversal_stats, r->coop_tris, eb, s, c, w, i)
                                   : vgx::launch_stream_extend(r->traversal_stats, eb, s, c, w, i);
+            if (ce == cudaSuccess && sorted)
+                ce = vgx::launch_stream_classify(clb, s, c, w, i);
             if (ce == cudaSuccess && deferred) {
-                ce = (q ? vgx::launch_stream_cache_shade(v.f64, csb, s, c, w, i, *q) : (v.restir ? vgx::launch_stream_shade_deferred_restir : vgx::launch_stream_shade_deferred)(v.f64, dsb, s, c, w, i));
+                ce = (q ? vgx::launch_stream_cache_shade(v.f64, csb, s, c, w, i, *q) : (v.restir ? vgx::launch_stream_shade_deferred_restir : vgx::launch_stream_shade_deferred)(v.f64, sorted, dsb, s, c, w, i));
                 if (ce == cudaSuccess && r->dynamic_fetch && r->ds.shadow_any) {
                     ce = vgx::launch_stream_shadow_trace(r->traversal_stats, r->coop_tris, shb, s, c, w, i);
                     if (ce == cudaSuccess)
@@ -307,8 +315,12 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
                      "extend launch");
         if (timed)
             VG_CHECK(cudaEventRecord(m, s), "event");
+        if (sorted) {
+            VG_CHECK(vgx::launch_stream_classify(clb, s, c, w, (uint32_t)wave), "classify launch");
+            acc->launches++;
+        }
         if (deferred) {
-            VG_CHECK((q ? vgx::launch_stream_cache_shade(v.f64, csb, s, c, w, (uint32_t)wave, *q) : (v.restir ? vgx::launch_stream_shade_deferred_restir : vgx::launch_stream_shade_deferred)(v.f64, dsb, s, c, w, (uint32_t)wave)), "shade launch");
+            VG_CHECK((q ? vgx::launch_stream_cache_shade(v.f64, csb, s, c, w, (uint32_t)wave, *q) : (v.restir ? vgx::launch_stream_shade_deferred_restir : vgx::launch_stream_shade_deferred)(v.f64, sorted, dsb, s, c, w, (uint32_t)wave)), "shade launch");
             cudaEvent_t qe = nullptr;
             if (timed) {
                 qe = pool.get();
@@ -809,6 +821,14 @@ int vg_set_dynamic_fetch(VgRenderer* r, int on)
     return VG_OK;
 }
 
+int vg_set_material_sort(VgRenderer* r, int on)
+{
+    if (!r)
+        return fail(VG_ERR_INVALID, "null renderer");
+    r->material_sort = on != 0;
+    return VG_OK;
+}
+
 int vg_set_coop_triangles(VgRenderer* r, int on)
 {
     if (!r)
@@ -1014,7 +1034,9 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
             (st = alloc(acc->fetch, 2 * (max_depth_alloc + 1) * 4, s, true)) != VG_OK ||
             (st = alloc(acc->tstats, 8 * 8, s, true)) != VG_OK ||
             (st = alloc(acc->meta, px * 4, s, false)) != VG_OK ||
-            (st = alloc(acc->sreq, acc->lighting ? 16 : px * 3 * 16, s, false)) != VG_OK)
+            (st = alloc(acc->sreq, acc->lighting ? 16 : px * 3 * 16, s, false)) != VG_OK ||
+            (st = alloc(acc->squeue, acc->lighting ? 16 : px * 4 * vgk::SHADE_CLASSES, s, false)) != VG_OK ||
+            (st = alloc(acc->scount, 2 * vgk::SHADE_CLASSES * 4, s, true)) != VG_OK)
             return st;
         if (!acc->host_counts && cudaHostAlloc((void**)&acc->host_counts, 64 * 4, cudaHostAllocDefault) != cudaSuccess) {
             acc->host_counts = nullptr;
@@ -1389,6 +1411,13 @@ int vg_autotune(VgRenderer* r, const VgPacked* pk, uint32_t width, uint32_t heig
             return o;
         },
         std::vector<bool>{!r->coop_tris});
+    try_setting(
+        [&](bool v, bool) {
+            bool o = r->material_sort;
+            r->material_sort = v;
+            return o;
+        },
+        std::vector<bool>{!r->material_sort});
     std::vector<uint32_t> refills, steps;
     for (uint32_t v : {4u, 8u, 16u})
         if (v != r->fetch_refill)
@@ -1448,6 +1477,7 @@ int vg_autotune(VgRenderer* r, const VgPacked* pk, uint32_t width, uint32_t heig
     out->bvh_traversal_cost = r->bvh_traversal_cost;
     out->extend_blocks_per_sm = r->extend_blocks;
     out->coop_triangles = r->coop_tris;
+    out->material_sort = r->material_sort;
     out->fetch_refill = r->fetch_refill;
     out->fetch_steps = r->fetch_steps;
     out->mpaths_after = best;
