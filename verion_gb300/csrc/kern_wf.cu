@@ -223,11 +223,15 @@ cudaError_t launch_stream_cache_start(bool f64, cudaStream_t s, const vgd::Ctx& 
     return cudaGetLastError();
 }
 
-cudaError_t launch_stream_cache_shade(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
-                                      uint32_t wave, const vgk::CacheWave& q)
+cudaError_t launch_stream_cache_shade(bool f64, bool sorted, int blocks, cudaStream_t s, const vgd::Ctx& c,
+                                      const vgk::Wave& w, uint32_t wave, const vgk::CacheWave& q)
 {
-    if (f64)
+    if (f64 && sorted)
+        vgk::wf_stream_shade_deferred<double, true, false, true><<<blocks, 128, 0, s>>>(c, w, wave, q);
+    else if (f64)
         vgk::wf_stream_shade_deferred<double, true><<<blocks, 128, 0, s>>>(c, w, wave, q);
+    else if (sorted)
+        vgk::wf_stream_shade_deferred<float, true, false, true><<<blocks, 128, 0, s>>>(c, w, wave, q);
     else
         vgk::wf_stream_shade_deferred<float, true><<<blocks, 128, 0, s>>>(c, w, wave, q);
     return cudaGetLastError();

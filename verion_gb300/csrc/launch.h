@@ -34,8 +34,8 @@ int stream_shade_blocks_per_sm(Variant v);
 // Three-stage wave (lighting split off): shade without traversal, then the shadow stage.
 cudaError_t launch_stream_cache_start(bool f64, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
                                       const vgk::CacheWave& q);
-cudaError_t launch_stream_cache_shade(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
-                                      uint32_t wave, const vgk::CacheWave& q);
+cudaError_t launch_stream_cache_shade(bool f64, bool sorted, int blocks, cudaStream_t s, const vgd::Ctx& c,
+                                      const vgk::Wave& w, uint32_t wave, const vgk::CacheWave& q);
 int stream_cache_shade_blocks_per_sm(bool f64);
 cudaError_t launch_stream_cache_tail(bool f64, uint32_t max_slots, cudaStream_t s, const vgd::Ctx& c,
                                      const vgk::Wave& w, uint32_t wave, const vgk::CacheWave& q);

@@ -200,8 +200,8 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
         csb = blocks_for(r, r->cache_shade_blocks[v.f64 ? 1 : 0]);
     }
     int shb = blocks_for(r, r->shadow_blocks[v.f64 ? 1 : 0]);
-    // Material-sorted shading: deferred plain (or ReSTIR) waves, not the cache's shade stage.
-    bool sorted = deferred && !q && r->material_sort && acc->squeue.p != nullptr && acc->scount.p != nullptr &&
+    // Material-sorted shading of the deferred shade stage (plain, ReSTIR and cache waves).
+    bool sorted = deferred && r->material_sort && acc->squeue.p != nullptr && acc->scount.p != nullptr &&
                   acc->squeue.bytes >= (size_t)w.n * 4 * vgk::SHADE_CLASSES;
     int clb = r->ctx->sms * 4;
     acc->wave_stages = deferred ? 3 : 2;
@@ -235,7 +235,7 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
             if (ce == cudaSuccess && sorted)
                 ce = vgx::launch_stream_classify(clb, s, c, w, i);
             if (ce == cudaSuccess && deferred) {
-                ce = (q ? vgx::launch_stream_cache_shade(v.f64, csb, s, c, w, i, *q) : (v.restir ? vgx::launch_stream_shade_deferred_restir : vgx::launch_stream_shade_deferred)(v.f64, sorted, dsb, s, c, w, i));
+                ce = (q ? vgx::launch_stream_cache_shade(v.f64, sorted, csb, s, c, w, i, *q) : (v.restir ? vgx::launch_stream_shade_deferred_restir : vgx::launch_stream_shade_deferred)(v.f64, sorted, dsb, s, c, w, i));
                 if (ce == cudaSuccess && r->dynamic_fetch && r->ds.shadow_any) {
                     ce = vgx::launch_stream_shadow_trace(r->traversal_stats, r->coop_tris, shb, s, c, w, i);
                     if (ce == cudaSuccess)
@@ -320,7 +320,7 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
             acc->launches++;
         }
         if (deferred) {
-            VG_CHECK((q ? vgx::launch_stream_cache_shade(v.f64, csb, s, c, w, (uint32_t)wave, *q) : (v.restir ? vgx::launch_stream_shade_deferred_restir : vgx::launch_stream_shade_deferred)(v.f64, sorted, dsb, s, c, w, (uint32_t)wave)), "shade launch");
+            VG_CHECK((q ? vgx::launch_stream_cache_shade(v.f64, sorted, csb, s, c, w, (uint32_t)wave, *q) : (v.restir ? vgx::launch_stream_shade_deferred_restir : vgx::launch_stream_shade_deferred)(v.f64, sorted, dsb, s, c, w, (uint32_t)wave)), "shade launch");
             cudaEvent_t qe = nullptr;
             if (timed) {
                 qe = pool.get();
