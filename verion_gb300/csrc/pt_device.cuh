@@ -619,8 +619,20 @@ __device__ PathState<LIGHT> generatePathFor(const Ctx& c, uint32_t px, uint32_t 
     return s;
 }
 
+// Out-of-line code for the kernels that run whole paths per thread (megakernel, streaming tail,
+// batch): with VG_TRACE_OUTLINE the closest-hit traversal is one called function instead of a
+// copy inlined into each path loop (a smaller instruction footprint for divergent warps).
+#ifndef VG_TRACE_OUTLINE
+#define VG_TRACE_OUTLINE 0
+#endif
+#if VG_TRACE_OUTLINE
+#define VG_TRACE_INLINE __noinline__
+#else
+#define VG_TRACE_INLINE __forceinline__
+#endif
+
 // pt_core.slang:684-700
-static __device__ __forceinline__ Hit traceClosest(const Ctx& c, V3 org, V3 dir)
+static __device__ VG_TRACE_INLINE Hit traceClosest(const Ctx& c, V3 org, V3 dir)
 {
     vgt::TRay r = vgt::make_ray(org, dir);
     vgt::TraceHit q = vgt::trace_bvh<false>(c.s.nodes, c.s.tris, r, 1.0e30f, c.err);
@@ -984,8 +996,17 @@ __device__ __forceinline__ void cacheQueryRecord(float* d, const CacheHook& hk, 
     d[19] = __uint_as_float(pixel);
 }
 
+// With VG_SHADE_OUTLINE shadePath is always a called function (one copy per instantiation).
+#ifndef VG_SHADE_OUTLINE
+#define VG_SHADE_OUTLINE 0
+#endif
+#if VG_SHADE_OUTLINE
+#define VG_SHADE_INLINE __noinline__
+#else
+#define VG_SHADE_INLINE
+#endif
 template <bool LIGHT, bool RESTIR, bool DEFER = false, bool CACHE = false>
-__device__ bool shadePath(const Ctx& c, PathState<LIGHT>& st, Hit hq, uint32_t depth, uint32_t pixel,
+__device__ VG_SHADE_INLINE bool shadePath(const Ctx& c, PathState<LIGHT>& st, Hit hq, uint32_t depth, uint32_t pixel,
                           ShadowReq* req = nullptr, CacheHook* hk = nullptr)
 {
     static_assert(!(DEFER && LIGHT), "deferred shadow rays need the lighting split off");
