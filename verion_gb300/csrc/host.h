@@ -207,6 +207,7 @@ struct VgRenderer {
     int shade_blocks[8] = {};
     int stream_shade_blocks[8] = {};
     int deferred_blocks[2] = {};
+    int deferred_restir_blocks[2] = {};
     int shadow_blocks[2] = {};
     bool defer_shadows = true; // streaming: shadow rays of the light sample in their own stage
     bool dynamic_fetch = true; // streaming: traversal stages refill idle lanes from the queue

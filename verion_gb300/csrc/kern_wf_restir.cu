@@ -92,4 +92,14 @@ cudaError_t launch_stream_finish_restir(bool f64, int blocks, cudaStream_t s, co
     return cudaGetLastError();
 }
 
+int stream_deferred_restir_blocks_per_sm(bool f64)
+{
+    int n = 0;
+    if (f64)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, vgk::wf_stream_shade_deferred<double, false, true, true>, 128, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, vgk::wf_stream_shade_deferred<float, false, true, true>, 128, 0);
+    return n > 0 ? n : 1;
+}
+
 } // namespace vgx

@@ -22,9 +22,13 @@ using namespace vgd;
 
 constexpr uint32_t FULL = 0xffffffffu;
 
-// Minimum resident 128-thread blocks per SM requested for the shade kernels (a register cap).
+// Minimum resident 128-thread blocks per SM requested for the shade kernels (a register cap), and
+// for the deferred shade stage's ReSTIR instantiations (whose candidate loop waits on memory).
 #ifndef VG_SHADE_MIN_BLOCKS
 #define VG_SHADE_MIN_BLOCKS 4
+#endif
+#ifndef VG_RESTIR_SHADE_MIN_BLOCKS
+#define VG_RESTIR_SHADE_MIN_BLOCKS VG_SHADE_MIN_BLOCKS
 #endif
 
 // State planes (16 bytes each, plane k of path p at state[k * N + p]):
@@ -508,7 +512,7 @@ static __global__ void __launch_bounds__(256) wf_stream_classify(const __grid_co
 // hook); it then leaves a query record (one atomic per warp) and finishes like any other.
 // With SORTED the wave's slots are taken class by class from the classify stage's queues.
 template <typename A, bool CACHE = false, bool RESTIR = false, bool SORTED = false>
-__global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_shade_deferred(const __grid_constant__ Ctx c,
+__global__ void __launch_bounds__(128, RESTIR ? VG_RESTIR_SHADE_MIN_BLOCKS : VG_SHADE_MIN_BLOCKS) wf_stream_shade_deferred(const __grid_constant__ Ctx c,
                                                                                     Wave w, uint32_t wave,
                                                                                     CacheWave q)
 {

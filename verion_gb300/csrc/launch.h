@@ -64,6 +64,7 @@ cudaError_t launch_stream_tail_restir(Variant v, uint32_t max_slots, cudaStream_
                                       const vgk::Wave& w, uint32_t wave);
 cudaError_t launch_stream_shade_deferred_restir(bool f64, bool sorted, int blocks, cudaStream_t s, const vgd::Ctx& c,
                                                 const vgk::Wave& w, uint32_t wave);
+int stream_deferred_restir_blocks_per_sm(bool f64);
 cudaError_t launch_stream_shadow_restir(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
                                         uint32_t wave);
 cudaError_t launch_stream_finish_restir(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,

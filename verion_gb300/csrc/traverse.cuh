@@ -65,21 +65,12 @@ __device__ __forceinline__ TRay make_ray(V3 o, V3 d)
     return r;
 }
 
-#ifndef VG_TRI_EARLY_REJECT
-#define VG_TRI_EARLY_REJECT 1
-#endif
-
 // Watertight test. On success returns true with the distance t = T / det and the edge functions
-// (U, V, W weigh vertices 0, 1, 2; divided by det they are the barycentrics). `tfar` is the
-// distance a hit must not exceed to matter (the closest hit so far, or an any-hit ray's tmax):
-// with VG_TRI_EARLY_REJECT the division is skipped where its result could only be rejected, so
-// the test returns false exactly when the callers would have rejected the hit anyway:
-// * T and det of different signs (or T zero): t = T / det <= 0;
-// * |T| > m (1 + 2^-20) with m = |det| tfar rounded, in the normal range: then the exact quotient
-//   exceeds tfar (1 + 2^-21) (two roundings of at most 2^-24 each), so the rounded t is above tfar
-//   by more than three of its ulps, beyond even a tie.
+// (U, V, W weigh vertices 0, 1, 2; divided by det they are the barycentrics). (Tried: a sign and
+// magnitude test ahead of the division, rejecting where the quotient could only be rejected
+// against the closest hit so far; it measured 1.5% slower per extend launch.)
 __device__ __forceinline__ bool tri_test(const TRay& r, V3 v0, V3 v1, V3 v2, float& t, float& U, float& V, float& W,
-                                         float& det, float tfar = 1.0e30f)
+                                         float& det)
 {
     V3 A = v0 - r.o;
     V3 B = v1 - r.o;
@@ -112,13 +103,6 @@ __device__ __forceinline__ bool tri_test(const TRay& r, V3 v0, V3 v1, V3 v2, flo
     float Bz = r.sz * Bkz;
     float Cz = r.sz * Ckz;
     float T = U * Az + V * Bz + W * Cz;
-#if VG_TRI_EARLY_REJECT
-    if (det > 0.0f ? T <= 0.0f : T >= 0.0f)
-        return false;
-    float m = fabsf(det) * tfar;
-    if (m >= 1.0e-30f && fabsf(T) > m * 1.00000095367431640625f)
-        return false;
-#endif
     t = T / det;
     return t > 0.0f;
 }
@@ -240,8 +224,7 @@ __device__ __forceinline__ TraceHit trace_bvh(const uint4* __restrict__ nodes, c
             float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
             float t, U, V, W, det;
             h.tests++;
-            if (tri_test(r, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), t, U, V, W, det,
-                         ANY ? tmax : best_t)) {
+            if (tri_test(r, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), t, U, V, W, det)) {
                 uint32_t gid = __float_as_uint(c.w);
                 bool take = ANY ? t < tmax : (t < best_t || (h.hit && t == best_t && gid < h.gid));
                 if (take) {
@@ -324,7 +307,7 @@ __device__ __forceinline__ bool walk_step(const uint4* __restrict__ nodes, const
         float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
         float t, U, V, W, det;
         w.h.tests++;
-        if (tri_test(r, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), t, U, V, W, det, w.tmax)) {
+        if (tri_test(r, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), t, U, V, W, det)) {
             uint32_t gid = __float_as_uint(c.w);
             bool take = ANY ? t < w.tmax : (t < w.tmax || (w.h.hit && t == w.tmax && gid < w.h.gid));
             if (take) {
@@ -507,9 +490,7 @@ __device__ __forceinline__ bool coop_tris(CoopWarp& cw, uint32_t lane, uint32_t 
             r.sy = rb.y;
             r.sz = rb.z;
             float t, U;
-            // No early far reject here: the owner's closest hit so far is not known to the pair lane.
-            if (tri_test(r, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), t, U, V, Wb, det,
-                         ANY ? rb.w : 3.0e38f)) {
+            if (tri_test(r, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), t, U, V, Wb, det)) {
                 if (ANY) {
                     if (t < rb.w)
                         cw.info[L].x = 1u;

@@ -193,6 +193,11 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
         r->deferred_blocks[v.f64 ? 1 : 0] =
             vgx::stream_deferred_blocks_per_sm(v.f64, &r->shadow_blocks[v.f64 ? 1 : 0]);
     int dsb = blocks_for(r, r->deferred_blocks[v.f64 ? 1 : 0]);
+    if (deferred && v.restir) {
+        if (r->deferred_restir_blocks[v.f64 ? 1 : 0] == 0)
+            r->deferred_restir_blocks[v.f64 ? 1 : 0] = vgx::stream_deferred_restir_blocks_per_sm(v.f64);
+        dsb = blocks_for(r, r->deferred_restir_blocks[v.f64 ? 1 : 0]);
+    }
     int csb = 0;
     if (q) {
         if (r->cache_shade_blocks[v.f64 ? 1 : 0] == 0)
