@@ -58,7 +58,7 @@ static __device__ __forceinline__ void plain_tile(const Ctx& c, uint32_t x, uint
     for (uint32_t k = 0; k < c.p[P_SAMPLES_PER_DISPATCH]; k++) {
         PathState<false> st = generatePathFor<false>(c, x, y, c.p[P_SAMPLE] + k);
         for (uint32_t depth = 0; depth < c.p[P_MAX_DEPTH]; depth++) {
-            if (!shadePath<false, false>(c, st, traceClosest(c, st.org, st.dir), depth, pixel))
+            if (!shadePathCall<false, false>(c, st, traceClosest(c, st.org, st.dir), depth, pixel))
                 break;
         }
         finishPath<false, A>(c, st, pixel);
@@ -88,7 +88,7 @@ static __device__ __forceinline__ bool cache_sample(const BatchReq& R, uint32_t 
     if (inside) {
         st = generatePathFor<false>(c, x, y, sample);
         for (uint32_t depth = 0; depth < c.p[P_MAX_DEPTH]; depth++) {
-            bool alive = shadePath<false, false, false, true>(c, st, traceClosest(c, st.org, st.dir), depth, pixel,
+            bool alive = shadePathCall<false, false, false, true>(c, st, traceClosest(c, st.org, st.dir), depth, pixel,
                                                               nullptr, &hk);
             if (hk.vertex && hk.train && nv < MAX_TRAIN_VERTICES) {
                 cacheFeatures(feat[nv], hk);

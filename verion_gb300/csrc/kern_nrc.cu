@@ -517,7 +517,7 @@ __global__ void __launch_bounds__(128) mk_cache_query(const __grid_constant__ Ct
     if (inside) {
         st = generatePathFor<false>(c, x, y, c.p[P_SAMPLE]);
         for (uint32_t depth = 0; depth < c.p[P_MAX_DEPTH]; depth++) {
-            bool alive = shadePath<false, false, false, true>(c, st, traceClosest(c, st.org, st.dir), depth, pixel,
+            bool alive = shadePathCall<false, false, false, true>(c, st, traceClosest(c, st.org, st.dir), depth, pixel,
                                                               nullptr, &hk);
             if (hk.query) {
                 query = true;
@@ -560,7 +560,7 @@ __global__ void __launch_bounds__(128) mk_cache_train(const __grid_constant__ Ct
         if (inside) {
             st = generatePathFor<false>(c, x, y, c.p[P_SAMPLE] + ks);
             for (uint32_t depth = 0; depth < c.p[P_MAX_DEPTH]; depth++) {
-                bool alive = shadePath<false, false, false, true>(c, st, traceClosest(c, st.org, st.dir), depth, pixel,
+                bool alive = shadePathCall<false, false, false, true>(c, st, traceClosest(c, st.org, st.dir), depth, pixel,
                                                                   nullptr, &hk);
                 if (hk.vertex && nv < MAX_TRAIN_VERTICES) {
                     cacheFeatures(feat[nv], hk);

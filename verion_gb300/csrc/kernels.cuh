@@ -23,12 +23,14 @@ using namespace vgd;
 constexpr uint32_t FULL = 0xffffffffu;
 
 // Minimum resident 128-thread blocks per SM requested for the shade kernels (a register cap), and
-// for the deferred shade stage's ReSTIR instantiations (whose candidate loop waits on memory).
+// for the deferred shade stage's ReSTIR instantiations, whose candidate loop waits on memory: 6
+// blocks there took the many-light ReSTIR frame from 7.89 to 7.43 ms (5 or 6 for the plain stage
+// are slower than 4).
 #ifndef VG_SHADE_MIN_BLOCKS
 #define VG_SHADE_MIN_BLOCKS 4
 #endif
 #ifndef VG_RESTIR_SHADE_MIN_BLOCKS
-#define VG_RESTIR_SHADE_MIN_BLOCKS VG_SHADE_MIN_BLOCKS
+#define VG_RESTIR_SHADE_MIN_BLOCKS 6
 #endif
 
 // State planes (16 bytes each, plane k of path p at state[k * N + p]):
@@ -186,7 +188,7 @@ __global__ void __launch_bounds__(128) mk_pathtrace(const __grid_constant__ Ctx 
             return;
         PathState<LIGHT> st = generatePathFor<LIGHT>(c, x, y, c.p[P_SAMPLE] + k);
         for (uint32_t depth = 0; depth < c.p[P_MAX_DEPTH]; depth++) {
-            if (!shadePath<LIGHT, RESTIR>(c, st, traceClosest(c, st.org, st.dir), depth, pixel))
+            if (!shadePathCall<LIGHT, RESTIR>(c, st, traceClosest(c, st.org, st.dir), depth, pixel))
                 break;
         }
         finishPath<LIGHT, A, RESTIR>(c, st, pixel);
@@ -822,7 +824,7 @@ __global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_tail(const
         hk.a = sp.y;
     }
     for (;;) {
-        if (shadePath<LIGHT, RESTIR, false, CACHE>(c, st, traceClosest(c, st.org, st.dir), depth, p, nullptr, &hk) &&
+        if (shadePathCall<LIGHT, RESTIR, false, CACHE>(c, st, traceClosest(c, st.org, st.dir), depth, p, nullptr, &hk) &&
             depth + 1 < w.depth) {
             depth++;
             continue;
