@@ -359,16 +359,22 @@ int vg_trace_closest_noalloc(VgRenderer* r, const float* rays, size_t n, uint32_
 void vg_debug_allocations(uint64_t* mallocs, uint64_t* frees);
 
 /* ---- Batched rendering (no reference counterpart) -----------------------------------------------
- * Many render requests in one persistent launch: the work items (16 x 8 pixel tiles with all of a
- * request's samples) of every request below a size threshold are laid out shortest request first
- * (or as given, or longest first) and taken by the CTAs of one kernel, so small requests finish
- * early while the GPU stays full; requests above the threshold then run one at a time on the
- * streaming wavefront, which is faster per path on large frames. A plain request's samples are exactly what vg_accumulate's megakernel adds (same sums);
- * a request with a cache ends its paths at the cache and evaluates the cache inside the same CTA
- * (tensor cores); after the launch each cache takes its renderer's training steps (vg_set_cache)
- * on the batch's training records. The sequence after the request upload is captured in a CUDA
- * graph the first time and replayed while the batch keeps the same shape (same renderers,
- * accumulations, sample counts and caches in the same order). */
+ * Many render requests of uneven size, scene and sample count in shared launches, each captured in
+ * a CUDA graph the first time and replayed while the batch keeps the same shape (same renderers,
+ * accumulations, sample counts and caches in the same order):
+ * - requests below a size threshold: one persistent tile launch. The work items (16 x 8 pixel tiles
+ *   with all of a request's samples) are laid out shortest request first (or as given, or longest
+ *   first) and taken by the CTAs of one kernel. A request with a cache ends its paths at the cache
+ *   and evaluates the cache inside the same CTA (tensor cores); after the launch each cache takes
+ *   its renderer's training steps (vg_set_cache) on the batch's training records.
+ * - plain requests from the threshold up: the batch wavefront, the streaming wavefront over the
+ *   pixels of all of them (each path slot traces one pixel of one request with all its samples,
+ *   then takes the next pixel in request order), its bounce loop running on the device inside the
+ *   graph (a conditional WHILE node).
+ * - requests with a cache from the threshold up: one at a time on the streaming cache integrator
+ *   after the shared launches, shortest first.
+ * A plain request's samples are exactly what vg_accumulate's megakernel adds (same sums, either
+ * shared launch); a cached request's exactly what the cache integrator adds with a fixed cache. */
 typedef enum VgBatchOrder { VG_BATCH_SHORTEST_FIRST = 0, VG_BATCH_AS_GIVEN = 1, VG_BATCH_LONGEST_FIRST = 2 } VgBatchOrder;
 
 typedef struct VgBatchRequest {
@@ -379,7 +385,7 @@ typedef struct VgBatchRequest {
 } VgBatchRequest;
 
 typedef struct VgBatchResult {
-    double seconds; /* from the batch's start to this request's last tile, device clock */
+    double seconds; /* from the batch's start to this request's last tile or pixel, device clock */
 } VgBatchResult;
 
 /* Renders all requests (blocking). *total_seconds (optional) is the whole batch on the device
@@ -390,20 +396,25 @@ int vg_batch_render(VgContext* ctx, const VgBatchRequest* requests, size_t n, Vg
  * shared bytes, and the CUDA status of the occupancy query, in that order. */
 int vg_batch_kernel_info(VgContext* ctx, int out[5]);
 /* Batch kernel CTAs per SM (0: as many as fit), the item order, and the size (pixels) from which a
- * request leaves the shared launch and runs on its own through the streaming wavefront (or the
- * cache integrator) after it, shortest first (~0: never; default 512 x 512). vg_batch_tune picks
- * all three. */
+ * request leaves the tile launch: plain requests for the batch wavefront, cached ones for their own
+ * run (~0: never; 0: all of them; default 512 x 512). vg_batch_tune picks all three. */
 int vg_set_batch_options(VgContext* ctx, int blocks_per_sm, int order, uint64_t wavefront_pixels);
-/* Autotuner: times the batch on scratch accumulations of the requests' sizes for each wavefront
- * threshold (256^2, 512^2, 1024^2 pixels, never), shortest or longest first, and the two largest
- * CTA counts per SM that fit; keeps the setting with the lowest objective (median plus 99th
- * percentile request latency) and reports it. The requests' own accumulations are not touched. */
+/* Path slots of the batch wavefront (1024 to 2^26; default 2^21): at most this many pixels are in
+ * flight at once. vg_batch_tune picks it. */
+int vg_set_batch_wave_slots(VgContext* ctx, uint32_t slots);
+/* Autotuner: times the batch on scratch accumulations of the requests' sizes for each threshold
+ * (0, 256^2, 512^2, 1024^2 pixels, never; one that splits the requests as an earlier one did is
+ * skipped), shortest or longest first, the two largest CTA counts per SM that fit (when the tile
+ * launch has requests) and 2^20 or 2^21 wavefront slots (when the batch wavefront has requests);
+ * keeps the setting with the lowest objective (median plus 99th percentile request latency) and
+ * reports it. The requests' own accumulations are not touched. */
 typedef struct VgBatchTune {
     int blocks_per_sm;
     int order;
     uint64_t wavefront_pixels;
     double p50_seconds, p99_seconds, total_seconds; /* of the chosen setting */
     uint32_t trials;
+    uint32_t wave_slots;
 } VgBatchTune;
 int vg_batch_tune(VgContext* ctx, const VgBatchRequest* requests, size_t n, VgBatchTune* out);
 

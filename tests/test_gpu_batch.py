@@ -1,7 +1,8 @@
-"""Batched rendering (vg_batch_render): requests of uneven size, scene and sample count in one
-persistent launch. Plain requests add exactly what a megakernel accumulate adds; a cached request
-without training adds exactly what the cache integrator adds; repeated batches replay the captured
-graph; the autotuner returns a setting that renders the same sums."""
+"""Batched rendering (vg_batch_render): requests of uneven size, scene and sample count in shared
+launches (the persistent tile launch, the batch wavefront with its device-side bounce loop). Plain
+requests add exactly what a megakernel accumulate adds on either; a cached request without
+training adds exactly what the cache integrator adds; repeated batches replay the captured graphs;
+the autotuner returns a setting that renders the same sums."""
 import numpy as np
 import pytest
 
@@ -59,6 +60,67 @@ def test_plain_requests_match_megakernel_accumulates(gpu_ctx, order):
     gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST)
 
 
+WAVE_SPEC = SPEC + [(3, 64, 48, 3, 32), (3, 37, 29, 2, 64)]
+
+
+@pytest.mark.parametrize("slots,tail", [(1 << 21, 32768), (1024, 64), (1024, 4096)])
+def test_batch_wavefront_matches_megakernel_accumulates(gpu_ctx, slots, tail):
+    # Threshold 0: every plain request shares the batch wavefront. The feature zoo has opacity
+    # cut-outs (shadow rays through translucent layers in the finish stage). With 1024 slots each
+    # slot takes many pixels in turn, through the device-side loop (tail 64) or mostly through the
+    # tail kernel (tail 4096, above the slot count).
+    from . import analytic as an
+
+    packed = scenes_for_batch() + [pack.pack(an.feature_zoo())]
+    rs, accs = [], []
+    for si, w, h, spp, prec in WAVE_SPEC:
+        r = Renderer(gpu_ctx, packed[si])
+        r.set_accum_precision(prec)
+        r.set_max_depth(16 if si == 2 else 8)
+        r.set_stream_tail(tail)
+        rs.append(r)
+        accs.append(r.new_accumulation(w, h))
+    gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST, 0)
+    gpu_ctx.set_batch_wave_slots(slots)
+    try:
+        reqs = [BatchRequest(r, a, spec[3]) for r, a, spec in zip(rs, accs, WAVE_SPEC)]
+        out = gpu_ctx.batch_render(reqs)
+        again = gpu_ctx.batch_render(reqs)  # same shape: the captured graph is replayed
+    finally:
+        gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST)
+        gpu_ctx.set_batch_wave_slots(1 << 21)
+    assert again.graph_replayed and not out.graph_replayed
+    assert all(t > 0 for t in again.seconds) and again.total_seconds >= max(again.seconds)
+    for (si, w, h, spp, prec), a in zip(WAVE_SPEC, accs):
+        r = Renderer(gpu_ctx, packed[si])
+        r.set_accum_precision(prec)
+        r.set_max_depth(16 if si == 2 else 8)
+        r.set_integrator(Integrator.MEGAKERNEL)
+        ref = r.new_accumulation(w, h)
+        r.accumulate(ref, spp)
+        r.accumulate(ref, spp)
+        assert a.samples() == 2 * spp
+        if prec == 64:
+            assert np.array_equal(a.sums_f64(), ref.sums_f64())
+        else:
+            assert np.array_equal(a.sums(), ref.sums())
+
+
+def test_batch_wavefront_finishes_small_requests_early(gpu_ctx):
+    packed = scenes_for_batch()
+    r = Renderer(gpu_ctx, packed[2])
+    r.set_max_depth(16)
+    sizes = [(32, 32, 1), (256, 256, 4), (64, 64, 2), (512, 256, 4)]
+    reqs = [BatchRequest(r, r.new_accumulation(w, h), spp) for w, h, spp in sizes]
+    gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST, 0)
+    try:
+        out = gpu_ctx.batch_render(reqs)
+    finally:
+        gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST)
+    assert out.seconds[0] < out.seconds[1] and out.seconds[0] < out.seconds[3]
+    assert out.seconds[2] < out.seconds[3]
+
+
 def test_shortest_first_finishes_small_requests_early(gpu_ctx):
     packed = scenes_for_batch()
     r = Renderer(gpu_ctx, packed[2])
@@ -106,6 +168,7 @@ def test_tune_picks_a_setting_and_keeps_the_sums(gpu_ctx):
     reqs = [BatchRequest(r, a, spec[3]) for r, a, spec in zip(rs, accs, SPEC)]
     t = gpu_ctx.batch_tune(reqs)
     assert t["trials"] >= 8 and t["blocks_per_sm"] >= 1 and t["p50_seconds"] > 0
+    assert t["wave_slots"] in (1 << 20, 1 << 21)
     assert all(a.samples() == 0 for a in accs)  # the tuner used scratch accumulations
     gpu_ctx.batch_render(reqs)
     si, w, h, spp, prec = SPEC[0]
@@ -115,6 +178,7 @@ def test_tune_picks_a_setting_and_keeps_the_sums(gpu_ctx):
     r.accumulate(ref, spp)
     assert np.array_equal(accs[0].sums(), ref.sums())
     gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST)
+    gpu_ctx.set_batch_wave_slots(1 << 21)
 
 
 def test_batch_rejects_adaptive_requests(gpu_ctx):
@@ -125,8 +189,8 @@ def test_batch_rejects_adaptive_requests(gpu_ctx):
 
 
 def test_large_requests_leave_the_shared_launch(gpu_ctx):
-    # Above the threshold a request runs on the streaming wavefront; its sums are still the
-    # megakernel's (the two integrators agree bit for bit) and it finishes after the shared launch.
+    # Above the threshold a plain request runs on the batch wavefront after the tile launch; its
+    # sums are still the megakernel's and it finishes after the small request.
     p = pack.pack(scenes.cornell())
     r = Renderer(gpu_ctx, p)
     r.set_accum_precision(32)

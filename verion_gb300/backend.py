@@ -123,7 +123,8 @@ class _BatchRequest(C.Structure):
 class _BatchTune(C.Structure):
     _fields_ = [("blocks_per_sm", C.c_int), ("order", C.c_int), ("wavefront_pixels", C.c_uint64),
                 ("p50_seconds", C.c_double),
-                ("p99_seconds", C.c_double), ("total_seconds", C.c_double), ("trials", C.c_uint32)]
+                ("p99_seconds", C.c_double), ("total_seconds", C.c_double), ("trials", C.c_uint32),
+                ("wave_slots", C.c_uint32)]
 
 
 BATCH_SHORTEST_FIRST, BATCH_AS_GIVEN, BATCH_LONGEST_FIRST = 0, 1, 2
@@ -253,6 +254,7 @@ def lib() -> C.CDLL:
             "vg_cache_time": (i32, [vp, vp, _S, u32, C.POINTER(f64)]),
             "vg_batch_render": (i32, [vp, vp, _S, vp, C.POINTER(f64), C.POINTER(C.c_int)]),
             "vg_set_batch_options": (i32, [vp, i32, i32, C.c_uint64]),
+            "vg_set_batch_wave_slots": (i32, [vp, C.c_uint32]),
             "vg_batch_kernel_info": (i32, [vp, vp]),
             "vg_batch_tune": (i32, [vp, vp, _S, C.POINTER(_BatchTune)]),
             "vg_accum_cache_stats": (i32, [vp, C.POINTER(CacheStats)]),
@@ -346,8 +348,13 @@ class Context:
     def set_batch_options(self, blocks_per_sm: int = 0, order: int = 0, wavefront_pixels: int = 512 * 512) -> None:
         _check(lib().vg_set_batch_options(self._h, blocks_per_sm, order, wavefront_pixels))
 
+    def set_batch_wave_slots(self, slots: int) -> None:
+        """vg_set_batch_wave_slots: path slots of the batch wavefront (pixels in flight at once)."""
+        _check(lib().vg_set_batch_wave_slots(self._h, slots))
+
     def batch_tune(self, requests) -> dict:
-        """vg_batch_tune: picks the batch kernel's CTAs per SM and item order for these requests."""
+        """vg_batch_tune: picks the tile launch's CTAs per SM, the item order, the size threshold and the
+        batch wavefront's slots for these requests."""
         arr = (_BatchRequest * len(requests))()
         for i, q in enumerate(requests):
             arr[i].renderer = q.renderer._h
@@ -358,7 +365,8 @@ class Context:
         _check(lib().vg_batch_tune(self._h, arr, len(requests), C.byref(t)))
         return {"blocks_per_sm": t.blocks_per_sm, "order": t.order, "wavefront_pixels": t.wavefront_pixels,
                 "p50_seconds": t.p50_seconds,
-                "p99_seconds": t.p99_seconds, "total_seconds": t.total_seconds, "trials": t.trials}
+                "p99_seconds": t.p99_seconds, "total_seconds": t.total_seconds, "trials": t.trials,
+                "wave_slots": t.wave_slots}
 
     def close(self):
         if self._h:

@@ -29,7 +29,7 @@ NVCC_FLAGS = ARCH + [
 ]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", str(CSRC)]
 
-CU_SOURCES = ["kern_mk.cu", "kern_wf.cu", "kern_wf_restir.cu", "kern_nrc.cu", "kern_batch.cu", "vgcuda.cu", "cache.cu", "batch.cu"]
+CU_SOURCES = ["kern_mk.cu", "kern_wf.cu", "kern_wf_restir.cu", "kern_nrc.cu", "kern_batch.cu", "kern_bwave.cu", "vgcuda.cu", "cache.cu", "batch.cu"]
 CXX_SOURCES = ["bvh_build.cpp", "exr.cpp"]
 DEPS = ["vg_math.h", "host.h", "cdf_guide.h", "tc.cuh", "nrc.cuh", "nrc_device.cuh", "vg_layout.h", "vec3.h", "bvh8.h", "traverse.cuh", "pt_device.cuh", "kernels.cuh",
         "launch.h", "launch_nrc.h", "launch_batch.h", "batch.h", "cache_host.h", "bvh_build.h"]

@@ -6,15 +6,30 @@
 #include "cache_host.h"
 #include "launch_batch.h"
 
+// The batch wavefront's buffers: the wave planes of `slots` path slots, the request table and the
+// completion state, and its captured graph.
+struct WaveBufs {
+    DevBuf state, hits, q0, q1, counts, fetch, sreq, meta, squeue, scount, slot_req, slot_pix;
+    DevBuf reqs, done, next, err, loop, t0;
+    uint32_t slots = 0;
+    size_t nreq = 0;
+    std::vector<vgb::WaveReq> host;
+    std::vector<uint64_t> signature;
+    cudaGraphExec_t graph = nullptr;
+};
+
 struct BatchState {
     DevBuf reqs, done, next, err, t0;
     std::vector<vgb::BatchReq> host;
     std::vector<uint64_t> signature; // what the captured graph was made for
     cudaGraphExec_t graph = nullptr;
+    WaveBufs wave;
     ~BatchState()
     {
         if (graph)
             cudaGraphExecDestroy(graph);
+        if (wave.graph)
+            cudaGraphExecDestroy(wave.graph);
     }
 };
 
@@ -239,19 +254,273 @@ int batch_kernel_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int b
     return VG_OK;
 }
 
-// The hybrid schedule: requests below `big` pixels share the persistent launch; the rest follow
-// one at a time on the streaming wavefront (or the cache integrator), shortest first.
+// Builds the batch wavefront's graph: prologue (counters, start kernel), a WHILE node whose body is
+// two waves and the condition kernel, and the tail kernel.
+int bwave_graph(VgContext* ctx, const vgb::WaveBatch& b, const vgk::Wave& w, cudaGraphExec_t* out)
+{
+    cudaStream_t s = ctx->stream;
+    int tb = 1, sb = 1;
+    vgx::bwave_blocks_per_sm(&tb, &sb);
+    cudaGraph_t g = nullptr, part = nullptr;
+    cudaGraphNode_t n0 = nullptr, n1 = nullptr, n2 = nullptr;
+    cudaGraphConditionalHandle loop = 0;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    auto done = [&](cudaError_t err, const char* what) -> int {
+        if (part)
+            cudaGraphDestroy(part);
+        if (g)
+            cudaGraphDestroy(g);
+        return cuda_fail(err, what);
+    };
+    if (e != cudaSuccess)
+        return cuda_fail(e, "graph creation");
+    if ((e = cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess)
+        return done(e, "graph condition");
+    // Prologue.
+    if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed)) != cudaSuccess)
+        return done(e, "graph capture");
+    cudaError_t ce = cudaMemsetAsync(w.counts, 0, 2 * 4, s);
+    if (ce == cudaSuccess)
+        ce = cudaMemsetAsync(w.fetch, 0, 8 * 4, s);
+    if (ce == cudaSuccess)
+        ce = cudaMemsetAsync(w.scount, 0, 2 * vgk::SHADE_CLASSES * 4, s);
+    if (ce == cudaSuccess)
+        ce = cudaMemsetAsync(b.err, 0, 4, s);
+    if (ce == cudaSuccess)
+        ce = vgx::bwave_capture_start(s, b, w);
+    e = cudaStreamEndCapture(s, &part);
+    if (ce != cudaSuccess || e != cudaSuccess)
+        return done(ce != cudaSuccess ? ce : e, "graph capture (start)");
+    if ((e = cudaGraphAddChildGraphNode(&n0, g, nullptr, 0, part)) != cudaSuccess)
+        return done(e, "graph node");
+    cudaGraphDestroy(part);
+    part = nullptr;
+    // The bounce loop.
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = loop;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    if ((e = cudaGraphAddNode(&n1, g, &n0, nullptr, 1, &cp)) != cudaSuccess)
+        return done(e, "graph loop node");
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if ((e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed)) != cudaSuccess)
+        return done(e, "graph capture");
+    ce = vgx::bwave_capture_body(s, tb * ctx->sms, sb * ctx->sms, ctx->sms, b, w, loop);
+    e = cudaStreamEndCapture(s, &body);
+    if (ce != cudaSuccess || e != cudaSuccess)
+        return done(ce != cudaSuccess ? ce : e, "graph capture (loop body)");
+    // Tail.
+    if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed)) != cudaSuccess)
+        return done(e, "graph capture");
+    ce = vgx::bwave_capture_tail(s, b, w);
+    e = cudaStreamEndCapture(s, &part);
+    if (ce != cudaSuccess || e != cudaSuccess)
+        return done(ce != cudaSuccess ? ce : e, "graph capture (tail)");
+    if ((e = cudaGraphAddChildGraphNode(&n2, g, &n1, 1, part)) != cudaSuccess)
+        return done(e, "graph node");
+    cudaGraphDestroy(part);
+    part = nullptr;
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    g = nullptr;
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        return cuda_fail(e, "graph instantiation");
+    }
+    return VG_OK;
+}
+
+// Plain requests on the batch wavefront (kern_bwave.cu), in `order`; the graph is captured the
+// first time and replayed while the batch keeps its shape. Latencies from the start kernel.
+int batch_wave_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int order, VgBatchResult* out,
+                   double* total_seconds, int* replayed)
+{
+    if (!ctx || !reqs || n == 0 || n > 65536)
+        return fail(VG_ERR_INVALID, "empty or oversized batch");
+    uint64_t items64 = 0, bounces = 0, chain = 0;
+    for (size_t i = 0; i < n; i++) {
+        const VgBatchRequest& q = reqs[i];
+        if (!q.renderer || !q.accum || q.renderer->ctx != ctx || q.accum->owner != q.renderer || q.samples == 0)
+            return fail(VG_ERR_INVALID, "batch request " + std::to_string(i) + " is malformed");
+        if (!batch_compatible(q.renderer, q.accum) || q.cache)
+            return fail(VG_ERR_UNSUPPORTED, "batch request " + std::to_string(i) +
+                                                " needs the shared launch or its own run (cache, adaptive, ReSTIR, lighting split)");
+        uint64_t px = (uint64_t)q.accum->width * q.accum->height;
+        uint64_t per = (uint64_t)q.samples * std::max<uint32_t>(q.renderer->max_depth, 1);
+        items64 += px;
+        bounces += px * per;
+        chain = std::max(chain, per);
+    }
+    if (items64 >= (1ull << 31))
+        return fail(VG_ERR_INVALID, "batch wavefront: more than 2^31 pixels in one batch");
+    if (!ctx->batch)
+        ctx->batch = new BatchState();
+    WaveBufs& B = ctx->batch->wave;
+    cudaStream_t s = ctx->stream;
+    uint32_t items = (uint32_t)items64;
+    uint32_t slots = (uint32_t)std::max<uint64_t>(std::min<uint64_t>(items64, std::max(ctx->batch_wave_slots, 1024u)), n);
+    int st;
+    if (B.slots < slots) {
+        size_t S = slots;
+        if ((st = alloc(B.state, S * 16 * vgk::BASE_PLANES, s, false)) != VG_OK ||
+            (st = alloc(B.hits, S * 16, s, false)) != VG_OK || (st = alloc(B.q0, S * 4, s, false)) != VG_OK ||
+            (st = alloc(B.q1, S * 4, s, false)) != VG_OK || (st = alloc(B.sreq, S * 16 * 3, s, false)) != VG_OK ||
+            (st = alloc(B.meta, S * 4, s, false)) != VG_OK ||
+            (st = alloc(B.squeue, S * 4 * vgk::SHADE_CLASSES, s, false)) != VG_OK ||
+            (st = alloc(B.slot_req, S * 4, s, false)) != VG_OK || (st = alloc(B.slot_pix, S * 4, s, false)) != VG_OK) {
+            B.slots = 0;
+            return st;
+        }
+        B.slots = slots;
+        B.signature.clear();
+    }
+    if (B.nreq < n) {
+        if ((st = alloc(B.reqs, n * sizeof(vgb::WaveReq), s, false)) != VG_OK ||
+            (st = alloc(B.done, n * sizeof(vgb::BatchDone), s, false)) != VG_OK) {
+            B.nreq = 0;
+            return st;
+        }
+        B.nreq = n;
+        B.signature.clear();
+    }
+    if ((!B.counts.p && (st = alloc(B.counts, 16, s, true)) != VG_OK) ||
+        (!B.fetch.p && (st = alloc(B.fetch, 64, s, true)) != VG_OK) ||
+        (!B.scount.p && (st = alloc(B.scount, 64, s, true)) != VG_OK) ||
+        (!B.next.p && (st = alloc(B.next, 16, s, true)) != VG_OK) ||
+        (!B.err.p && (st = alloc(B.err, 16, s, true)) != VG_OK) ||
+        (!B.loop.p && (st = alloc(B.loop, 16, s, true)) != VG_OK) ||
+        (!B.t0.p && (st = alloc(B.t0, 16, s, true)) != VG_OK))
+        return st;
+    std::vector<size_t> idx = order_of(reqs, n, order);
+    B.host.resize(n);
+    std::vector<uint64_t> sig;
+    uint32_t begin = 0;
+    for (size_t j = 0; j < n; j++) {
+        const VgBatchRequest& q = reqs[idx[j]];
+        VgRenderer* r = q.renderer;
+        VgAccum* a = q.accum;
+        if (a->samples == 0) {
+            a->adaptive_fixed = true;
+            a->adaptive = r->adaptive;
+            a->restir = r->restir;
+        }
+        vgb::WaveReq& R = B.host[j];
+        memset(&R, 0, sizeof(R));
+        R.c = make_ctx(r, a);
+        R.c.p[P_SAMPLE] = a->samples;
+        R.c.p[P_SAMPLES_PER_DISPATCH] = q.samples;
+        R.item_begin = begin;
+        R.pixels = a->width * a->height;
+        R.f64 = a->precision == 64;
+        R.index = (uint32_t)idx[j];
+        begin += R.pixels;
+        sig.insert(sig.end(), {(uint64_t)(uintptr_t)r, (uint64_t)(uintptr_t)a, q.samples});
+    }
+    VgRenderer* r0 = reqs[idx[0]].renderer;
+    vgk::Wave w{};
+    w.state = (float4*)B.state.p;
+    w.hits = (uint4*)B.hits.p;
+    w.queue[0] = (uint32_t*)B.q0.p;
+    w.queue[1] = (uint32_t*)B.q1.p;
+    w.counts = (uint32_t*)B.counts.p;
+    w.fetch = (uint32_t*)B.fetch.p;
+    w.tstats = nullptr;
+    w.sreq = (float4*)B.sreq.p;
+    w.meta = (uint32_t*)B.meta.p;
+    w.n = slots;
+    w.depth = 0;
+    w.refill = r0->fetch_refill;
+    w.steps = r0->fetch_steps;
+    w.shadow_refill = r0->shadow_fetch_refill;
+    w.shadow_steps = r0->shadow_fetch_steps;
+    w.squeue = (uint32_t*)B.squeue.p;
+    w.scount = (uint32_t*)B.scount.p;
+    vgb::WaveBatch b{};
+    b.reqs = (const vgb::WaveReq*)B.reqs.p;
+    b.nreq = (uint32_t)n;
+    b.items = items;
+    b.slot_req = (uint32_t*)B.slot_req.p;
+    b.slot_pix = (uint32_t*)B.slot_pix.p;
+    b.next = (uint32_t*)B.next.p;
+    b.done = (vgb::BatchDone*)B.done.p;
+    b.err = (uint32_t*)B.err.p;
+    b.loop = (uint32_t*)B.loop.p;
+    b.t0 = (unsigned long long*)B.t0.p;
+    b.tail = std::min(r0->tail_threshold, slots);
+    // Until the work items run out every slot is live, so each wave takes `slots` bounces; then at
+    // most one pixel's samples remain per slot. Two waves per iteration.
+    uint64_t waves = bounces / slots + chain + 4;
+    b.max_iter = (uint32_t)std::min<uint64_t>(waves / 2 + 2, 1u << 30);
+    sig.insert(sig.end(), {(uint64_t)slots, (uint64_t)items, (uint64_t)b.tail, (uint64_t)b.max_iter,
+                           (uint64_t)w.refill << 32 | w.steps, (uint64_t)w.shadow_refill << 32 | w.shadow_steps});
+    VG_CHECK(cudaMemcpyAsync(B.reqs.p, B.host.data(), n * sizeof(vgb::WaveReq), cudaMemcpyHostToDevice, s),
+             "batch table");
+    for (size_t j = 0; j < n; j++)
+        VG_CHECK(cudaMemsetAsync(B.host[j].c.err, 0, 4, s), "error flag");
+    bool reuse = B.graph && sig == B.signature;
+    if (!reuse) {
+        if (B.graph) {
+            cudaGraphExecDestroy(B.graph);
+            B.graph = nullptr;
+        }
+        B.signature.clear();
+        if ((st = bwave_graph(ctx, b, w, &B.graph)) != VG_OK)
+            return st;
+        B.signature = sig;
+    }
+    EventPool pool;
+    cudaEvent_t e0 = pool.get(), e1 = pool.get();
+    VG_CHECK(cudaEventRecord(e0, s), "event");
+    VG_CHECK(cudaGraphLaunch(B.graph, s), "graph launch");
+    VG_CHECK(cudaEventRecord(e1, s), "event");
+    if ((st = wait_event(e1)) != VG_OK)
+        return st;
+    uint32_t err = 0;
+    unsigned long long t0 = 0;
+    std::vector<vgb::BatchDone> done(n);
+    VG_CHECK(cudaMemcpy(&err, B.err.p, 4, cudaMemcpyDeviceToHost), "batch error flag");
+    VG_CHECK(cudaMemcpy(&t0, B.t0.p, 8, cudaMemcpyDeviceToHost), "batch clock");
+    VG_CHECK(cudaMemcpy(done.data(), B.done.p, n * sizeof(vgb::BatchDone), cudaMemcpyDeviceToHost), "batch times");
+    if (err)
+        return fail(VG_ERR_KERNEL, "batch wavefront: a traversal stack overflowed");
+    for (size_t j = 0; j < n; j++) {
+        if ((st = read_err(reqs[idx[j]].renderer)) != VG_OK)
+            return st;
+        if (done[j].remaining != 0)
+            return fail(VG_ERR_KERNEL, "batch wavefront: a request did not finish");
+    }
+    float ms = 0.0f;
+    VG_CHECK(cudaEventElapsedTime(&ms, e0, e1), "event");
+    for (size_t j = 0; j < n; j++) {
+        const VgBatchRequest& q = reqs[idx[j]];
+        q.accum->samples += q.samples;
+        q.accum->launches += 1;
+        if (out)
+            out[idx[j]].seconds = (double)(done[j].done_ns - t0) * 1e-9;
+    }
+    if (total_seconds)
+        *total_seconds = ms * 1e-3;
+    if (replayed)
+        *replayed = reuse ? 1 : 0;
+    return VG_OK;
+}
+
+// The hybrid schedule: requests below `big` pixels share the persistent tile launch; the plain
+// requests from `big` up share the batch wavefront after it; cached requests from `big` up follow
+// one at a time on the streaming cache integrator, shortest first. *replayed: every captured graph
+// that ran was a replay.
 int batch_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int blocks_per_sm, int order, uint64_t big,
               VgBatchResult* out, double* total_seconds, int* replayed)
 {
     if (!ctx || !reqs || n == 0 || n > 65536)
         return fail(VG_ERR_INVALID, "empty or oversized batch");
-    std::vector<size_t> small, large;
+    std::vector<size_t> small, wave, large;
     for (size_t i = 0; i < n; i++) {
         if (!reqs[i].renderer || !reqs[i].accum)
             return fail(VG_ERR_INVALID, "batch request " + std::to_string(i) + " is malformed");
         uint64_t px = (uint64_t)reqs[i].accum->width * reqs[i].accum->height;
-        (px >= big ? large : small).push_back(i);
+        (px < big ? small : reqs[i].cache ? large : wave).push_back(i);
     }
     for (size_t i : large) {
         const VgBatchRequest& q = reqs[i];
@@ -264,18 +533,30 @@ int batch_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int blocks_p
             return fail(VG_ERR_INVALID, "batch request " + std::to_string(i) + " has a cache of another context");
     }
     double t = 0.0;
-    int st, rep = 0;
-    if (!small.empty()) {
+    int st, graphs = 0, replays = 0;
+    auto shared = [&](const std::vector<size_t>& part, bool tiles) -> int {
         std::vector<VgBatchRequest> sr;
-        for (size_t i : small)
+        for (size_t i : part)
             sr.push_back(reqs[i]);
         std::vector<VgBatchResult> so(sr.size());
-        if ((st = batch_kernel_run(ctx, sr.data(), sr.size(), blocks_per_sm, order, so.data(), &t, &rep)) != VG_OK)
-            return st;
-        for (size_t j = 0; j < small.size(); j++)
+        double pt = 0.0;
+        int rep = 0;
+        int e = tiles ? batch_kernel_run(ctx, sr.data(), sr.size(), blocks_per_sm, order, so.data(), &pt, &rep)
+                      : batch_wave_run(ctx, sr.data(), sr.size(), order, so.data(), &pt, &rep);
+        if (e != VG_OK)
+            return e;
+        for (size_t j = 0; j < part.size(); j++)
             if (out)
-                out[small[j]].seconds = so[j].seconds;
-    }
+                out[part[j]].seconds = t + so[j].seconds;
+        t += pt;
+        graphs++;
+        replays += rep;
+        return VG_OK;
+    };
+    if (!small.empty() && (st = shared(small, true)) != VG_OK)
+        return st;
+    if (!wave.empty() && (st = shared(wave, false)) != VG_OK)
+        return st;
     auto cost = [&](size_t i) { return (double)reqs[i].accum->width * reqs[i].accum->height * reqs[i].samples; };
     std::stable_sort(large.begin(), large.end(), [&](size_t a, size_t b) { return cost(a) < cost(b); });
     for (size_t i : large) {
@@ -298,7 +579,7 @@ int batch_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int blocks_p
     if (total_seconds)
         *total_seconds = t;
     if (replayed)
-        *replayed = rep;
+        *replayed = graphs > 0 && replays == graphs ? 1 : 0;
     return VG_OK;
 }
 
@@ -335,6 +616,14 @@ int vg_set_batch_options(VgContext* ctx, int blocks_per_sm, int order, uint64_t 
     return VG_OK;
 }
 
+int vg_set_batch_wave_slots(VgContext* ctx, uint32_t slots)
+{
+    if (!ctx || slots < 1024 || slots > (1u << 26))
+        return fail(VG_ERR_INVALID, "batch wavefront slots must be 1024 to 2^26");
+    ctx->batch_wave_slots = slots;
+    return VG_OK;
+}
+
 int vg_batch_tune(VgContext* ctx, const VgBatchRequest* requests, size_t n, VgBatchTune* out)
 {
     DevGuard device_guard(dev_of(ctx));
@@ -360,18 +649,42 @@ int vg_batch_tune(VgContext* ctx, const VgBatchRequest* requests, size_t n, VgBa
     }
     int best_b = 0, best_o = 0;
     uint64_t best_px = ctx->batch_wavefront_pixels;
+    uint32_t best_slots = ctx->batch_wave_slots, slots0 = ctx->batch_wave_slots;
     double best = 1e300;
-    const uint64_t thresholds[] = {256ull * 256, 512ull * 512, 1024ull * 1024, ~0ull};
+    const uint64_t thresholds[] = {0, 256ull * 256, 512ull * 512, 1024ull * 1024, ~0ull};
     VgBatchTune res{};
     uint32_t trials = 0;
     std::vector<VgBatchResult> times(n);
     int max_b = vgx::batch_blocks_per_sm();
-    // As given is the caller's order: left out. CTA counts: the two largest that fit.
-    for (uint64_t big : thresholds)
-    for (int o : {(int)VG_BATCH_SHORTEST_FIRST, (int)VG_BATCH_LONGEST_FIRST}) {
-        for (int bps = std::max(1, max_b - 1); bps <= max_b && st == VG_OK; bps++) {
+    std::vector<std::pair<size_t, size_t>> tried;
+    // As given is the caller's order: left out. CTA counts of the tile launch: the two largest
+    // that fit; path slots of the batch wavefront: 2^20 and 2^21. A threshold that splits the
+    // requests as an earlier one did is skipped.
+    for (uint64_t big : thresholds) {
+        size_t n_small = 0, n_wave = 0;
+        for (size_t i = 0; i < n; i++) {
+            uint64_t px = (uint64_t)requests[i].accum->width * requests[i].accum->height;
+            n_small += px < big;
+            n_wave += px >= big && !requests[i].cache;
+        }
+        if (std::find(tried.begin(), tried.end(), std::make_pair(n_small, n_wave)) != tried.end())
+            continue;
+        tried.push_back({n_small, n_wave});
+        std::vector<int> bpss, slotss;
+        for (int bps = n_small ? std::max(1, max_b - 1) : max_b; bps <= max_b; bps++)
+            bpss.push_back(bps);
+        if (n_wave)
+            slotss = {1 << 20, 1 << 21};
+        else
+            slotss = {(int)slots0};
+        for (int o : {(int)VG_BATCH_SHORTEST_FIRST, (int)VG_BATCH_LONGEST_FIRST})
+        for (int bps : bpss)
+        for (int sl : slotss) {
+            if (st != VG_OK)
+                break;
+            ctx->batch_wave_slots = (uint32_t)sl;
             double total = 0.0;
-            // One run to capture the graph, one timed replay.
+            // One run to capture the graphs, one timed replay.
             for (int rep = 0; rep < 2 && st == VG_OK; rep++)
                 st = batch_run(ctx, trial.data(), n, bps, o, big, times.data(), &total, nullptr);
             if (st != VG_OK)
@@ -388,12 +701,14 @@ int vg_batch_tune(VgContext* ctx, const VgBatchRequest* requests, size_t n, VgBa
                 best_b = bps;
                 best_o = o;
                 best_px = big;
+                best_slots = (uint32_t)sl;
                 res.p50_seconds = p50;
                 res.p99_seconds = p99;
                 res.total_seconds = total;
             }
         }
     }
+    ctx->batch_wave_slots = best_slots;
     for (VgAccum* a : scratch)
         if (a)
             vg_accum_destroy(a);
@@ -405,6 +720,7 @@ int vg_batch_tune(VgContext* ctx, const VgBatchRequest* requests, size_t n, VgBa
     res.blocks_per_sm = best_b;
     res.order = best_o;
     res.wavefront_pixels = best_px;
+    res.wave_slots = best_slots;
     res.trials = trials;
     *out = res;
     return VG_OK;

@@ -29,4 +29,31 @@ struct BatchDone {
     unsigned long long done_ns;   // %globaltimer at completion
 };
 
+// One request of the batch wavefront (kern_bwave.cu): its pixels are the work items
+// [item_begin, item_begin + pixels) of the batch, each traced with all of the request's samples.
+struct alignas(16) WaveReq {
+    vgd::Ctx c;          // scene tables, parameter block (samples from P_SAMPLE, P_SAMPLES_PER_DISPATCH of them), sums
+    uint32_t item_begin;
+    uint32_t pixels;
+    uint32_t f64;        // sums in double precision
+    uint32_t index;      // position of the request in the caller's list
+};
+
+// The batch wavefront's work and completion state besides the wave buffers (vgk::Wave, whose
+// slots here hold any request's pixel).
+struct WaveBatch {
+    const WaveReq* reqs;
+    uint32_t nreq;
+    uint32_t items;             // pixels of all requests
+    uint32_t* slot_req;         // per slot: request of the pixel it traces
+    uint32_t* slot_pix;         // per slot: that pixel
+    uint32_t* next;             // next work item
+    BatchDone* done;            // per request: pixels not finished, completion time
+    uint32_t* err;              // traversal error flags of the batch
+    uint32_t* loop;             // iterations of the device-side bounce loop
+    unsigned long long* t0;     // start time
+    uint32_t tail;              // live slots at or below which the loop hands over to the tail kernel
+    uint32_t max_iter;          // bound on the loop's iterations
+};
+
 } // namespace vgb

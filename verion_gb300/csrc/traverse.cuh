@@ -606,12 +606,16 @@ __device__ __forceinline__ void trace_queue_coop(const uint4* __restrict__ nodes
     }
 }
 
-template <bool ANY, typename GetRay, typename PutHit>
-__device__ __forceinline__ void trace_queue(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
-                                            uint32_t* fetch, uint32_t count, uint32_t* err, uint32_t refill,
-                                            uint32_t steps, GetRay get, PutHit put)
+// The body of trace_queue and trace_queue_scenes: with SCENES, `get` also names the BVH of each ray
+// (its node and triangle arrays), which the lane keeps while it walks that ray.
+template <bool ANY, bool SCENES, typename GetRay, typename PutHit>
+__device__ __forceinline__ void trace_queue_impl(const uint4* __restrict__ nodes0, const float4* __restrict__ tris0,
+                                                 uint32_t* fetch, uint32_t count, uint32_t* err, uint32_t refill,
+                                                 uint32_t steps, GetRay get, PutHit put)
 {
     const uint32_t FULLM = 0xffffffffu;
+    const uint4* nodes = nodes0;
+    const float4* tris = tris0;
     uint32_t lane = threadIdx.x & 31u;
     uint32_t lt = (1u << lane) - 1u;
     uint2 stack[bvh8::STACK_SIZE];
@@ -637,7 +641,12 @@ __device__ __forceinline__ void trace_queue(const uint4* __restrict__ nodes, con
                     w.h.gid = 0xffffffffu;
                     w.h.b1 = w.h.b2 = 0.0f;
                     w.h.nodes = w.h.tests = 0;
-                    if (get(idx, o, d, tmax)) {
+                    bool ok;
+                    if constexpr (SCENES)
+                        ok = get(idx, o, d, tmax, nodes, tris);
+                    else
+                        ok = get(idx, o, d, tmax);
+                    if (ok) {
                         w.r = make_ray(o, d);
                         w.tmax = tmax;
                         w.h.t = tmax;
@@ -667,6 +676,23 @@ __device__ __forceinline__ void trace_queue(const uint4* __restrict__ nodes, con
             }
         }
     }
+}
+
+template <bool ANY, typename GetRay, typename PutHit>
+__device__ __forceinline__ void trace_queue(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
+                                            uint32_t* fetch, uint32_t count, uint32_t* err, uint32_t refill,
+                                            uint32_t steps, GetRay get, PutHit put)
+{
+    trace_queue_impl<ANY, false>(nodes, tris, fetch, count, err, refill, steps, get, put);
+}
+
+// trace_queue over the rays of several scenes: get(idx, o, d, tmax, nodes, tris) also sets the
+// ray's BVH arrays.
+template <bool ANY, typename GetRay, typename PutHit>
+__device__ __forceinline__ void trace_queue_scenes(uint32_t* fetch, uint32_t count, uint32_t* err, uint32_t refill,
+                                                   uint32_t steps, GetRay get, PutHit put)
+{
+    trace_queue_impl<ANY, true>(nullptr, nullptr, fetch, count, err, refill, steps, get, put);
 }
 
 } // namespace vgt
