@@ -106,6 +106,74 @@ def test_batch_wavefront_matches_megakernel_accumulates(gpu_ctx, slots, tail):
             assert np.array_equal(a.sums(), ref.sums())
 
 
+@pytest.mark.parametrize("slots", [1 << 21, 1024])
+def test_batch_wavefront_cached_requests_match_the_cache_integrator(gpu_ctx, slots):
+    # Threshold 0: cached requests share the batch wavefront with plain ones. Without training the
+    # caches are fixed, so each cached request adds exactly what the megakernel cache integrator
+    # adds (one sample per frame): the same paths, training pixels, queries and answers, in the
+    # same order per pixel. Two caches answer in the same wave kernel; the feature zoo has
+    # translucent surfaces; with 1024 slots the slots take many pixels each.
+    from . import analytic as an
+
+    packed = [pack.pack(scenes.cornell()), pack.pack(an.feature_zoo())]
+    spec = [(0, 48, 40, 3, 64, 0), (1, 37, 29, 2, 64, 1), (0, 33, 20, 4, 32, 0), (0, 40, 30, 2, 32, None)]
+
+    def renderer(si, prec, cached):
+        r = Renderer(gpu_ctx, packed[si])
+        r.set_accum_precision(prec)
+        c = None
+        if cached:
+            c = Cache(gpu_ctx, bounds=r.bounds(), seed=7)
+            r.set_cache(c, spread=0.01, train_paths=256, train_steps=0, train_batch=1024)
+        return r, c
+
+    shared = {}
+    reqs, accs = [], []
+    for si, w, h, spp, prec, ci in spec:
+        if ci is None:
+            r, c = renderer(si, prec, False)
+        else:
+            if ci not in shared:
+                shared[ci] = renderer(si, prec, True)
+            r, c = shared[ci]
+            r.set_accum_precision(prec)
+        a = r.new_accumulation(w, h)
+        accs.append(a)
+        reqs.append(BatchRequest(r, a, spp, c))
+    gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST, 0)
+    gpu_ctx.set_batch_wave_slots(slots)
+    try:
+        out = gpu_ctx.batch_render(reqs)
+    finally:
+        gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST)
+        gpu_ctx.set_batch_wave_slots(1 << 21)
+    assert len(out.seconds) == len(spec)
+    for (si, w, h, spp, prec, ci), a in zip(spec, accs):
+        r, _ = renderer(si, prec, ci is not None)
+        ref = r.new_accumulation(w, h)
+        r.accumulate(ref, spp)
+        assert a.samples() == spp
+        if prec == 64:
+            assert np.array_equal(a.sums_f64(), ref.sums_f64()), (si, w, h)
+        else:
+            assert np.array_equal(a.sums(), ref.sums()), (si, w, h)
+
+
+def test_batch_wavefront_trains_the_caches(gpu_ctx):
+    p = pack.pack(scenes.cornell())
+    r = Renderer(gpu_ctx, p)
+    cache = Cache(gpu_ctx, bounds=r.bounds())
+    r.set_cache(cache, spread=0.01, train_paths=1024, train_steps=2, train_batch=4096)
+    before, _ = cache.read_params()
+    gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST, 0)
+    try:
+        gpu_ctx.batch_render([BatchRequest(r, r.new_accumulation(64, 64), 2, cache)])
+    finally:
+        gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST)
+    after, _ = cache.read_params()
+    assert not np.array_equal(before, after)
+
+
 def test_batch_wavefront_finishes_small_requests_early(gpu_ctx):
     packed = scenes_for_batch()
     r = Renderer(gpu_ctx, packed[2])

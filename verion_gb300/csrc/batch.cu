@@ -11,8 +11,9 @@
 struct WaveBufs {
     DevBuf state, hits, q0, q1, counts, fetch, sreq, meta, squeue, scount, slot_req, slot_pix;
     DevBuf reqs, done, next, err, loop, t0;
-    uint32_t slots = 0;
-    size_t nreq = 0;
+    DevBuf spread, tvert, tnv, caches, qrec, qcount; // cached requests
+    uint32_t slots = 0, cache_slots = 0;
+    size_t nreq = 0, ncache = 0;
     std::vector<vgb::WaveReq> host;
     std::vector<uint64_t> signature;
     cudaGraphExec_t graph = nullptr;
@@ -168,6 +169,10 @@ int batch_kernel_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int b
     // larger request is safe.
     int bps = blocks_per_sm > 0 ? std::min(blocks_per_sm, 8) : vgx::batch_blocks_per_sm();
     sig.insert(sig.end(), {(uint64_t)bps, (uint64_t)order});
+    // The captured training steps use the caches' work buffers, which other calls may reallocate.
+    for (auto& kc : caches)
+        sig.insert(sig.end(), {(uint64_t)(uintptr_t)kc.first->X.p, (uint64_t)(uintptr_t)kc.first->GX.p,
+                               (uint64_t)(uintptr_t)kc.first->batch_rec.p, (uint64_t)(uintptr_t)kc.first->batch_count.p});
     if (b->reqs.bytes < n * sizeof(vgb::BatchReq) || b->done.bytes < n * sizeof(vgb::BatchDone)) {
         if ((st = alloc(b->reqs, n * sizeof(vgb::BatchReq), s, false)) != VG_OK ||
             (st = alloc(b->done, n * sizeof(vgb::BatchDone), s, false)) != VG_OK)
@@ -256,7 +261,8 @@ int batch_kernel_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int b
 
 // Builds the batch wavefront's graph: prologue (counters, start kernel), a WHILE node whose body is
 // two waves and the condition kernel, and the tail kernel.
-int bwave_graph(VgContext* ctx, const vgb::WaveBatch& b, const vgk::Wave& w, cudaGraphExec_t* out)
+int bwave_graph(VgContext* ctx, const vgb::WaveBatch& b, const vgk::Wave& w,
+                const std::vector<std::pair<VgCache*, VgRenderer*>>& caches, cudaGraphExec_t* out)
 {
     cudaStream_t s = ctx->stream;
     int tb = 1, sb = 1;
@@ -281,9 +287,9 @@ int bwave_graph(VgContext* ctx, const vgb::WaveBatch& b, const vgk::Wave& w, cud
         return done(e, "graph capture");
     cudaError_t ce = cudaMemsetAsync(w.counts, 0, 2 * 4, s);
     if (ce == cudaSuccess)
-        ce = cudaMemsetAsync(w.fetch, 0, 8 * 4, s);
+        ce = cudaMemsetAsync(w.fetch, 0, 16 * 4, s);
     if (ce == cudaSuccess)
-        ce = cudaMemsetAsync(w.scount, 0, 2 * vgk::SHADE_CLASSES * 4, s);
+        ce = cudaMemsetAsync(w.scount, 0, 2 * 2 * vgk::SHADE_CLASSES * 4, s);
     if (ce == cudaSuccess)
         ce = cudaMemsetAsync(b.err, 0, 4, s);
     if (ce == cudaSuccess)
@@ -310,11 +316,27 @@ int bwave_graph(VgContext* ctx, const vgb::WaveBatch& b, const vgk::Wave& w, cud
     e = cudaStreamEndCapture(s, &body);
     if (ce != cudaSuccess || e != cudaSuccess)
         return done(ce != cudaSuccess ? ce : e, "graph capture (loop body)");
-    // Tail.
+    // Tail (batches without caches; with caches the loop runs until no slot is live), then the
+    // caches' training steps on the batch's training records.
     if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed)) != cudaSuccess)
         return done(e, "graph capture");
-    ce = vgx::bwave_capture_tail(s, b, w);
+    ce = caches.empty() ? vgx::bwave_capture_tail(s, b, w) : cudaSuccess;
+    int st = VG_OK;
+    for (auto& kc : caches) {
+        VgCache* k = kc.first;
+        VgRenderer* r = kc.second;
+        uint32_t tcap = r->cache_steps * r->cache_batch;
+        for (uint32_t t = 0; t < r->cache_steps && st == VG_OK; t++)
+            st = vgc::cache_train_step(k, (const float*)k->batch_rec.p, (const uint32_t*)k->batch_count.p, tcap,
+                                       t * r->cache_batch, r->cache_batch);
+    }
     e = cudaStreamEndCapture(s, &part);
+    if (st != VG_OK) {
+        if (part)
+            cudaGraphDestroy(part);
+        cudaGraphDestroy(g);
+        return st;
+    }
     if (ce != cudaSuccess || e != cudaSuccess)
         return done(ce != cudaSuccess ? ce : e, "graph capture (tail)");
     if ((e = cudaGraphAddChildGraphNode(&n2, g, &n1, 1, part)) != cudaSuccess)
@@ -331,8 +353,8 @@ int bwave_graph(VgContext* ctx, const vgb::WaveBatch& b, const vgk::Wave& w, cud
     return VG_OK;
 }
 
-// Plain requests on the batch wavefront (kern_bwave.cu), in `order`; the graph is captured the
-// first time and replayed while the batch keeps its shape. Latencies from the start kernel.
+// Requests on the batch wavefront (kern_bwave.cu), in `order`; the graph is captured the first time
+// and replayed while the batch keeps its shape. Latencies from the start kernel.
 int batch_wave_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int order, VgBatchResult* out,
                    double* total_seconds, int* replayed)
 {
@@ -343,10 +365,14 @@ int batch_wave_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int ord
         const VgBatchRequest& q = reqs[i];
         if (!q.renderer || !q.accum || q.renderer->ctx != ctx || q.accum->owner != q.renderer || q.samples == 0)
             return fail(VG_ERR_INVALID, "batch request " + std::to_string(i) + " is malformed");
-        if (!batch_compatible(q.renderer, q.accum) || q.cache)
+        if (!batch_compatible(q.renderer, q.accum))
             return fail(VG_ERR_UNSUPPORTED, "batch request " + std::to_string(i) +
-                                                " needs the shared launch or its own run (cache, adaptive, ReSTIR, lighting split)");
+                                                " uses adaptive sampling, ReSTIR or the lighting split");
         uint64_t px = (uint64_t)q.accum->width * q.accum->height;
+        if (q.cache && (q.cache->ctx != ctx || px > (1u << 22) || n > 1024))
+            return fail(VG_ERR_UNSUPPORTED, "batch request " + std::to_string(i) +
+                                                ": a cached request on the batch wavefront needs the context's cache, "
+                                                "at most 2^22 pixels and at most 1024 requests in the batch");
         uint64_t per = (uint64_t)q.samples * std::max<uint32_t>(q.renderer->max_depth, 1);
         items64 += px;
         bounces += px * per;
@@ -367,7 +393,7 @@ int batch_wave_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int ord
             (st = alloc(B.hits, S * 16, s, false)) != VG_OK || (st = alloc(B.q0, S * 4, s, false)) != VG_OK ||
             (st = alloc(B.q1, S * 4, s, false)) != VG_OK || (st = alloc(B.sreq, S * 16 * 3, s, false)) != VG_OK ||
             (st = alloc(B.meta, S * 4, s, false)) != VG_OK ||
-            (st = alloc(B.squeue, S * 4 * vgk::SHADE_CLASSES, s, false)) != VG_OK ||
+            (st = alloc(B.squeue, S * 4 * 2 * vgk::SHADE_CLASSES, s, false)) != VG_OK ||
             (st = alloc(B.slot_req, S * 4, s, false)) != VG_OK || (st = alloc(B.slot_pix, S * 4, s, false)) != VG_OK) {
             B.slots = 0;
             return st;
@@ -393,6 +419,65 @@ int batch_wave_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int ord
         (!B.t0.p && (st = alloc(B.t0, 16, s, true)) != VG_OK))
         return st;
     std::vector<size_t> idx = order_of(reqs, n, order);
+    // The caches of the batch (the first renderer using a cache sets its training steps), their
+    // training buffers and query buffers (one record per slot and wave).
+    std::vector<std::pair<VgCache*, VgRenderer*>> caches;
+    for (size_t i : idx) {
+        VgCache* k = reqs[i].cache;
+        if (!k)
+            continue;
+        bool seen = false;
+        for (auto& kc : caches)
+            seen |= kc.first == k;
+        if (seen)
+            continue;
+        VgRenderer* r = reqs[i].renderer;
+        size_t tcap = std::max<size_t>((size_t)r->cache_steps * r->cache_batch, 1);
+        if (k->batch_rec.bytes < tcap * vgn::REC_WORDS * 4 &&
+            (st = alloc(k->batch_rec, tcap * vgn::REC_WORDS * 4, s, false)) != VG_OK)
+            return st;
+        if (!k->batch_count.p && (st = alloc(k->batch_count, 16, s, true)) != VG_OK)
+            return st;
+        if ((st = vgc::ensure_work(k, std::max<size_t>(r->cache_batch, 1))) != VG_OK)
+            return st;
+        caches.push_back({k, r});
+    }
+    size_t nc = caches.size();
+    if (nc && B.cache_slots < slots) {
+        size_t S = slots;
+        if ((st = alloc(B.spread, S * 8, s, false)) != VG_OK ||
+            (st = alloc(B.tvert, S * vgb::WAVE_MAX_TRAIN_VERTICES * vgb::WAVE_VERTEX_VEC4 * 16, s, false)) != VG_OK ||
+            (st = alloc(B.tnv, S * 4, s, false)) != VG_OK) {
+            B.cache_slots = 0;
+            return st;
+        }
+        B.cache_slots = slots;
+        B.ncache = 0; // query buffers are per slot too
+        B.signature.clear();
+    }
+    if (nc && B.ncache < nc) {
+        if ((st = alloc(B.caches, nc * sizeof(vgb::WaveCache), s, false)) != VG_OK ||
+            (st = alloc(B.qrec, nc * (size_t)B.cache_slots * vgn::REC_WORDS * 4, s, false)) != VG_OK ||
+            (st = alloc(B.qcount, nc * 4, s, true)) != VG_OK) {
+            B.ncache = 0;
+            return st;
+        }
+        B.ncache = nc;
+        B.signature.clear();
+    }
+    std::vector<vgb::WaveCache> ktab(nc);
+    for (size_t j = 0; j < nc; j++) {
+        VgCache* k = caches[j].first;
+        VgRenderer* r = caches[j].second;
+        vgb::WaveCache& K = ktab[j];
+        memset(&K, 0, sizeof(K));
+        K.cd = k->dev();
+        K.qrec = (float*)B.qrec.p + j * (size_t)B.cache_slots * vgn::REC_WORDS;
+        K.qcount = (uint32_t*)B.qcount.p + j;
+        K.trec = (float*)k->batch_rec.p;
+        K.tcount = (uint32_t*)k->batch_count.p;
+        K.tcap = r->cache_steps * r->cache_batch;
+    }
     B.host.resize(n);
     std::vector<uint64_t> sig;
     uint32_t begin = 0;
@@ -414,8 +499,18 @@ int batch_wave_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int ord
         R.pixels = a->width * a->height;
         R.f64 = a->precision == 64;
         R.index = (uint32_t)idx[j];
+        R.cache = vgb::NO_CACHE;
+        if (q.cache) {
+            for (size_t c = 0; c < nc; c++)
+                if (caches[c].first == q.cache)
+                    R.cache = (uint32_t)c;
+            R.spread = r->cache_spread;
+            R.train_stride = (uint32_t)std::max<size_t>(1, r->cache_train_paths ? R.pixels / r->cache_train_paths
+                                                                                : (size_t)R.pixels + 1);
+        }
         begin += R.pixels;
-        sig.insert(sig.end(), {(uint64_t)(uintptr_t)r, (uint64_t)(uintptr_t)a, q.samples});
+        sig.insert(sig.end(), {(uint64_t)(uintptr_t)r, (uint64_t)(uintptr_t)a, q.samples, (uint64_t)(uintptr_t)q.cache,
+                               q.cache ? ((uint64_t)r->cache_steps << 32 | r->cache_batch) : 0});
     }
     VgRenderer* r0 = reqs[idx[0]].renderer;
     vgk::Wave w{};
@@ -447,17 +542,33 @@ int batch_wave_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int ord
     b.err = (uint32_t*)B.err.p;
     b.loop = (uint32_t*)B.loop.p;
     b.t0 = (unsigned long long*)B.t0.p;
-    b.tail = std::min(r0->tail_threshold, slots);
+    b.tail = nc ? 0u : std::min(r0->tail_threshold, slots);
+    b.caches = nc ? (const vgb::WaveCache*)B.caches.p : nullptr;
+    b.ncache = (uint32_t)nc;
+    b.spread = nc ? (float2*)B.spread.p : nullptr;
+    b.tvert = nc ? (float4*)B.tvert.p : nullptr;
+    b.tnv = nc ? (uint32_t*)B.tnv.p : nullptr;
     // Until the work items run out every slot is live, so each wave takes `slots` bounces; then at
     // most one pixel's samples remain per slot. Two waves per iteration.
     uint64_t waves = bounces / slots + chain + 4;
     b.max_iter = (uint32_t)std::min<uint64_t>(waves / 2 + 2, 1u << 30);
     sig.insert(sig.end(), {(uint64_t)slots, (uint64_t)items, (uint64_t)b.tail, (uint64_t)b.max_iter,
                            (uint64_t)w.refill << 32 | w.steps, (uint64_t)w.shadow_refill << 32 | w.shadow_steps});
+    // The captured training steps use the caches' work buffers, which other calls may reallocate.
+    for (auto& kc : caches)
+        sig.insert(sig.end(), {(uint64_t)(uintptr_t)kc.first->X.p, (uint64_t)(uintptr_t)kc.first->GX.p,
+                               (uint64_t)(uintptr_t)kc.first->batch_rec.p, (uint64_t)(uintptr_t)kc.first->batch_count.p});
     VG_CHECK(cudaMemcpyAsync(B.reqs.p, B.host.data(), n * sizeof(vgb::WaveReq), cudaMemcpyHostToDevice, s),
              "batch table");
+    if (nc)
+        VG_CHECK(cudaMemcpyAsync(B.caches.p, ktab.data(), nc * sizeof(vgb::WaveCache), cudaMemcpyHostToDevice, s),
+                 "batch cache table");
     for (size_t j = 0; j < n; j++)
         VG_CHECK(cudaMemsetAsync(B.host[j].c.err, 0, 4, s), "error flag");
+    for (auto& kc : caches) {
+        VG_CHECK(cudaMemsetAsync(kc.first->batch_count.p, 0, 4, s), "training count");
+        VG_CHECK(cudaMemsetAsync(kc.first->err.p, 0, 4, s), "cache error flag");
+    }
     bool reuse = B.graph && sig == B.signature;
     if (!reuse) {
         if (B.graph) {
@@ -465,7 +576,7 @@ int batch_wave_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int ord
             B.graph = nullptr;
         }
         B.signature.clear();
-        if ((st = bwave_graph(ctx, b, w, &B.graph)) != VG_OK)
+        if ((st = bwave_graph(ctx, b, w, caches, &B.graph)) != VG_OK)
             return st;
         B.signature = sig;
     }
@@ -482,8 +593,13 @@ int batch_wave_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int ord
     VG_CHECK(cudaMemcpy(&err, B.err.p, 4, cudaMemcpyDeviceToHost), "batch error flag");
     VG_CHECK(cudaMemcpy(&t0, B.t0.p, 8, cudaMemcpyDeviceToHost), "batch clock");
     VG_CHECK(cudaMemcpy(done.data(), B.done.p, n * sizeof(vgb::BatchDone), cudaMemcpyDeviceToHost), "batch times");
+    if (err & vgn::ERR_MMA_TIMEOUT)
+        return fail(VG_ERR_KERNEL, "batch wavefront: a tensor-core completion wait timed out");
     if (err)
         return fail(VG_ERR_KERNEL, "batch wavefront: a traversal stack overflowed");
+    for (auto& kc : caches)
+        if ((st = vgc::cache_check(kc.first)) != VG_OK)
+            return st;
     for (size_t j = 0; j < n; j++) {
         if ((st = read_err(reqs[idx[j]].renderer)) != VG_OK)
             return st;
@@ -506,10 +622,11 @@ int batch_wave_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int ord
     return VG_OK;
 }
 
-// The hybrid schedule: requests below `big` pixels share the persistent tile launch; the plain
-// requests from `big` up share the batch wavefront after it; cached requests from `big` up follow
-// one at a time on the streaming cache integrator, shortest first. *replayed: every captured graph
-// that ran was a replay.
+// The hybrid schedule: requests below `big` pixels share the persistent tile launch; the requests
+// from `big` up share the batch wavefront after it, except cached ones the wavefront cannot tag
+// (more than 2^22 pixels, or more than 1024 requests in the batch), which follow one at a time on
+// the streaming cache integrator, shortest first. *replayed: every captured graph that ran was a
+// replay.
 int batch_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int blocks_per_sm, int order, uint64_t big,
               VgBatchResult* out, double* total_seconds, int* replayed)
 {
@@ -520,7 +637,7 @@ int batch_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int blocks_p
         if (!reqs[i].renderer || !reqs[i].accum)
             return fail(VG_ERR_INVALID, "batch request " + std::to_string(i) + " is malformed");
         uint64_t px = (uint64_t)reqs[i].accum->width * reqs[i].accum->height;
-        (px < big ? small : reqs[i].cache ? large : wave).push_back(i);
+        (px < big ? small : reqs[i].cache && (px > (1u << 22) || n > 1024) ? large : wave).push_back(i);
     }
     for (size_t i : large) {
         const VgBatchRequest& q = reqs[i];
@@ -665,7 +782,7 @@ int vg_batch_tune(VgContext* ctx, const VgBatchRequest* requests, size_t n, VgBa
         for (size_t i = 0; i < n; i++) {
             uint64_t px = (uint64_t)requests[i].accum->width * requests[i].accum->height;
             n_small += px < big;
-            n_wave += px >= big && !requests[i].cache;
+            n_wave += px >= big;
         }
         if (std::find(tried.begin(), tried.end(), std::make_pair(n_small, n_wave)) != tried.end())
             continue;

@@ -37,6 +37,27 @@ struct alignas(16) WaveReq {
     uint32_t pixels;
     uint32_t f64;        // sums in double precision
     uint32_t index;      // position of the request in the caller's list
+    uint32_t cache;      // the request's radiance cache in the batch's cache table, NO_CACHE for a plain request
+    float spread;        // cache: path-spread threshold
+    uint32_t train_stride; // cache: one pixel in train_stride traces a training path per sample
+    uint32_t pad;
+};
+
+constexpr uint32_t NO_CACHE = 0xffffffffu;
+constexpr uint32_t WAVE_MAX_TRAIN_VERTICES = 16; // cache vertices recorded per training path
+constexpr uint32_t WAVE_VERTEX_VEC4 = 6;         // per vertex: 16 features, throughput, radiance so far
+
+// A radiance cache of the batch wavefront: its network and grid; the query records of the current
+// wave (at most one per slot), each with its request and pixel ((request << 22) | pixel) in the
+// last word; the batch's training records.
+struct alignas(16) WaveCache {
+    vgn::CacheDev cd;
+    float* qrec;
+    uint32_t* qcount;
+    float* trec;
+    uint32_t* tcount;
+    uint32_t tcap;
+    uint32_t pad[3];
 };
 
 // The batch wavefront's work and completion state besides the wave buffers (vgk::Wave, whose
@@ -54,6 +75,11 @@ struct WaveBatch {
     unsigned long long* t0;     // start time
     uint32_t tail;              // live slots at or below which the loop hands over to the tail kernel
     uint32_t max_iter;          // bound on the loop's iterations
+    const WaveCache* caches;    // the radiance caches of the batch's cached requests
+    uint32_t ncache;
+    float2* spread;             // per slot: the path spread (a0, a) of a cached request's path
+    float4* tvert;              // per slot: WAVE_MAX_TRAIN_VERTICES x WAVE_VERTEX_VEC4 (training paths)
+    uint32_t* tnv;              // per slot: vertices recorded by its training path
 };
 
 } // namespace vgb
