@@ -556,11 +556,12 @@ def _pct(v, q):
 def batch_report(ctx, spp_scale, side_range=(256, 2048), spp_range=(16, 256)):
     """Batched serving (64 requests): resolution log-uniform 256^2-2048^2 (square), scenes of ~10k-2M
     triangles generated like the 1M-triangle workload, spp log-uniform 16-256 (times spp_scale),
-    depth 16, every second request with a radiance cache. One batch (autotuned, graph replayed)
-    against the same requests rendered one at a time with accumulate (each on the faster of the
-    wavefront and the megakernel), shortest first; latency = device time from the
-    start until the request's last tile. The batch is first autotuned (vg_batch_tune) at a quarter
-    of the sample counts."""
+    depth 16, every second request with a radiance cache. One batch (vg_batch_render: the tile
+    launch below the tuned size threshold, the batch wavefront from it up, each a replayed CUDA
+    graph) against the same requests rendered one at a time with accumulate (each on the faster of
+    the wavefront and the megakernel), shortest first; latency = device time from the start until
+    the request's last tile or pixel. The batch is first autotuned (vg_batch_tune: threshold,
+    order, tile CTAs per SM, wavefront slots) at a quarter of the sample counts."""
     from verion_gb300 import pack, scenes
     from verion_gb300.backend import BatchRequest, Cache, Integrator, Renderer
 
@@ -620,6 +621,10 @@ def batch_report(ctx, spp_scale, side_range=(256, 2048), spp_range=(16, 256)):
         lat[i] = now
     for r in plain_r + cached_r:
         r.set_integrator(Integrator.MEGAKERNEL)
+    big = tuned["wavefront_pixels"]
+    launches = {"tile_launch": sum(1 for s in spec if s[0] * s[0] < big),
+                "batch_wavefront": sum(1 for s in spec if s[0] * s[0] >= big and not (s[3] and s[0] * s[0] > 1 << 22)),
+                "one_at_a_time": sum(1 for s in spec if s[0] * s[0] >= big and s[3] and s[0] * s[0] > 1 << 22)}
     return {
         "config": f"64 requests, square {min(s[0] for s in spec)}-{max(s[0] for s in spec)} px, "
                   f"spp {min(s[1] for s in spec)}-{max(s[1] for s in spec)} ({spp_range[0]}-{spp_range[1]} x {spp_scale}), "
@@ -628,7 +633,7 @@ def batch_report(ctx, spp_scale, side_range=(256, 2048), spp_range=(16, 256)):
         "paths": paths,
         "batch": {"p50_s": _pct(out.seconds, 0.5), "p99_s": _pct(out.seconds, 0.99), "total_s": out.total_seconds,
                   "mpaths_s": paths / out.total_seconds / 1e6, "graph_replayed": out.graph_replayed,
-                  "tuned": tuned},
+                  "requests_by_launch": launches, "tuned": tuned},
         "one_at_a_time": {"p50_s": _pct(lat, 0.5), "p99_s": _pct(lat, 0.99), "total_s": now,
                           "mpaths_s": paths / now / 1e6},
     }
