@@ -67,6 +67,9 @@ def parse():
     ap.add_argument("--profile-batch", action="store_true",
                     help="profiling helper: one small batch (16 requests of 128-256 px square, 4-16 spp, plain and "
                          "cached, scenes of the 1M-triangle kind), rendered twice through vg_batch_render")
+    ap.add_argument("--profile-batch-wave", action="store_true",
+                    help="profiling helper: the --profile-batch requests through the batch wavefront (size "
+                         "threshold 0), rendered twice through vg_batch_render")
     ap.add_argument("--profile-restir", action="store_true",
                     help="profiling helper: the many-light scene with ReSTIR DI (32 candidates) at 480x270 on the "
                          "streaming wavefront, four frames of one sample")
@@ -713,9 +716,12 @@ def run_cuda(args):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     total = args.warmup + args.steps
 
-    if args.profile_batch:
+    if args.profile_batch or args.profile_batch_wave:
         from verion_gb300 import pack, scenes
-        from verion_gb300.backend import BatchRequest, Cache
+        from verion_gb300.backend import BATCH_SHORTEST_FIRST, BatchRequest, Cache
+
+        if args.profile_batch_wave:
+            ctx.set_batch_options(0, BATCH_SHORTEST_FIRST, 0)
 
         pb = pack.pack(scenes.many_spheres(spheres=16, sphere_n=21, grid=160))
         rb, rcb = Renderer(ctx, pb), Renderer(ctx, pb)

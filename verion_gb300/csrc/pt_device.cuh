@@ -662,6 +662,60 @@ static __device__ __forceinline__ float restirMis(const Surface& surf, V3 woL, V
     return plsa * plsa / fmaxf(plsa * plsa + qb * qb, 1.0e-30f);
 }
 
+// The target function of a ReSTIR candidate, lum(evalReflective(...) * g) * restirMis(...), for many
+// candidates at one shading point: the terms that depend on the outgoing direction alone
+// (G1(wo), the multiple-scattering factor, 4 wo.z) are computed once per shading point, and the
+// reflectance and the reflective pdf share their half vector, GGX density and Fresnel terms. Each
+// value is computed by the same operations in the same order as in evalLobes and reflectivePdf,
+// so the result is theirs bit for bit.
+struct RestirTargetPoint {
+    float g1o, g1oCoat, den;
+    V3 msf;
+};
+
+static __device__ __forceinline__ RestirTargetPoint restirTargetPoint(const Ctx& c, const Surface& s, V3 woL)
+{
+    RestirTargetPoint e;
+    e.g1o = G1(woL.z, s.alpha);
+    e.g1oCoat = s.coat > 0.0f ? G1(woL.z, s.coatAlpha) : 0.0f;
+    e.den = 4.0f * woL.z;
+    e.msf = multiscatterFactor(c, s, woL.z);
+    return e;
+}
+
+static __device__ __forceinline__ float restirTarget(const Surface& s, const RestirTargetPoint& e, V3 woL, V3 wiL, V3 g,
+                                                     float plsa)
+{
+    V3 hh = normalize(woL + wiL);
+    float woh = fmaxf(dot(woL, hh), 0.0f);
+    float t = s.transmission;
+    float dg = Dggx(hh.z, s.alpha) * e.g1o;
+    float fEta = fresnelDielectric(woh, s.eta);
+    // evalLobes
+    float core = dg * G1(wiL.z, s.alpha) / e.den;
+    V3 spec = s.metallic * schlick(s.albedo, woh) * e.msf * core +
+              (1.0f - s.metallic) * (t * fEta * s.tComp + (1.0f - t) * fresnelDielectric(woh, s.ior)) * core;
+    V3 diff = (1.0f - s.metallic) * (1.0f - t) * (1.0f - s.fSel) * s.albedo * (wiL.z / PI);
+    // reflectivePdf
+    float pSpec = s.metallic + (1.0f - s.metallic) * (t * fEta + (1.0f - t) * s.fSel);
+    float pDiff = (1.0f - s.metallic) * (1.0f - t) * (1.0f - s.fSel) * wiL.z / PI;
+    float q = pSpec * (dg / e.den) + pDiff;
+    if (s.sheenP > 0.0f) {
+        spec = (1.0f - s.sheenP) * spec + s.sheenColor * sheenCore(woL.z, wiL.z, hh.z, s.sheenAlpha);
+        diff *= 1.0f - s.sheenP;
+        q = (1.0f - s.sheenP) * q + s.sheenP * wiL.z / PI;
+    }
+    if (s.coat > 0.0f) {
+        float dgC = Dggx(hh.z, s.coatAlpha) * e.g1oCoat;
+        float coreC = dgC * G1(wiL.z, s.coatAlpha) / e.den;
+        spec = (1.0f - s.coatP) * spec + s.coat * fresnelDielectric(woh, 1.5f) * coreC;
+        diff *= 1.0f - s.coatP;
+        q = (1.0f - s.coatP) * q + s.coatP * (dgC / e.den);
+    }
+    float mis = plsa * plsa / fmaxf(plsa * plsa + q * q, 1.0e-30f);
+    return lum((spec + diff) * g) * mis;
+}
+
 struct RestirPick {
     bool valid;
     uint32_t e;
@@ -684,6 +738,7 @@ static __device__ __noinline__ RestirPick restirDI(const Ctx& c, uint32_t pixel,
     V3 selX = v3(0.0f);
     float selPhat = 0.0f;
     const float* E = c.s.emitters;
+    RestirTargetPoint tp = restirTargetPoint(c, surf, woL);
     for (uint32_t k = 0; k < max(c.p[P_RESTIR_CANDIDATES], 1u); k++) {
         float ue = rng.next();
         float ua = rng.next();
@@ -702,7 +757,7 @@ static __device__ __noinline__ RestirPick restirDI(const Ctx& c, uint32_t pixel,
         float phat = 0.0f;
         if (q > 0.0f && restirLight(c, lo, recv, x, p, n, wi, dist, cosi, g, plsa)) {
             V3 wiL = v3(dot(wi, T), dot(wi, B), cosi);
-            phat = lum(evalReflective(c, surf, woL, wiL) * g) * restirMis(surf, woL, wiL, plsa);
+            phat = restirTarget(surf, tp, woL, wiL, g, plsa);
         }
         float wgt = phat / fmaxf(q, 1.0e-30f);
         mTotal += 1.0f;
@@ -745,7 +800,7 @@ static __device__ __noinline__ RestirPick restirDI(const Ctx& c, uint32_t pixel,
             float phat = 0.0f;
             if (restirLight(c, ei - 1, recv, xc, p, n, wi, dist, cosi, g, plsa)) {
                 V3 wiL = v3(dot(wi, T), dot(wi, B), cosi);
-                phat = lum(evalReflective(c, surf, woL, wiL) * g) * restirMis(surf, woL, wiL, plsa);
+                phat = restirTarget(surf, tp, woL, wiL, g, plsa);
             }
             float wgt = phat * X.w * mc;
             mTotal += mc;
