@@ -69,7 +69,7 @@ def parse():
                          "cached, scenes of the 1M-triangle kind), rendered twice through vg_batch_render")
     ap.add_argument("--profile-batch-wave", action="store_true",
                     help="profiling helper: the --profile-batch requests through the batch wavefront (size "
-                         "threshold 0), rendered twice through vg_batch_render")
+                         "threshold 0, host-driven loop), rendered twice through vg_batch_render")
     ap.add_argument("--profile-restir", action="store_true",
                     help="profiling helper: the many-light scene with ReSTIR DI (32 candidates) at 480x270 on the "
                          "streaming wavefront, four frames of one sample")
@@ -721,7 +721,9 @@ def run_cuda(args):
         from verion_gb300.backend import BATCH_SHORTEST_FIRST, BatchRequest, Cache
 
         if args.profile_batch_wave:
+            # The host-driven loop: a profiler cannot look into a graph with a conditional node.
             ctx.set_batch_options(0, BATCH_SHORTEST_FIRST, 0)
+            ctx.set_batch_device_loop(False)
 
         pb = pack.pack(scenes.many_spheres(spheres=16, sphere_n=21, grid=160))
         rb, rcb = Renderer(ctx, pb), Renderer(ctx, pb)

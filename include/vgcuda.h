@@ -402,6 +402,11 @@ int vg_set_batch_options(VgContext* ctx, int blocks_per_sm, int order, uint64_t 
 /* Path slots of the batch wavefront (1024 to 2^26; default 2^21): at most this many pixels are in
  * flight at once. vg_batch_tune picks it. */
 int vg_set_batch_wave_slots(VgContext* ctx, uint32_t slots);
+/* Batch wavefront: run the bounce loop on the device inside the batch's graph (on, the default) or
+ * from the host, one graph launch per two waves with the live count read back after each (off:
+ * for tools that cannot look into graphs with conditional nodes, such as kernel profilers). Same
+ * sums either way. */
+int vg_set_batch_device_loop(VgContext* ctx, int on);
 /* Autotuner: times the batch on scratch accumulations of the requests' sizes for each threshold
  * (0, 256^2, 512^2, 1024^2 pixels, never; one that splits the requests as an earlier one did is
  * skipped), shortest or longest first, the two largest CTA counts per SM that fit (when the tile

@@ -63,12 +63,13 @@ def test_plain_requests_match_megakernel_accumulates(gpu_ctx, order):
 WAVE_SPEC = SPEC + [(3, 64, 48, 3, 32), (3, 37, 29, 2, 64)]
 
 
-@pytest.mark.parametrize("slots,tail", [(1 << 21, 32768), (1024, 64), (1024, 4096)])
-def test_batch_wavefront_matches_megakernel_accumulates(gpu_ctx, slots, tail):
+@pytest.mark.parametrize("slots,tail,device_loop", [(1 << 21, 32768, True), (1024, 64, True), (1024, 4096, True),
+                                                   (1024, 64, False)])
+def test_batch_wavefront_matches_megakernel_accumulates(gpu_ctx, slots, tail, device_loop):
     # Threshold 0: every plain request shares the batch wavefront. The feature zoo has opacity
     # cut-outs (shadow rays through translucent layers in the finish stage). With 1024 slots each
     # slot takes many pixels in turn, through the device-side loop (tail 64) or mostly through the
-    # tail kernel (tail 4096, above the slot count).
+    # tail kernel (tail 4096, above the slot count); the host-driven loop gives the same sums.
     from . import analytic as an
 
     packed = scenes_for_batch() + [pack.pack(an.feature_zoo())]
@@ -82,6 +83,7 @@ def test_batch_wavefront_matches_megakernel_accumulates(gpu_ctx, slots, tail):
         accs.append(r.new_accumulation(w, h))
     gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST, 0)
     gpu_ctx.set_batch_wave_slots(slots)
+    gpu_ctx.set_batch_device_loop(device_loop)
     try:
         reqs = [BatchRequest(r, a, spec[3]) for r, a, spec in zip(rs, accs, WAVE_SPEC)]
         out = gpu_ctx.batch_render(reqs)
@@ -89,6 +91,7 @@ def test_batch_wavefront_matches_megakernel_accumulates(gpu_ctx, slots, tail):
     finally:
         gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST)
         gpu_ctx.set_batch_wave_slots(1 << 21)
+        gpu_ctx.set_batch_device_loop(True)
     assert again.graph_replayed and not out.graph_replayed
     assert all(t > 0 for t in again.seconds) and again.total_seconds >= max(again.seconds)
     for (si, w, h, spp, prec), a in zip(WAVE_SPEC, accs):

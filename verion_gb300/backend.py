@@ -255,6 +255,7 @@ def lib() -> C.CDLL:
             "vg_batch_render": (i32, [vp, vp, _S, vp, C.POINTER(f64), C.POINTER(C.c_int)]),
             "vg_set_batch_options": (i32, [vp, i32, i32, C.c_uint64]),
             "vg_set_batch_wave_slots": (i32, [vp, C.c_uint32]),
+            "vg_set_batch_device_loop": (i32, [vp, i32]),
             "vg_batch_kernel_info": (i32, [vp, vp]),
             "vg_batch_tune": (i32, [vp, vp, _S, C.POINTER(_BatchTune)]),
             "vg_accum_cache_stats": (i32, [vp, C.POINTER(CacheStats)]),
@@ -351,6 +352,10 @@ class Context:
     def set_batch_wave_slots(self, slots: int) -> None:
         """vg_set_batch_wave_slots: path slots of the batch wavefront (pixels in flight at once)."""
         _check(lib().vg_set_batch_wave_slots(self._h, slots))
+
+    def set_batch_device_loop(self, on: bool) -> None:
+        """vg_set_batch_device_loop: the batch wavefront's bounce loop in the graph (True) or on the host."""
+        _check(lib().vg_set_batch_device_loop(self._h, 1 if on else 0))
 
     def batch_tune(self, requests) -> dict:
         """vg_batch_tune: picks the tile launch's CTAs per SM, the item order, the size threshold and the

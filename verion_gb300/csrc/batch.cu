@@ -1,10 +1,28 @@
 // Batched rendering (include/vgcuda.h, "Batched rendering"): the request table, the persistent
 // batch launch (kern_batch.cu) and the caches' training steps, captured once in a CUDA graph and
 // replayed while the batch keeps its shape; and the batch autotuner. No reference counterpart.
+#include <functional>
 #include <numeric>
 
 #include "cache_host.h"
 #include "launch_batch.h"
+
+// The batch wavefront's graphs. Device loop: one graph of the prologue (counters, start kernel), a
+// WHILE node whose body is two waves and the condition kernel, and the epilogue (the tail kernel
+// for batches without caches, the caches' training steps). Host loop (for tools that cannot look
+// into conditional graphs, such as profilers): the prologue, the two-wave body and the epilogue as
+// three graphs, the host reading the live count after each body.
+struct WaveGraphs {
+    cudaGraphExec_t one = nullptr, pro = nullptr, body = nullptr, epi = nullptr;
+    void release()
+    {
+        for (cudaGraphExec_t* g : {&one, &pro, &body, &epi})
+            if (*g) {
+                cudaGraphExecDestroy(*g);
+                *g = nullptr;
+            }
+    }
+};
 
 // The batch wavefront's buffers: the wave planes of `slots` path slots, the request table and the
 // completion state, and its captured graph.
@@ -16,7 +34,7 @@ struct WaveBufs {
     size_t nreq = 0, ncache = 0;
     std::vector<vgb::WaveReq> host;
     std::vector<uint64_t> signature;
-    cudaGraphExec_t graph = nullptr;
+    WaveGraphs* graphs = nullptr;
 };
 
 struct BatchState {
@@ -29,8 +47,10 @@ struct BatchState {
     {
         if (graph)
             cudaGraphExecDestroy(graph);
-        if (wave.graph)
-            cudaGraphExecDestroy(wave.graph);
+        if (wave.graphs) {
+            wave.graphs->release();
+            delete wave.graphs;
+        }
     }
 };
 
@@ -259,49 +279,124 @@ int batch_kernel_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int b
     return VG_OK;
 }
 
-// Builds the batch wavefront's graph: prologue (counters, start kernel), a WHILE node whose body is
-// two waves and the condition kernel, and the tail kernel.
-int bwave_graph(VgContext* ctx, const vgb::WaveBatch& b, const vgk::Wave& w,
-                const std::vector<std::pair<VgCache*, VgRenderer*>>& caches, cudaGraphExec_t* out)
+namespace {
+
+int capture_part(cudaStream_t s, cudaGraph_t* out, const std::function<int()>& launches, const char* what)
+{
+    *out = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess)
+        return cuda_fail(e, what);
+    int st = launches();
+    e = cudaStreamEndCapture(s, out);
+    if (st != VG_OK || e != cudaSuccess) {
+        if (*out)
+            cudaGraphDestroy(*out);
+        *out = nullptr;
+        return st != VG_OK ? st : cuda_fail(e, what);
+    }
+    return VG_OK;
+}
+
+int instantiate(cudaGraph_t g, cudaGraphExec_t* out)
+{
+    cudaError_t e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        return cuda_fail(e, "graph instantiation");
+    }
+    return VG_OK;
+}
+
+} // namespace
+
+int bwave_graphs(VgContext* ctx, const vgb::WaveBatch& b, const vgk::Wave& w,
+                 const std::vector<std::pair<VgCache*, VgRenderer*>>& caches, bool device_loop, WaveGraphs* out)
 {
     cudaStream_t s = ctx->stream;
     int tb = 1, sb = 1;
     vgx::bwave_blocks_per_sm(&tb, &sb);
-    cudaGraph_t g = nullptr, part = nullptr;
+    auto pro = [&]() -> int {
+        cudaError_t ce = cudaMemsetAsync(w.counts, 0, 2 * 4, s);
+        if (ce == cudaSuccess)
+            ce = cudaMemsetAsync(w.fetch, 0, 16 * 4, s);
+        if (ce == cudaSuccess)
+            ce = cudaMemsetAsync(w.scount, 0, 2 * 2 * vgk::SHADE_CLASSES * 4, s);
+        if (ce == cudaSuccess)
+            ce = cudaMemsetAsync(b.err, 0, 4, s);
+        if (ce == cudaSuccess)
+            ce = vgx::bwave_capture_start(s, b, w);
+        return ce == cudaSuccess ? VG_OK : cuda_fail(ce, "graph capture (start)");
+    };
+    auto epi = [&]() -> int {
+        if (caches.empty()) {
+            cudaError_t ce = vgx::bwave_capture_tail(s, b, w);
+            if (ce != cudaSuccess)
+                return cuda_fail(ce, "graph capture (tail)");
+        }
+        for (auto& kc : caches) {
+            VgCache* k = kc.first;
+            VgRenderer* r = kc.second;
+            uint32_t tcap = r->cache_steps * r->cache_batch;
+            for (uint32_t t = 0; t < r->cache_steps; t++) {
+                int st = vgc::cache_train_step(k, (const float*)k->batch_rec.p, (const uint32_t*)k->batch_count.p,
+                                               tcap, t * r->cache_batch, r->cache_batch);
+                if (st != VG_OK)
+                    return st;
+            }
+        }
+        return VG_OK;
+    };
+    cudaGraph_t gp = nullptr, ge = nullptr;
+    int st;
+    if ((st = capture_part(s, &gp, pro, "graph capture")) != VG_OK)
+        return st;
+    if ((st = capture_part(s, &ge, epi, "graph capture")) != VG_OK) {
+        cudaGraphDestroy(gp);
+        return st;
+    }
+    if (!device_loop) {
+        cudaGraph_t gb = nullptr;
+        auto body = [&]() -> int {
+            cudaError_t ce = vgx::bwave_capture_body(s, tb * ctx->sms, sb * ctx->sms, ctx->sms, b, w, 0, false);
+            return ce == cudaSuccess ? VG_OK : cuda_fail(ce, "graph capture (loop body)");
+        };
+        if ((st = capture_part(s, &gb, body, "graph capture")) != VG_OK) {
+            cudaGraphDestroy(gp);
+            cudaGraphDestroy(ge);
+            return st;
+        }
+        if ((st = instantiate(gp, &out->pro)) != VG_OK) {
+            cudaGraphDestroy(gb);
+            cudaGraphDestroy(ge);
+            return st;
+        }
+        if ((st = instantiate(gb, &out->body)) != VG_OK) {
+            cudaGraphDestroy(ge);
+            return st;
+        }
+        return instantiate(ge, &out->epi);
+    }
+    cudaGraph_t g = nullptr;
     cudaGraphNode_t n0 = nullptr, n1 = nullptr, n2 = nullptr;
     cudaGraphConditionalHandle loop = 0;
-    cudaError_t e = cudaGraphCreate(&g, 0);
     auto done = [&](cudaError_t err, const char* what) -> int {
-        if (part)
-            cudaGraphDestroy(part);
+        if (gp)
+            cudaGraphDestroy(gp);
+        if (ge)
+            cudaGraphDestroy(ge);
         if (g)
             cudaGraphDestroy(g);
         return cuda_fail(err, what);
     };
+    cudaError_t e = cudaGraphCreate(&g, 0);
     if (e != cudaSuccess)
-        return cuda_fail(e, "graph creation");
+        return done(e, "graph creation");
     if ((e = cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess)
         return done(e, "graph condition");
-    // Prologue.
-    if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed)) != cudaSuccess)
-        return done(e, "graph capture");
-    cudaError_t ce = cudaMemsetAsync(w.counts, 0, 2 * 4, s);
-    if (ce == cudaSuccess)
-        ce = cudaMemsetAsync(w.fetch, 0, 16 * 4, s);
-    if (ce == cudaSuccess)
-        ce = cudaMemsetAsync(w.scount, 0, 2 * 2 * vgk::SHADE_CLASSES * 4, s);
-    if (ce == cudaSuccess)
-        ce = cudaMemsetAsync(b.err, 0, 4, s);
-    if (ce == cudaSuccess)
-        ce = vgx::bwave_capture_start(s, b, w);
-    e = cudaStreamEndCapture(s, &part);
-    if (ce != cudaSuccess || e != cudaSuccess)
-        return done(ce != cudaSuccess ? ce : e, "graph capture (start)");
-    if ((e = cudaGraphAddChildGraphNode(&n0, g, nullptr, 0, part)) != cudaSuccess)
+    if ((e = cudaGraphAddChildGraphNode(&n0, g, nullptr, 0, gp)) != cudaSuccess)
         return done(e, "graph node");
-    cudaGraphDestroy(part);
-    part = nullptr;
-    // The bounce loop.
     cudaGraphNodeParams cp{};
     cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = loop;
@@ -312,45 +407,16 @@ int bwave_graph(VgContext* ctx, const vgb::WaveBatch& b, const vgk::Wave& w,
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     if ((e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed)) != cudaSuccess)
         return done(e, "graph capture");
-    ce = vgx::bwave_capture_body(s, tb * ctx->sms, sb * ctx->sms, ctx->sms, b, w, loop);
+    cudaError_t ce = vgx::bwave_capture_body(s, tb * ctx->sms, sb * ctx->sms, ctx->sms, b, w, loop, true);
     e = cudaStreamEndCapture(s, &body);
     if (ce != cudaSuccess || e != cudaSuccess)
         return done(ce != cudaSuccess ? ce : e, "graph capture (loop body)");
-    // Tail (batches without caches; with caches the loop runs until no slot is live), then the
-    // caches' training steps on the batch's training records.
-    if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed)) != cudaSuccess)
-        return done(e, "graph capture");
-    ce = caches.empty() ? vgx::bwave_capture_tail(s, b, w) : cudaSuccess;
-    int st = VG_OK;
-    for (auto& kc : caches) {
-        VgCache* k = kc.first;
-        VgRenderer* r = kc.second;
-        uint32_t tcap = r->cache_steps * r->cache_batch;
-        for (uint32_t t = 0; t < r->cache_steps && st == VG_OK; t++)
-            st = vgc::cache_train_step(k, (const float*)k->batch_rec.p, (const uint32_t*)k->batch_count.p, tcap,
-                                       t * r->cache_batch, r->cache_batch);
-    }
-    e = cudaStreamEndCapture(s, &part);
-    if (st != VG_OK) {
-        if (part)
-            cudaGraphDestroy(part);
-        cudaGraphDestroy(g);
-        return st;
-    }
-    if (ce != cudaSuccess || e != cudaSuccess)
-        return done(ce != cudaSuccess ? ce : e, "graph capture (tail)");
-    if ((e = cudaGraphAddChildGraphNode(&n2, g, &n1, 1, part)) != cudaSuccess)
+    if ((e = cudaGraphAddChildGraphNode(&n2, g, &n1, 1, ge)) != cudaSuccess)
         return done(e, "graph node");
-    cudaGraphDestroy(part);
-    part = nullptr;
-    e = cudaGraphInstantiate(out, g, 0);
-    cudaGraphDestroy(g);
-    g = nullptr;
-    if (e != cudaSuccess) {
-        *out = nullptr;
-        return cuda_fail(e, "graph instantiation");
-    }
-    return VG_OK;
+    cudaGraphDestroy(gp);
+    cudaGraphDestroy(ge);
+    gp = ge = nullptr;
+    return instantiate(g, &out->one);
 }
 
 // Requests on the batch wavefront (kern_bwave.cu), in `order`; the graph is captured the first time
@@ -569,21 +635,36 @@ int batch_wave_run(VgContext* ctx, const VgBatchRequest* reqs, size_t n, int ord
         VG_CHECK(cudaMemsetAsync(kc.first->batch_count.p, 0, 4, s), "training count");
         VG_CHECK(cudaMemsetAsync(kc.first->err.p, 0, 4, s), "cache error flag");
     }
-    bool reuse = B.graph && sig == B.signature;
+    sig.push_back(ctx->batch_device_loop ? 1 : 0);
+    if (!B.graphs)
+        B.graphs = new WaveGraphs();
+    bool reuse = (B.graphs->one || B.graphs->pro) && sig == B.signature;
     if (!reuse) {
-        if (B.graph) {
-            cudaGraphExecDestroy(B.graph);
-            B.graph = nullptr;
-        }
+        B.graphs->release();
         B.signature.clear();
-        if ((st = bwave_graph(ctx, b, w, caches, &B.graph)) != VG_OK)
+        if ((st = bwave_graphs(ctx, b, w, caches, ctx->batch_device_loop, B.graphs)) != VG_OK) {
+            B.graphs->release();
             return st;
+        }
         B.signature = sig;
     }
     EventPool pool;
     cudaEvent_t e0 = pool.get(), e1 = pool.get();
     VG_CHECK(cudaEventRecord(e0, s), "event");
-    VG_CHECK(cudaGraphLaunch(B.graph, s), "graph launch");
+    if (ctx->batch_device_loop) {
+        VG_CHECK(cudaGraphLaunch(B.graphs->one, s), "graph launch");
+    } else {
+        VG_CHECK(cudaGraphLaunch(B.graphs->pro, s), "graph launch");
+        for (uint32_t it = 0; it < b.max_iter; it++) {
+            VG_CHECK(cudaGraphLaunch(B.graphs->body, s), "graph launch");
+            uint32_t live = 0;
+            VG_CHECK(cudaMemcpyAsync(&live, w.counts, 4, cudaMemcpyDeviceToHost, s), "live count");
+            VG_CHECK(cudaStreamSynchronize(s), "live count");
+            if (live <= b.tail)
+                break;
+        }
+        VG_CHECK(cudaGraphLaunch(B.graphs->epi, s), "graph launch");
+    }
     VG_CHECK(cudaEventRecord(e1, s), "event");
     if ((st = wait_event(e1)) != VG_OK)
         return st;
@@ -730,6 +811,14 @@ int vg_set_batch_options(VgContext* ctx, int blocks_per_sm, int order, uint64_t 
     ctx->batch_blocks_per_sm = blocks_per_sm;
     ctx->batch_order = order;
     ctx->batch_wavefront_pixels = wavefront_pixels;
+    return VG_OK;
+}
+
+int vg_set_batch_device_loop(VgContext* ctx, int on)
+{
+    if (!ctx)
+        return fail(VG_ERR_INVALID, "null context");
+    ctx->batch_device_loop = on != 0;
     return VG_OK;
 }
 

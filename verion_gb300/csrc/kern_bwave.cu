@@ -613,7 +613,7 @@ cudaError_t bwave_capture_start(cudaStream_t s, const vgb::WaveBatch& b, const v
 }
 
 cudaError_t bwave_capture_body(cudaStream_t s, int trace_blocks, int shade_blocks, int sms, const vgb::WaveBatch& b,
-                               const vgk::Wave& w, cudaGraphConditionalHandle loop)
+                               const vgk::Wave& w, cudaGraphConditionalHandle loop, bool condition)
 {
     for (uint32_t wave = 0; wave < 2; wave++) {
         bw_extend<<<trace_blocks, 128, 0, s>>>(b, w, wave);
@@ -626,7 +626,8 @@ cudaError_t bwave_capture_body(cudaStream_t s, int trace_blocks, int shade_block
         if (b.ncache)
             bw_answer<<<sms * 2, 128, ANSWER_SMEM, s>>>(b);
     }
-    bw_condition<<<1, 1, 0, s>>>(b, w, loop);
+    if (condition)
+        bw_condition<<<1, 1, 0, s>>>(b, w, loop);
     return cudaGetLastError();
 }
 

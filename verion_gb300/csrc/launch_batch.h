@@ -16,10 +16,11 @@ cudaError_t launch_batch(int blocks, cudaStream_t s, const vgb::BatchReq* reqs, 
                          uint32_t* next, vgb::BatchDone* done, uint32_t* err, unsigned long long* t0);
 
 // The batch wavefront (kern_bwave.cu), launched inside stream capture: the start kernel; the loop
-// body (two waves and the kernel that sets the WHILE node's condition `loop`); the tail kernel.
+// body (two waves, and with `condition` the kernel that sets the WHILE node's condition `loop`);
+// the tail kernel.
 cudaError_t bwave_capture_start(cudaStream_t s, const vgb::WaveBatch& b, const vgk::Wave& w);
 cudaError_t bwave_capture_body(cudaStream_t s, int trace_blocks, int shade_blocks, int sms, const vgb::WaveBatch& b,
-                               const vgk::Wave& w, cudaGraphConditionalHandle loop);
+                               const vgk::Wave& w, cudaGraphConditionalHandle loop, bool condition);
 cudaError_t bwave_capture_tail(cudaStream_t s, const vgb::WaveBatch& b, const vgk::Wave& w);
 // Resident 128-thread blocks per SM of the batch wavefront's traversal and shade stages.
 void bwave_blocks_per_sm(int* trace, int* shade);
