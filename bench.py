@@ -66,7 +66,8 @@ def parse():
                          "timed launch of each (encode, inference, training pass, scatter); prints their times")
     ap.add_argument("--profile-batch", action="store_true",
                     help="profiling helper: one small batch (16 requests of 128-256 px square, 4-16 spp, plain and "
-                         "cached, scenes of the 1M-triangle kind), rendered twice through vg_batch_render")
+                         "cached, scenes of the 1M-triangle kind) on the tile launch, rendered twice through "
+                         "vg_batch_render")
     ap.add_argument("--profile-batch-wave", action="store_true",
                     help="profiling helper: the --profile-batch requests through the batch wavefront (size "
                          "threshold 0, host-driven loop), rendered twice through vg_batch_render")
@@ -724,6 +725,8 @@ def run_cuda(args):
             # The host-driven loop: a profiler cannot look into a graph with a conditional node.
             ctx.set_batch_options(0, BATCH_SHORTEST_FIRST, 0)
             ctx.set_batch_device_loop(False)
+        else:
+            ctx.set_batch_options(0, BATCH_SHORTEST_FIRST, (1 << 64) - 1)  # the tile launch
 
         pb = pack.pack(scenes.many_spheres(spheres=16, sphere_n=21, grid=160))
         rb, rcb = Renderer(ctx, pb), Renderer(ctx, pb)

@@ -396,8 +396,8 @@ int vg_batch_render(VgContext* ctx, const VgBatchRequest* requests, size_t n, Vg
  * shared bytes, and the CUDA status of the occupancy query, in that order. */
 int vg_batch_kernel_info(VgContext* ctx, int out[5]);
 /* Batch kernel CTAs per SM (0: as many as fit), the item order, and the size (pixels) from which a
- * request leaves the tile launch: plain requests for the batch wavefront, cached ones for their own
- * run (~0: never; 0: all of them; default 512 x 512). vg_batch_tune picks all three. */
+ * request leaves the tile launch for the batch wavefront (~0: never; default 0: every request on
+ * the batch wavefront, the faster on both measured mixes). vg_batch_tune picks all three. */
 int vg_set_batch_options(VgContext* ctx, int blocks_per_sm, int order, uint64_t wavefront_pixels);
 /* Path slots of the batch wavefront (1024 to 2^26; default 2^21): at most this many pixels are in
  * flight at once. vg_batch_tune picks it. */

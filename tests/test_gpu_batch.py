@@ -19,6 +19,8 @@ def scenes_for_batch():
             pack.pack(scenes.many_spheres(hdri=(64, 32)))]
 
 
+TILES_ONLY = (1 << 64) - 1  # size threshold: every request on the tile launch
+
 SPEC = [(0, 40, 30, 8, 32), (1, 17, 13, 3, 64), (2, 48, 27, 2, 32), (0, 96, 64, 4, 64), (2, 33, 71, 3, 64),
         (1, 128, 96, 1, 32)]
 
@@ -38,7 +40,7 @@ def make(ctx, packed):
 def test_plain_requests_match_megakernel_accumulates(gpu_ctx, order):
     packed = scenes_for_batch()
     rs, accs = make(gpu_ctx, packed)
-    gpu_ctx.set_batch_options(0, order)
+    gpu_ctx.set_batch_options(0, order, TILES_ONLY)
     reqs = [BatchRequest(r, a, spec[3]) for r, a, spec in zip(rs, accs, SPEC)]
     out = gpu_ctx.batch_render(reqs)
     again = gpu_ctx.batch_render(reqs)  # same shape: the captured graph is replayed
@@ -198,8 +200,11 @@ def test_shortest_first_finishes_small_requests_early(gpu_ctx):
     r.set_max_depth(16)
     sizes = [(32, 32, 1), (256, 256, 4), (64, 64, 2), (512, 256, 4)]
     reqs = [BatchRequest(r, r.new_accumulation(w, h), spp) for w, h, spp in sizes]
-    gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST)
-    out = gpu_ctx.batch_render(reqs)
+    gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST, TILES_ONLY)
+    try:
+        out = gpu_ctx.batch_render(reqs)
+    finally:
+        gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST)
     assert out.seconds[0] < out.seconds[1] and out.seconds[0] < out.seconds[3]
     assert max(out.seconds) == out.seconds[3]
 
@@ -217,7 +222,11 @@ def test_cached_request_matches_the_cache_integrator_without_training(gpu_ctx):
     r2.set_cache(c2, spread=0.01, train_paths=256, train_steps=0, train_batch=1024)
     a2 = r2.new_accumulation(w, h)
     plain = r2.new_accumulation(w, h)
-    out = gpu_ctx.batch_render([BatchRequest(r2, a2, spp, c2), BatchRequest(r2, plain, 2)])
+    gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST, TILES_ONLY)
+    try:
+        out = gpu_ctx.batch_render([BatchRequest(r2, a2, spp, c2), BatchRequest(r2, plain, 2)])
+    finally:
+        gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST)
     assert len(out.seconds) == 2
     assert np.array_equal(a2.sums_f64(), a1.sums_f64())
 
@@ -228,7 +237,11 @@ def test_cached_requests_train_their_cache(gpu_ctx):
     cache = Cache(gpu_ctx, bounds=r.bounds())
     r.set_cache(cache, spread=0.01, train_paths=1024, train_steps=2, train_batch=4096)
     before, _ = cache.read_params()
-    gpu_ctx.batch_render([BatchRequest(r, r.new_accumulation(64, 64), 2, cache)])
+    gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST, TILES_ONLY)
+    try:
+        gpu_ctx.batch_render([BatchRequest(r, r.new_accumulation(64, 64), 2, cache)])
+    finally:
+        gpu_ctx.set_batch_options(0, BATCH_SHORTEST_FIRST)
     after, _ = cache.read_params()
     assert not np.array_equal(before, after)
 

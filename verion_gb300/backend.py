@@ -346,7 +346,7 @@ class Context:
         _check(lib().vg_batch_kernel_info(self._h, v))
         return dict(zip(("blocks_per_sm", "registers", "local_bytes", "static_smem", "cuda_status"), list(v)))
 
-    def set_batch_options(self, blocks_per_sm: int = 0, order: int = 0, wavefront_pixels: int = 512 * 512) -> None:
+    def set_batch_options(self, blocks_per_sm: int = 0, order: int = 0, wavefront_pixels: int = 0) -> None:
         _check(lib().vg_set_batch_options(self._h, blocks_per_sm, order, wavefront_pixels))
 
     def set_batch_wave_slots(self, slots: int) -> None:

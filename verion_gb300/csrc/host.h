@@ -162,7 +162,7 @@ struct VgContext {
     BatchState* batch = nullptr;
     int batch_blocks_per_sm = 0; // 0: as many as fit (vg_batch_tune chooses)
     int batch_order = 0;         // VgBatchOrder
-    uint64_t batch_wavefront_pixels = 512 * 512; // requests at least this large share the batch wavefront
+    uint64_t batch_wavefront_pixels = 0;          // requests at least this large share the batch wavefront
     uint32_t batch_wave_slots = 1u << 21;         // path slots of the batch wavefront
     bool batch_device_loop = true;                // batch wavefront: bounce loop in the graph (else the host's)
     cudaStream_t side = nullptr;                 // second stream (created on first use): cache training paths
