@@ -15,12 +15,6 @@
 #include "bvh8.h"
 #include "vec3.h"
 
-// Postponed leaf testing in the dynamic-fetch traversal (trace_queue; an A/B build switch, off
-// by default).
-#ifndef VG_TRI_POSTPONE
-#define VG_TRI_POSTPONE 0
-#endif
-
 namespace vgt {
 
 struct TRay {
@@ -290,43 +284,7 @@ struct Walk {
     uint32_t node;
     int sp;
     TraceHit h;
-#if VG_TRI_POSTPONE
-    uint32_t pbits, pbase; // postponed leaf triangles (bits from pbase)
-    bool ndone;            // no node left to visit
-#endif
 };
-
-// Triangles `bits` (from `base`) of the walk's ray; returns true for an any hit.
-template <bool ANY>
-__device__ __forceinline__ bool walk_tris(const float4* __restrict__ tris, Walk& w, uint32_t bits, uint32_t base)
-{
-    const TRay& r = w.r;
-    while (bits) {
-        uint32_t j = __ffs(bits) - 1;
-        bits &= bits - 1;
-        const float4* tp = tris + (size_t)(base + j) * bvh8::TRI_VEC4;
-        float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-        float t, U, V, W, det;
-        w.h.tests++;
-        if (tri_test(r, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), v3(c.x, c.y, c.z), t, U, V, W, det)) {
-            uint32_t gid = __float_as_uint(c.w);
-            bool take = ANY ? t < w.tmax : (t < w.tmax || (w.h.hit && t == w.tmax && gid < w.h.gid));
-            if (take) {
-                w.h.hit = true;
-                w.h.t = t;
-                w.tmax = ANY ? w.tmax : t;
-                w.h.gid = gid;
-                w.h.inst = __float_as_uint(a.w);
-                w.h.prim = __float_as_uint(b.w);
-                w.h.b1 = V / det;
-                w.h.b2 = W / det;
-                if (ANY)
-                    return true;
-            }
-        }
-    }
-    return false;
-}
 
 // One node visit: box tests, the node's triangles, then the next node. Returns true when the walk
 // has finished (stack empty, or any-hit found).
@@ -694,10 +652,6 @@ __device__ __forceinline__ void trace_queue_impl(const uint4* __restrict__ nodes
                         w.h.t = tmax;
                         w.node = 0;
                         w.sp = 0;
-#if VG_TRI_POSTPONE
-                        w.pbits = 0;
-                        w.ndone = false;
-#endif
                         active = true;
                     } else {
                         w.h.t = tmax;
@@ -711,47 +665,6 @@ __device__ __forceinline__ void trace_queue_impl(const uint4* __restrict__ nodes
                 break;
             continue;
         }
-#if VG_TRI_POSTPONE
-        // Postponed leaf testing: a lane keeps the triangles of one visited leaf set pending and
-        // goes on with its nodes; the warp tests the pending sets together once at least half of
-        // its active lanes hold one, or when a lane has no node left. A lane that meets a second
-        // leaf set while one is pending tests the new one at once. Box tests meanwhile use the
-        // older tmax, so they visit a superset of the nodes, and the hit is the same.
-#pragma unroll 1
-        for (uint32_t s = 0; s < steps; s++) {
-            bool fin = false;
-            if (active && !w.ndone) {
-                const uint4* np = nodes + (size_t)w.node * bvh8::NODE_VEC4;
-                uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
-                w.h.nodes++;
-                uint32_t imask = w0.w >> 24;
-                uint32_t inner_hits, tri_bits;
-                node_test(w.r, w0, w2, w3, w4, imask, w1.z, w1.w, w.tmax, inner_hits, tri_bits);
-                if (tri_bits) {
-                    if (w.pbits == 0) {
-                        w.pbits = tri_bits;
-                        w.pbase = w1.y;
-                    } else {
-                        fin = walk_tris<ANY>(tris, w, tri_bits, w1.y);
-                    }
-                }
-                if (!fin)
-                    w.ndone = next_node(w, inner_hits, w1.x, imask, stack, err);
-            }
-            bool pend = active && !fin && w.pbits != 0;
-            uint32_t pm = __ballot_sync(FULLM, pend);
-            uint32_t am = __ballot_sync(FULLM, active && !fin);
-            bool must = __ballot_sync(FULLM, pend && w.ndone) != 0;
-            if (pend && (must || 2u * (uint32_t)__popc(pm) >= (uint32_t)__popc(am))) {
-                fin = walk_tris<ANY>(tris, w, w.pbits, w.pbase);
-                w.pbits = 0;
-            }
-            if (active && (fin || (w.ndone && w.pbits == 0))) {
-                put(w.item, w.h);
-                active = false;
-            }
-        }
-#else
         if (active) {
 #pragma unroll 1
             for (uint32_t s = 0; s < steps; s++) {
@@ -762,7 +675,6 @@ __device__ __forceinline__ void trace_queue_impl(const uint4* __restrict__ nodes
                 }
             }
         }
-#endif
     }
 }
 
