@@ -55,13 +55,23 @@ static __device__ __forceinline__ void plain_tile(const Ctx& c, uint32_t x, uint
     if (!inside)
         return;
     uint32_t pixel = y * c.p[P_WIDTH] + x;
-    for (uint32_t k = 0; k < c.p[P_SAMPLES_PER_DISPATCH]; k++) {
-        PathState<false> st = generatePathFor<false>(c, x, y, c.p[P_SAMPLE] + k);
-        for (uint32_t depth = 0; depth < c.p[P_MAX_DEPTH]; depth++) {
-            if (!shadePathCall<false, false>(c, st, traceClosest(c, st.org, st.dir), depth, pixel))
-                break;
+    uint32_t n = c.p[P_SAMPLES_PER_DISPATCH];
+    if (n == 0)
+        return;
+    // One loop over bounces, a path's end starting the pixel's next sample (mk_pathtrace).
+    uint32_t k = 0, depth = 0;
+    PathState<false> st = generatePathFor<false>(c, x, y, c.p[P_SAMPLE]);
+    for (;;) {
+        if (shadePathCall<false, false>(c, st, traceClosest(c, st.org, st.dir), depth, pixel) &&
+            depth + 1 < c.p[P_MAX_DEPTH]) {
+            depth++;
+            continue;
         }
         finishPath<false, A>(c, st, pixel);
+        if (++k >= n)
+            break;
+        depth = 0;
+        st = generatePathFor<false>(c, x, y, c.p[P_SAMPLE] + k);
     }
 }
 

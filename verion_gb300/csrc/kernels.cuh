@@ -174,7 +174,11 @@ __device__ __forceinline__ PathState<LIGHT> loadPath(const Ctx& c, const Wave& w
     return s;
 }
 
-// pathtrace.slang:9-26: one thread per pixel, params[35] samples from params[6].
+// pathtrace.slang:9-26: one thread per pixel, params[35] samples from params[6]. One loop over
+// bounces: a lane whose path ends adds it and starts its pixel's next sample in the same
+// iteration, so the warp's lanes stay on bounce work until they run out of samples instead of
+// waiting at the end of each sample for the warp's longest path. Same samples, same order per
+// pixel, same sums.
 template <bool LIGHT, bool RESTIR, typename A>
 __global__ void __launch_bounds__(128) mk_pathtrace(const __grid_constant__ Ctx c)
 {
@@ -183,15 +187,22 @@ __global__ void __launch_bounds__(128) mk_pathtrace(const __grid_constant__ Ctx 
     if (x >= c.p[P_WIDTH] || y >= c.p[P_HEIGHT])
         return;
     uint32_t pixel = y * c.p[P_WIDTH] + x;
-    for (uint32_t k = 0; k < c.p[P_SAMPLES_PER_DISPATCH]; k++) {
-        if (c.p[P_ADAPTIVE] != 0 && !pixelActive<A>(c, pixel))
-            return;
-        PathState<LIGHT> st = generatePathFor<LIGHT>(c, x, y, c.p[P_SAMPLE] + k);
-        for (uint32_t depth = 0; depth < c.p[P_MAX_DEPTH]; depth++) {
-            if (!shadePathCall<LIGHT, RESTIR>(c, st, traceClosest(c, st.org, st.dir), depth, pixel))
-                break;
+    uint32_t n = c.p[P_SAMPLES_PER_DISPATCH];
+    if (n == 0 || (c.p[P_ADAPTIVE] != 0 && !pixelActive<A>(c, pixel)))
+        return;
+    uint32_t k = 0, depth = 0;
+    PathState<LIGHT> st = generatePathFor<LIGHT>(c, x, y, c.p[P_SAMPLE]);
+    for (;;) {
+        if (shadePathCall<LIGHT, RESTIR>(c, st, traceClosest(c, st.org, st.dir), depth, pixel) &&
+            depth + 1 < c.p[P_MAX_DEPTH]) {
+            depth++;
+            continue;
         }
         finishPath<LIGHT, A, RESTIR>(c, st, pixel);
+        if (++k >= n || (c.p[P_ADAPTIVE] != 0 && !pixelActive<A>(c, pixel)))
+            break;
+        depth = 0;
+        st = generatePathFor<LIGHT>(c, x, y, c.p[P_SAMPLE] + k);
     }
 }
 
