@@ -44,6 +44,7 @@ using vgb::WaveReq;
 // Shading classes: the four material classes of a plain request's slot, then the same four of a
 // cached request's slot (shaded by the cache instantiation of bw_shade).
 constexpr uint32_t BW_CLASSES = 2 * SHADE_CLASSES;
+static_assert(sizeof(WaveReq) % 16 == 0 && sizeof(WaveCache) % 16 == 0, "request and cache tables are 16-byte records");
 constexpr uint32_t ANSWER_SMEM = IMG_FWD_BYTES + 16384 + 1024;
 
 // Training pixel test of a cached request's sample (mk_cache_train's, per sample).
