@@ -71,6 +71,10 @@ def parse():
     ap.add_argument("--profile-batch-wave", action="store_true",
                     help="profiling helper: the --profile-batch requests through the batch wavefront (size "
                          "threshold 0, host-driven loop), rendered twice through vg_batch_render")
+    ap.add_argument("--profile-per-sample", action="store_true",
+                    help="profiling helper: the benchmark scene at --width x --height on the per-sample wavefront "
+                         "(the reference's depth-by-depth order: wf_begin / wf_select / wf_extend / wf_shade), "
+                         "adaptive (0.02, 16), 20 samples in one accumulate call")
     ap.add_argument("--profile-restir", action="store_true",
                     help="profiling helper: the many-light scene with ReSTIR DI (32 candidates) at 480x270 on the "
                          "streaming wavefront, four frames of one sample")
@@ -744,6 +748,20 @@ def run_cuda(args):
                 reqs.append(BatchRequest(rr, rr.new_accumulation(side, side), spp, cb if i % 2 else None))
             out = ctx.batch_render(reqs)
         print(json.dumps({"batch_total_s": out.total_seconds}), flush=True)
+        return
+
+    if args.profile_per_sample:
+        from verion_gb300.backend import WavefrontMode
+
+        rp = Renderer(ctx, packed)
+        rp.set_integrator(Integrator.WAVEFRONT)
+        rp.set_wavefront_mode(WavefrontMode.PER_SAMPLE)
+        rp.set_max_depth(DEPTH)
+        rp.set_adaptive(Adaptive(*ADAPTIVE))
+        rp.set_accum_precision(64)
+        acc_p = rp.new_accumulation(WIDTH, HEIGHT)
+        rp.accumulate(acc_p, 20)
+        print(json.dumps({"per_sample_ms": 1e3 * acc_p.gpu_seconds()}), flush=True)
         return
 
     if args.profile_restir:
