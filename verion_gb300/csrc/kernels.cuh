@@ -179,8 +179,18 @@ __device__ __forceinline__ PathState<LIGHT> loadPath(const Ctx& c, const Wave& w
 // iteration, so the warp's lanes stay on bounce work until they run out of samples instead of
 // waiting at the end of each sample for the warp's longest path. Same samples, same order per
 // pixel, same sums.
+// Minimum resident 128-thread blocks per SM requested for the megakernel (a register cap; 0: none).
+#ifndef VG_MK_MIN_BLOCKS
+#define VG_MK_MIN_BLOCKS 0
+#endif
+#if VG_MK_MIN_BLOCKS > 0
+#define VG_MK_BOUNDS __launch_bounds__(128, VG_MK_MIN_BLOCKS)
+#else
+#define VG_MK_BOUNDS __launch_bounds__(128)
+#endif
+
 template <bool LIGHT, bool RESTIR, typename A>
-__global__ void __launch_bounds__(128) mk_pathtrace(const __grid_constant__ Ctx c)
+__global__ void VG_MK_BOUNDS mk_pathtrace(const __grid_constant__ Ctx c)
 {
     uint32_t x = blockIdx.x * 16 + (threadIdx.x & 15u);
     uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 4);
