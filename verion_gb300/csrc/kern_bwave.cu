@@ -560,7 +560,7 @@ __global__ void bw_condition(WaveBatch b, Wave w, cudaGraphConditionalHandle loo
 // The tail: one thread per live slot (a grid-stride loop over queue 0) runs its path, the rest of
 // its pixel's samples and then further work items to the end, trace and shade in a loop as the
 // megakernel does.
-__global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) bw_tail(WaveBatch b, Wave w)
+__global__ void __launch_bounds__(128, VG_TAIL_MIN_BLOCKS) bw_tail(WaveBatch b, Wave w)
 {
     uint32_t count = w.counts[0];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {

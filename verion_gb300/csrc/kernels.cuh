@@ -32,6 +32,11 @@ constexpr uint32_t FULL = 0xffffffffu;
 #ifndef VG_RESTIR_SHADE_MIN_BLOCKS
 #define VG_RESTIR_SHADE_MIN_BLOCKS 6
 #endif
+// The same for the kernels that run whole paths per thread through the out-of-line shadePathCall
+// (the streaming tail, the batch wavefront's tail).
+#ifndef VG_TAIL_MIN_BLOCKS
+#define VG_TAIL_MIN_BLOCKS VG_SHADE_MIN_BLOCKS
+#endif
 
 // State planes (16 bytes each, plane k of path p at state[k * N + p]):
 //   0 (org.xyz, rng)  1 (dir.xyz, flags)  2 (thr.xyz, pathLen)  3 (total.xyz, qPrev)
@@ -180,8 +185,12 @@ __device__ __forceinline__ PathState<LIGHT> loadPath(const Ctx& c, const Wave& w
 // waiting at the end of each sample for the warp's longest path. Same samples, same order per
 // pixel, same sums.
 // Minimum resident 128-thread blocks per SM requested for the megakernel (a register cap; 0: none).
+// Its threads spend most of their time waiting on dependent node loads in the traversal, so
+// occupancy pays more than registers: on the 1M-triangle workload at 1080p, 72.8 Mpaths/s with no
+// cap (168 registers, 3 blocks per SM), 88.9 at 8 blocks (64 registers), 102.4 at 12, 114.1 at 16
+// (32 registers, every warp slot of the SM; the spilled values are few and L1-resident).
 #ifndef VG_MK_MIN_BLOCKS
-#define VG_MK_MIN_BLOCKS 0
+#define VG_MK_MIN_BLOCKS 16
 #endif
 #if VG_MK_MIN_BLOCKS > 0
 #define VG_MK_BOUNDS __launch_bounds__(128, VG_MK_MIN_BLOCKS)
@@ -823,7 +832,7 @@ __global__ void __launch_bounds__(128, 8) wf_stream_finish(const __grid_constant
 // instead of one half-empty wave per bounce. Same functions, same order per pixel, same sums.
 // With CACHE (lighting split off) paths end at the cache as in wf_stream_shade_deferred.
 template <bool LIGHT, typename A, bool CACHE = false, bool RESTIR = false>
-__global__ void __launch_bounds__(128, VG_SHADE_MIN_BLOCKS) wf_stream_tail(const __grid_constant__ Ctx c, Wave w,
+__global__ void __launch_bounds__(128, VG_TAIL_MIN_BLOCKS) wf_stream_tail(const __grid_constant__ Ctx c, Wave w,
                                                                           uint32_t wave, CacheWave q)
 {
     static_assert(!(CACHE && LIGHT), "the cache runs with the lighting split off");
