@@ -23,14 +23,15 @@ using namespace vgd;
 constexpr uint32_t FULL = 0xffffffffu;
 
 // Minimum resident 128-thread blocks per SM requested for the shade kernels (a register cap), and
-// for the deferred shade stage's ReSTIR instantiations, whose candidate loop waits on memory: 6
-// blocks there took the many-light ReSTIR frame from 7.89 to 7.43 ms (5 or 6 for the plain stage
-// are slower than 4).
+// for the deferred shade stage's ReSTIR instantiations, whose candidate loop waits on memory: on
+// the many-light ReSTIR frame 4 blocks gave 7.89 ms, 6 blocks 7.43 (then 7.01 with the shared
+// candidate target terms), 10 blocks 6.76, 12 blocks 6.72, 16 blocks 6.90. The plain stage keeps
+// 4: 5, 6, 8 or 16 blocks are slower (its inlined shadePath spills heavily below 128 registers).
 #ifndef VG_SHADE_MIN_BLOCKS
 #define VG_SHADE_MIN_BLOCKS 4
 #endif
 #ifndef VG_RESTIR_SHADE_MIN_BLOCKS
-#define VG_RESTIR_SHADE_MIN_BLOCKS 6
+#define VG_RESTIR_SHADE_MIN_BLOCKS 12
 #endif
 // The same for the kernels that run whole paths per thread through the out-of-line shadePathCall
 // (the streaming tail, the batch wavefront's tail).
