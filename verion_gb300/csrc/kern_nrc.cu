@@ -500,8 +500,19 @@ static __device__ __forceinline__ bool is_train_pixel(const NrcPathArgs& a, uint
     return (pixel + a.train_offset) % a.train_stride == 0;
 }
 
+// Minimum resident 128-thread blocks per SM requested for the whole-path kernels of the cache
+// integrator (a register cap; 0: none), as for the megakernel.
+#ifndef VG_CACHE_PATH_MIN_BLOCKS
+#define VG_CACHE_PATH_MIN_BLOCKS 0
+#endif
+#if VG_CACHE_PATH_MIN_BLOCKS > 0
+#define VG_CACHE_PATH_BOUNDS __launch_bounds__(128, VG_CACHE_PATH_MIN_BLOCKS)
+#else
+#define VG_CACHE_PATH_BOUNDS __launch_bounds__(128)
+#endif
+
 template <typename A>
-__global__ void __launch_bounds__(128) mk_cache_query(const __grid_constant__ Ctx c, NrcPathArgs a)
+__global__ void VG_CACHE_PATH_BOUNDS mk_cache_query(const __grid_constant__ Ctx c, NrcPathArgs a)
 {
     uint32_t x = blockIdx.x * 16 + (threadIdx.x & 15u);
     uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 4);
@@ -538,7 +549,7 @@ __global__ void __launch_bounds__(128) mk_cache_query(const __grid_constant__ Ct
 // (pixel + train_offset) % train_stride == 0; each traces the frame's P_SAMPLES_PER_DISPATCH
 // samples one after the other.
 template <typename A>
-__global__ void __launch_bounds__(128) mk_cache_train(const __grid_constant__ Ctx c, NrcPathArgs a, uint32_t first,
+__global__ void VG_CACHE_PATH_BOUNDS mk_cache_train(const __grid_constant__ Ctx c, NrcPathArgs a, uint32_t first,
                                                       uint32_t count)
 {
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
