@@ -76,8 +76,8 @@ def parse():
                          "(the reference's depth-by-depth order: wf_begin / wf_select / wf_extend / wf_shade), "
                          "adaptive (0.02, 16), 20 samples in one accumulate call")
     ap.add_argument("--profile-restir", action="store_true",
-                    help="profiling helper: the many-light scene with ReSTIR DI (32 candidates) at 480x270 on the "
-                         "streaming wavefront, four frames of one sample")
+                    help="profiling helper: the many-light scene with ReSTIR DI (32 candidates) at --width x --height "
+                         "on the streaming wavefront, four frames of one sample")
     ap.add_argument("--width", type=int, default=WIDTH, help="smaller frames are for profiling runs only")
     ap.add_argument("--height", type=int, default=HEIGHT)
     a = ap.parse_args()
@@ -773,7 +773,7 @@ def run_cuda(args):
         rr.set_integrator(Integrator.WAVEFRONT)
         rr.set_accum_precision(32)
         rr.set_restir(Restir(di=True, gi=False, candidates=32, history=20))
-        acc_r = rr.new_accumulation(480, 270)
+        acc_r = rr.new_accumulation(WIDTH, HEIGHT)
         for _ in range(4):
             rr.accumulate(acc_r, 1)
         print(json.dumps({"restir_ms_per_frame": 1e3 * acc_r.gpu_seconds() / 4}), flush=True)
