@@ -33,14 +33,6 @@ constexpr uint32_t FULL = 0xffffffffu;
 #ifndef VG_RESTIR_SHADE_MIN_BLOCKS
 #define VG_RESTIR_SHADE_MIN_BLOCKS 12
 #endif
-// The plain deferred shade stage's own cap, and whether it calls the out-of-line shadePathCall
-// (A/B build switches).
-#ifndef VG_DEFERRED_MIN_BLOCKS
-#define VG_DEFERRED_MIN_BLOCKS VG_SHADE_MIN_BLOCKS
-#endif
-#ifndef VG_DEFERRED_OUTLINE
-#define VG_DEFERRED_OUTLINE 0
-#endif
 // The same for the kernels that run whole paths per thread through the out-of-line shadePathCall
 // (the streaming tail, the batch wavefront's tail).
 #ifndef VG_TAIL_MIN_BLOCKS
@@ -553,7 +545,7 @@ static __global__ void __launch_bounds__(256) wf_stream_classify(const __grid_co
 // hook); it then leaves a query record (one atomic per warp) and finishes like any other.
 // With SORTED the wave's slots are taken class by class from the classify stage's queues.
 template <typename A, bool CACHE = false, bool RESTIR = false, bool SORTED = false>
-__global__ void __launch_bounds__(128, RESTIR ? VG_RESTIR_SHADE_MIN_BLOCKS : VG_DEFERRED_MIN_BLOCKS) wf_stream_shade_deferred(const __grid_constant__ Ctx c,
+__global__ void __launch_bounds__(128, RESTIR ? VG_RESTIR_SHADE_MIN_BLOCKS : VG_SHADE_MIN_BLOCKS) wf_stream_shade_deferred(const __grid_constant__ Ctx c,
                                                                                     Wave w, uint32_t wave,
                                                                                     CacheWave q)
 {
@@ -600,11 +592,7 @@ __global__ void __launch_bounds__(128, RESTIR ? VG_RESTIR_SHADE_MIN_BLOCKS : VG_
                 hk.a0 = sp.x;
                 hk.a = sp.y;
             }
-#if VG_DEFERRED_OUTLINE
-            bool alive = shadePathCall<false, RESTIR, true, CACHE>(c, st, h, depth, p, &req, &hk) && depth + 1 < w.depth;
-#else
             bool alive = shadePath<false, RESTIR, true, CACHE>(c, st, h, depth, p, &req, &hk) && depth + 1 < w.depth;
-#endif
             if (CACHE) {
                 query = hk.query && !bad3(st.parts.total);
                 if (alive)
