@@ -26,7 +26,9 @@ constexpr uint32_t FULL = 0xffffffffu;
 // for the deferred shade stage's ReSTIR instantiations, whose candidate loop waits on memory: on
 // the many-light ReSTIR frame 4 blocks gave 7.89 ms, 6 blocks 7.43 (then 7.01 with the shared
 // candidate target terms), 10 blocks 6.76, 12 blocks 6.72, 16 blocks 6.90. The plain stage keeps
-// 4: 5, 6, 8 or 16 blocks are slower (its inlined shadePath spills heavily below 128 registers).
+// 4: 5, 6, 8 or 16 blocks are slower (its inlined shadePath spills heavily below 128 registers),
+// and so is calling the out-of-line shadePathCall from it (8.99 ms of shading per benchmark step
+// inline at 4 blocks; out of line 9.67 at 4 blocks, 10.5 at 8, 10.9 at 12, 11.4 at 16).
 #ifndef VG_SHADE_MIN_BLOCKS
 #define VG_SHADE_MIN_BLOCKS 4
 #endif
