@@ -270,6 +270,20 @@ cudaError_t launch_stream_shadow(bool f64, int blocks, cudaStream_t s, const vgd
     return cudaGetLastError();
 }
 
+int stream_finish_blocks_per_sm(bool f64)
+{
+    static int n[2] = {0, 0};
+    int& k = n[f64 ? 1 : 0];
+    if (k == 0) {
+        if (f64)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, vgk::wf_stream_finish<double>, 128, 0);
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, vgk::wf_stream_finish<float>, 128, 0);
+        k = k > 0 ? k : 1;
+    }
+    return k;
+}
+
 int stream_deferred_blocks_per_sm(bool f64, int* shadow)
 {
     int n = 0, m = 0;

@@ -805,8 +805,13 @@ __global__ void __launch_bounds__(128, VG_TRACE_MIN_BLOCKS) wf_stream_shadow_tra
 
 // After the shadow trace: add the unoccluded light sample, then queue, finish or restart each slot
 // (the second half of wf_stream_shadow).
+// Minimum resident 128-thread blocks per SM requested for the finish stage (a register cap).
+#ifndef VG_FINISH_MIN_BLOCKS
+#define VG_FINISH_MIN_BLOCKS 8
+#endif
+
 template <typename A, bool RESTIR = false>
-__global__ void __launch_bounds__(128, 8) wf_stream_finish(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
+__global__ void __launch_bounds__(128, VG_FINISH_MIN_BLOCKS) wf_stream_finish(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
 {
     uint32_t in = wave & 1u, out = in ^ 1u;
     if (blockIdx.x == 0 && threadIdx.x == 0)

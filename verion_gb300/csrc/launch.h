@@ -53,6 +53,8 @@ cudaError_t launch_stream_extend_dyn(bool stats, bool coop, int blocks, cudaStre
 cudaError_t launch_stream_shadow_trace(bool stats, bool coop, int blocks, cudaStream_t s, const vgd::Ctx& c,
                                        const vgk::Wave& w, uint32_t wave);
 int stream_trace_blocks_per_sm(bool coop);
+// Resident 128-thread blocks per SM of the finish stage (its grid fills the SMs once).
+int stream_finish_blocks_per_sm(bool f64);
 cudaError_t launch_stream_finish(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
                                  uint32_t wave);
 // The same streaming stages compiled with ReSTIR (kern_wf_restir.cu); the host runs them one

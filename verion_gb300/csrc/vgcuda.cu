@@ -205,6 +205,7 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
         csb = blocks_for(r, r->cache_shade_blocks[v.f64 ? 1 : 0]);
     }
     int shb = blocks_for(r, r->shadow_blocks[v.f64 ? 1 : 0]);
+    int fnb = blocks_for(r, vgx::stream_finish_blocks_per_sm(v.f64));
     // Material-sorted shading of the deferred shade stage (plain, ReSTIR and cache waves).
     bool sorted = deferred && r->material_sort && acc->squeue.p != nullptr && acc->scount.p != nullptr &&
                   acc->squeue.bytes >= (size_t)w.n * 4 * vgk::SHADE_CLASSES;
@@ -244,7 +245,7 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
                 if (ce == cudaSuccess && r->dynamic_fetch && r->ds.shadow_any) {
                     ce = vgx::launch_stream_shadow_trace(r->traversal_stats, r->coop_tris, shb, s, c, w, i);
                     if (ce == cudaSuccess)
-                        ce = (v.restir ? vgx::launch_stream_finish_restir : vgx::launch_stream_finish)(v.f64, shb, s, c, w, i);
+                        ce = (v.restir ? vgx::launch_stream_finish_restir : vgx::launch_stream_finish)(v.f64, fnb, s, c, w, i);
                 } else if (ce == cudaSuccess)
                     ce = (v.restir ? vgx::launch_stream_shadow_restir : vgx::launch_stream_shadow)(v.f64, shb, s, c, w, i);
             } else if (ce == cudaSuccess)
@@ -333,7 +334,7 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
             }
             if (r->dynamic_fetch && r->ds.shadow_any) {
                 VG_CHECK(vgx::launch_stream_shadow_trace(r->traversal_stats, r->coop_tris, shb, s, c, w, (uint32_t)wave), "shadow launch");
-                VG_CHECK((v.restir ? vgx::launch_stream_finish_restir : vgx::launch_stream_finish)(v.f64, shb, s, c, w, (uint32_t)wave), "finish launch");
+                VG_CHECK((v.restir ? vgx::launch_stream_finish_restir : vgx::launch_stream_finish)(v.f64, fnb, s, c, w, (uint32_t)wave), "finish launch");
                 acc->launches++;
             } else {
                 VG_CHECK((v.restir ? vgx::launch_stream_shadow_restir : vgx::launch_stream_shadow)(v.f64, shb, s, c, w, (uint32_t)wave), "shadow launch");
