@@ -805,7 +805,8 @@ __global__ void __launch_bounds__(128, VG_TRACE_MIN_BLOCKS) wf_stream_shadow_tra
 
 // After the shadow trace: add the unoccluded light sample, then queue, finish or restart each slot
 // (the second half of wf_stream_shadow).
-// Minimum resident 128-thread blocks per SM requested for the finish stage (a register cap).
+// Minimum resident 128-thread blocks per SM requested for the finish stage (a register cap; its grid
+// follows). 12 or 16 blocks (40 or 32 registers) are 1.1-1.6% slower per benchmark step than 8.
 #ifndef VG_FINISH_MIN_BLOCKS
 #define VG_FINISH_MIN_BLOCKS 8
 #endif
