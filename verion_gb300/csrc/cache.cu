@@ -132,7 +132,7 @@ using namespace vgc;
 
 // The cache integrator's samples (called by vg_accumulate with the parameter block filled in), in
 // frames: the query paths and training paths of a frame's samples, then the cache's answers for
-// the queries (encoding and inference fused, one launch per sample of the frame, in sample order), then
+// the queries (encode + inference, one launch pair per sample of the frame, in sample order), then
 // the training steps on the frame's training records. With the streaming wavefront (`w`) a frame
 // holds up to cache_frame samples (the cache is fixed within it); with the one-kernel query
 // paths, one.
@@ -250,9 +250,13 @@ int cache_accumulate(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, uint32_t samples,
             VG_CHECK(cudaEventRecord(e1, s), "event");
         for (uint32_t j = 0; j < n; j++) {
             const float* rj = a.qrec + (size_t)j * px * vgn::REC_WORDS;
-            VG_CHECK(vgx::nrc_launch_answer(4 * r->ctx->sms, s, d, rj, ctr + 1 + j, a.qcap, c.accum, f64 ? 64 : 32),
-                     "cache answer launch");
-            acc->launches += 1;
+            VG_CHECK(vgx::nrc_launch_encode(encode_blocks(k), s, d, rj, ctr + 1 + j, a.qcap, 0, a.qcap,
+                                            (uint8_t*)k->X.p),
+                     "cache encode launch");
+            VG_CHECK(vgx::nrc_launch_infer(3 * r->ctx->sms, s, d, (const uint8_t*)k->X.p, rj, ctr + 1 + j, a.qcap,
+                                           nullptr, c.accum, f64 ? 64 : 32),
+                     "cache inference launch");
+            acc->launches += 2;
         }
         if (timed)
             VG_CHECK(cudaEventRecord(e2, s), "event");

@@ -187,95 +187,6 @@ __global__ void __launch_bounds__(128) nrc_infer(CacheDev cd, const uint8_t* __r
         tmem_free(tmem, 64);
 }
 
-// The fused form of nrc_encode + nrc_infer (accumulate mode) for the cache integrator's queries:
-// each CTA encodes a 128-record tile straight into shared memory (one row per thread) and runs the
-// five layers on it, so the input tile never goes through memory. The same operations on the same
-// values as the two kernels, so the same sums.
-constexpr uint32_t ANSWER_SMEM = IMG_FWD_BYTES + 16384 + 1024;
-
-template <typename A>
-__global__ void __launch_bounds__(128) nrc_answer(CacheDev cd, const float* __restrict__ rec, const uint32_t* count,
-                                                  uint32_t cap, A* accum)
-{
-    uint32_t n = min(*count, cap);
-    uint32_t tiles = (n + TILE - 1) / TILE;
-    if (blockIdx.x >= tiles)
-        return;
-    extern __shared__ uint8_t smem_raw[];
-    uint8_t* sm = align1024(smem_raw);
-    uint8_t* W = sm;
-    uint8_t* H = sm + IMG_FWD_BYTES;
-    __shared__ uint64_t bar;
-    __shared__ uint32_t tslot;
-    uint32_t tid = threadIdx.x, warp = tid >> 5;
-    for (uint32_t i = tid; i < IMG_FWD_BYTES / 16; i += blockDim.x)
-        reinterpret_cast<uint4*>(W)[i] = __ldg(reinterpret_cast<const uint4*>(cd.img) + i);
-    if (tid == 0) {
-        bar_init(&bar, 1);
-        fence_bar_init();
-    }
-    if (warp == 0)
-        tmem_alloc(&tslot, 64);
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    uint32_t tmem = tslot;
-    uint32_t lane_addr = tmem + ((warp * 32u) << 16);
-    uint32_t phase = 0;
-    bool ok = true;
-    for (uint32_t t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
-        uint32_t i = t * TILE + tid;
-        bool has = i < n;
-        const float* r = rec + (size_t)i * REC_WORDS;
-        float v[64];
-        if (has) {
-            input_row(cd, r, v);
-        } else {
-#pragma unroll
-            for (int x = 0; x < 64; x++)
-                v[x] = 0.0f;
-        }
-        store_row(H, tid, v);
-        for (uint32_t l = 0; l < 5; l++) {
-            fence_async_smem();
-            __syncthreads();
-            tc_fence_after();
-            if (tid == 0) {
-                const uint8_t* B = W + (l < 4 ? IMG_W + l * 8192u : IMG_W4);
-                issue_layer(tmem, H, 0, B, 0, l < 4 ? 64u : 16u, 4, false);
-                mma_commit(&bar);
-            }
-            bool fin = wait_mma(&bar, phase);
-            phase ^= 1u;
-            ok = __syncthreads_and(fin) != 0;
-            if (!ok)
-                break;
-            tc_fence_after();
-            load_acc(lane_addr, v, l < 4 ? 64 : 16);
-            tc_fence_before();
-            if (l < 4) {
-#pragma unroll
-                for (int x = 0; x < 64; x++)
-                    v[x] = fmaxf(v[x], 0.0f);
-                store_row(H, tid, v);
-            }
-        }
-        if (ok && has) {
-            A* a = accum + 3 * (size_t)__float_as_uint(r[19]);
-            a[0] += (A)(r[16] * fmaxf(v[0], 0.0f));
-            a[1] += (A)(r[17] * fmaxf(v[1], 0.0f));
-            a[2] += (A)(r[18] * fmaxf(v[2], 0.0f));
-        }
-        __syncthreads();
-    }
-    if (!ok && tid == 0)
-        atomicOr(cd.err, ERR_MMA_TIMEOUT);
-    tc_fence_before();
-    __syncthreads();
-    if (warp == 0)
-        tmem_free(tmem, 64);
-}
-
 // ---- training -----------------------------------------------------------------------------------
 
 // Shared-memory plan of the training kernel (bytes from a 1024-aligned base).
@@ -709,8 +620,6 @@ void nrc_prepare()
     cudaFuncSetAttribute(nrc_infer<1, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM);
     cudaFuncSetAttribute(nrc_infer<1, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM);
     cudaFuncSetAttribute(nrc_train, cudaFuncAttributeMaxDynamicSharedMemorySize, TRAIN_SMEM);
-    cudaFuncSetAttribute(nrc_answer<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, ANSWER_SMEM);
-    cudaFuncSetAttribute(nrc_answer<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, ANSWER_SMEM);
     done = true;
 }
 
@@ -738,17 +647,6 @@ cudaError_t nrc_launch_infer(int blocks, cudaStream_t s, const vgn::CacheDev& cd
         nrc_infer<1, double><<<blocks, 128, INFER_SMEM, s>>>(cd, X, rec, count, cap, nullptr, (double*)accum);
     else
         nrc_infer<1, float><<<blocks, 128, INFER_SMEM, s>>>(cd, X, rec, count, cap, nullptr, (float*)accum);
-    return cudaGetLastError();
-}
-
-cudaError_t nrc_launch_answer(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const float* rec,
-                              const uint32_t* count, uint32_t cap, void* accum, int accum_bits)
-{
-    nrc_prepare();
-    if (accum_bits == 64)
-        nrc_answer<double><<<blocks, 128, ANSWER_SMEM, s>>>(cd, rec, count, cap, (double*)accum);
-    else
-        nrc_answer<float><<<blocks, 128, ANSWER_SMEM, s>>>(cd, rec, count, cap, (float*)accum);
     return cudaGetLastError();
 }
 

@@ -44,9 +44,6 @@ cudaError_t nrc_launch_scatter(int blocks, cudaStream_t s, const vgn::CacheDev& 
                                const uint32_t* count, uint32_t cap, uint32_t offset, uint32_t limit, const float* GX);
 cudaError_t nrc_launch_infer(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const uint8_t* X, const float* rec,
                              const uint32_t* count, uint32_t cap, float* out, void* accum, int accum_bits);
-// nrc_encode + nrc_infer into `accum` in one kernel (the input tile stays in shared memory).
-cudaError_t nrc_launch_answer(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const float* rec,
-                              const uint32_t* count, uint32_t cap, void* accum, int accum_bits);
 cudaError_t nrc_launch_train(int blocks, cudaStream_t s, const vgn::CacheDev& cd, const uint8_t* X, const float* rec,
                              const uint32_t* count, uint32_t cap, uint32_t offset, uint32_t batch, float* GX);
 cudaError_t nrc_launch_adam(cudaStream_t s, float* p, float* g, float* m, float* v, size_t n, const uint32_t* count,
