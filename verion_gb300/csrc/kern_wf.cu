@@ -330,6 +330,16 @@ cudaError_t launch_stream_shadow_trace(bool stats, bool coop, int blocks, cudaSt
     return cudaGetLastError();
 }
 
+int stream_shadow_trace_blocks_per_sm()
+{
+    static int n = 0;
+    if (n == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, vgk::wf_stream_shadow_trace<false, false>, 128, 0);
+        n = n > 0 ? n : 1;
+    }
+    return n;
+}
+
 int stream_trace_blocks_per_sm(bool coop)
 {
     int n = 0;

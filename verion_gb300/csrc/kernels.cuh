@@ -773,8 +773,13 @@ __global__ void __launch_bounds__(128, VG_TRACE_MIN_BLOCKS) wf_stream_extend_dyn
 // Shadow rays of the deferred light samples, any hit (opaque scenes: one layer, no opacity roll).
 // The result goes to hits[p].x (1 occluded), which the finish stage reads. STATS: the rays traced
 // are counted into tstats[4].
+// The same for the shadow stage alone (its any-hit rays end at the first occluder).
+#ifndef VG_SHADOW_MIN_BLOCKS
+#define VG_SHADOW_MIN_BLOCKS VG_TRACE_MIN_BLOCKS
+#endif
+
 template <bool STATS, bool COOP>
-__global__ void __launch_bounds__(128, VG_TRACE_MIN_BLOCKS) wf_stream_shadow_trace(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
+__global__ void __launch_bounds__(128, VG_SHADOW_MIN_BLOCKS) wf_stream_shadow_trace(const __grid_constant__ Ctx c, Wave w, uint32_t wave)
 {
     uint32_t in = wave & 1u;
     uint32_t count = w.counts[in];

@@ -53,8 +53,10 @@ cudaError_t launch_stream_extend_dyn(bool stats, bool coop, int blocks, cudaStre
 cudaError_t launch_stream_shadow_trace(bool stats, bool coop, int blocks, cudaStream_t s, const vgd::Ctx& c,
                                        const vgk::Wave& w, uint32_t wave);
 int stream_trace_blocks_per_sm(bool coop);
-// Resident 128-thread blocks per SM of the finish stage (its grid fills the SMs once).
+// Resident 128-thread blocks per SM of the finish stage and of the shadow stage (their grids fill
+// the SMs once).
 int stream_finish_blocks_per_sm(bool f64);
+int stream_shadow_trace_blocks_per_sm();
 cudaError_t launch_stream_finish(bool f64, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w,
                                  uint32_t wave);
 // The same streaming stages compiled with ReSTIR (kern_wf_restir.cu); the host runs them one

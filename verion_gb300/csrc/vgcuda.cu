@@ -206,6 +206,7 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
     }
     int shb = blocks_for(r, r->shadow_blocks[v.f64 ? 1 : 0]);
     int fnb = blocks_for(r, vgx::stream_finish_blocks_per_sm(v.f64));
+    int stb = blocks_for(r, vgx::stream_shadow_trace_blocks_per_sm());
     // Material-sorted shading of the deferred shade stage (plain, ReSTIR and cache waves).
     bool sorted = deferred && r->material_sort && acc->squeue.p != nullptr && acc->scount.p != nullptr &&
                   acc->squeue.bytes >= (size_t)w.n * 4 * vgk::SHADE_CLASSES;
@@ -243,7 +244,7 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
             if (ce == cudaSuccess && deferred) {
                 ce = (q ? vgx::launch_stream_cache_shade(v.f64, sorted, csb, s, c, w, i, *q) : (v.restir ? vgx::launch_stream_shade_deferred_restir : vgx::launch_stream_shade_deferred)(v.f64, sorted, dsb, s, c, w, i));
                 if (ce == cudaSuccess && r->dynamic_fetch && r->ds.shadow_any) {
-                    ce = vgx::launch_stream_shadow_trace(r->traversal_stats, r->coop_tris, shb, s, c, w, i);
+                    ce = vgx::launch_stream_shadow_trace(r->traversal_stats, r->coop_tris, stb, s, c, w, i);
                     if (ce == cudaSuccess)
                         ce = (v.restir ? vgx::launch_stream_finish_restir : vgx::launch_stream_finish)(v.f64, fnb, s, c, w, i);
                 } else if (ce == cudaSuccess)
@@ -333,7 +334,7 @@ int stream_samples(VgRenderer* r, VgAccum* acc, vgd::Ctx& c, vgx::Variant v, con
                 VG_CHECK(cudaEventRecord(qe, s), "event");
             }
             if (r->dynamic_fetch && r->ds.shadow_any) {
-                VG_CHECK(vgx::launch_stream_shadow_trace(r->traversal_stats, r->coop_tris, shb, s, c, w, (uint32_t)wave), "shadow launch");
+                VG_CHECK(vgx::launch_stream_shadow_trace(r->traversal_stats, r->coop_tris, stb, s, c, w, (uint32_t)wave), "shadow launch");
                 VG_CHECK((v.restir ? vgx::launch_stream_finish_restir : vgx::launch_stream_finish)(v.f64, fnb, s, c, w, (uint32_t)wave), "finish launch");
                 acc->launches++;
             } else {
