@@ -66,6 +66,11 @@ def test_null_handles_are_rejected(lib_path):
     assert L.vg_set_multiscatter(None, 1) == backend.VG_ERR_INVALID
     assert L.vg_accumulate(None, None, 1) == backend.VG_ERR_INVALID
     assert L.vg_accum_samples(None) == 0
+    # Batched serving: no context, no requests.
+    assert L.vg_batch_render(None, None, 0, None, None, None) == backend.VG_ERR_INVALID
+    assert L.vg_set_batch_options(None, 0, 0, 0) == backend.VG_ERR_INVALID
+    assert L.vg_set_batch_wave_slots(None, 1 << 21) == backend.VG_ERR_INVALID
+    assert L.vg_set_batch_device_loop(None, 1) == backend.VG_ERR_INVALID
 
 
 def test_oracle_library_loads(oracle_lib):
