@@ -367,16 +367,18 @@ void vg_debug_allocations(uint64_t* mallocs, uint64_t* frees);
  *   first) and taken by the CTAs of one kernel. A request with a cache ends its paths at the cache
  *   and evaluates the cache inside the same CTA (tensor cores); after the launch each cache takes
  *   its renderer's training steps (vg_set_cache) on the batch's training records.
- * - plain requests from the threshold up: the batch wavefront, the streaming wavefront over the
- *   pixels of all of them (each path slot traces one pixel of one request with all its samples,
- *   then takes the next pixel in request order), its bounce loop running on the device inside the
- *   graph (a conditional WHILE node).
+ * - requests from the threshold up (by default every request): the batch wavefront, the streaming
+ *   wavefront over the pixels of all of them (each path slot traces one pixel of one request with
+ *   all its samples, then takes the next pixel in request order), its bounce loop running on the
+ *   device inside the graph (a conditional WHILE node). A cached request's queries are answered
+ *   after each wave by one kernel for all caches; the caches train after the loop.
  * - requests with a cache that the batch wavefront cannot tag (more than 2^22 pixels, or more than
  *   1024 requests in the batch): one at a time on the streaming cache integrator after the shared
  *   launches, shortest first.
  * The batch wavefront takes at most 2^31 pixels per batch (VG_ERR_INVALID beyond).
  * A plain request's samples are exactly what vg_accumulate's megakernel adds (same sums, either
- * shared launch); a cached request's exactly what the cache integrator adds with a fixed cache. */
+ * shared launch); a cached request's exactly what the megakernel cache integrator adds with a fixed
+ * cache. */
 typedef enum VgBatchOrder { VG_BATCH_SHORTEST_FIRST = 0, VG_BATCH_AS_GIVEN = 1, VG_BATCH_LONGEST_FIRST = 2 } VgBatchOrder;
 
 typedef struct VgBatchRequest {
