@@ -252,6 +252,7 @@ struct VgAccum {
     DevBuf re_g[2], re_n[2], re_x[2], re_m[2];
     DevBuf re_gx[2], re_gn[2], re_gl[2], re_s[7]; // ReSTIR GI planes
     DevBuf state, hits, queue[2], counts, fetch, tstats, meta, sreq, squeue, scount;
+    DevBuf mk_next;                  // the megakernel's pixel counter
     uint32_t* host_counts = nullptr; // pinned ring of wave output counts (streaming wavefront)
     uint32_t last_waves = 0;
     std::vector<uint32_t> wave_live; // last streaming accumulate: live slots after each wave

@@ -4,24 +4,40 @@
 
 namespace vgx {
 
+// Persistent form: resident blocks per SM times the SMs, the work counter cleared first; else one
+// 16 x 8 tile per block.
 template <bool L, bool R, typename A>
-static cudaError_t mk(dim3 grid, cudaStream_t s, const vgd::Ctx& c)
+static cudaError_t mk(int sms, uint32_t w, uint32_t h, cudaStream_t s, const vgd::Ctx& c, uint32_t* next)
 {
-    vgk::mk_pathtrace<L, R, A><<<grid, 128, 0, s>>>(c);
+#if VG_MK_PERSISTENT
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vgk::mk_pathtrace<L, R, A>, 128, 0) != cudaSuccess ||
+            per_sm < 1)
+            per_sm = 1;
+    }
+    cudaError_t e = cudaMemsetAsync(next, 0, 4, s);
+    if (e != cudaSuccess)
+        return e;
+    vgk::mk_pathtrace<L, R, A><<<per_sm * sms, 128, 0, s>>>(c, next);
+#else
+    vgk::mk_pathtrace<L, R, A><<<dim3((w + 15) / 16, (h + 7) / 8), 128, 0, s>>>(c, next);
+#endif
     return cudaGetLastError();
 }
 
-cudaError_t launch_megakernel(Variant v, dim3 grid, cudaStream_t s, const vgd::Ctx& c)
+cudaError_t launch_megakernel(Variant v, int sms, uint32_t w, uint32_t h, cudaStream_t s, const vgd::Ctx& c,
+                              uint32_t* next)
 {
     switch (v.index()) {
-    case 0: return mk<false, false, float>(grid, s, c);
-    case 1: return mk<true, false, float>(grid, s, c);
-    case 2: return mk<false, true, float>(grid, s, c);
-    case 3: return mk<true, true, float>(grid, s, c);
-    case 4: return mk<false, false, double>(grid, s, c);
-    case 5: return mk<true, false, double>(grid, s, c);
-    case 6: return mk<false, true, double>(grid, s, c);
-    default: return mk<true, true, double>(grid, s, c);
+    case 0: return mk<false, false, float>(sms, w, h, s, c, next);
+    case 1: return mk<true, false, float>(sms, w, h, s, c, next);
+    case 2: return mk<false, true, float>(sms, w, h, s, c, next);
+    case 3: return mk<true, true, float>(sms, w, h, s, c, next);
+    case 4: return mk<false, false, double>(sms, w, h, s, c, next);
+    case 5: return mk<true, false, double>(sms, w, h, s, c, next);
+    case 6: return mk<false, true, double>(sms, w, h, s, c, next);
+    default: return mk<true, true, double>(sms, w, h, s, c, next);
     }
 }
 

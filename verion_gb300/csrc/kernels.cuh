@@ -182,16 +182,11 @@ __device__ __forceinline__ PathState<LIGHT> loadPath(const Ctx& c, const Wave& w
     return s;
 }
 
-// pathtrace.slang:9-26: one thread per pixel, params[35] samples from params[6]. One loop over
-// bounces: a lane whose path ends adds it and starts its pixel's next sample in the same
-// iteration, so the warp's lanes stay on bounce work until they run out of samples instead of
-// waiting at the end of each sample for the warp's longest path. Same samples, same order per
-// pixel, same sums.
 // Minimum resident 128-thread blocks per SM requested for the megakernel (a register cap; 0: none).
 // Its threads spend most of their time waiting on dependent node loads in the traversal, so
 // occupancy pays more than registers: on the 1M-triangle workload at 1080p, 72.8 Mpaths/s with no
 // cap (168 registers, 3 blocks per SM), 88.9 at 8 blocks (64 registers), 102.4 at 12, 114.1 at 16
-// (32 registers, every warp slot of the SM; the spilled values are few and L1-resident).
+// (32 registers, every warp slot of the SM; the spills mostly stay in L1 and L2).
 #ifndef VG_MK_MIN_BLOCKS
 #define VG_MK_MIN_BLOCKS 16
 #endif
@@ -201,16 +196,78 @@ __device__ __forceinline__ PathState<LIGHT> loadPath(const Ctx& c, const Wave& w
 #define VG_MK_BOUNDS __launch_bounds__(128)
 #endif
 
+// Idle lanes at or above which a megakernel warp takes new pixels (VG_MK_PERSISTENT).
+#ifndef VG_MK_REFILL
+#define VG_MK_REFILL 4
+#endif
+#ifndef VG_MK_PERSISTENT
+#define VG_MK_PERSISTENT 1
+#endif
+
+// pathtrace.slang:9-26: params[35] samples from params[6] for every pixel, each pixel's samples in
+// order in one thread. One loop over bounces: a lane whose path ends adds it and starts its
+// pixel's next sample in the same iteration. Persistent (VG_MK_PERSISTENT): a grid that fills the
+// SMs once, whose warps take pixels from the work counter `next` (one atomic per refill) whenever at
+// least VG_MK_REFILL lanes have finished theirs, so a warp does not idle on its longest pixel.
+// Same samples, same order per pixel, same sums either way.
 template <bool LIGHT, bool RESTIR, typename A>
-__global__ void VG_MK_BOUNDS mk_pathtrace(const __grid_constant__ Ctx c)
+__global__ void VG_MK_BOUNDS mk_pathtrace(const __grid_constant__ Ctx c, uint32_t* next)
 {
+    uint32_t width = c.p[P_WIDTH];
+    uint32_t n = c.p[P_SAMPLES_PER_DISPATCH];
+    bool adaptive = c.p[P_ADAPTIVE] != 0;
+#if VG_MK_PERSISTENT
+    uint32_t npix = width * c.p[P_HEIGHT];
+    uint32_t lane = lane_id(), lt = (1u << lane) - 1u;
+    bool active = false, exhausted = n == 0;
+    uint32_t pixel = 0, k = 0, depth = 0;
+    PathState<LIGHT> st;
+    for (;;) {
+        uint32_t idle = __ballot_sync(FULL, !active);
+        if (!exhausted && (idle == FULL || (uint32_t)__popc(idle) >= VG_MK_REFILL)) {
+            uint32_t cnt = __popc(idle), base = 0;
+            if (lane == 0)
+                base = atomicAdd(next, cnt);
+            base = __shfl_sync(FULL, base, 0);
+            exhausted = base + cnt >= npix;
+            if (!active) {
+                uint32_t idx = base + __popc(idle & lt);
+                if (idx < npix && !(adaptive && !pixelActive<A>(c, idx))) {
+                    pixel = idx;
+                    k = 0;
+                    depth = 0;
+                    st = generatePathFor<LIGHT>(c, pixel % width, pixel / width, c.p[P_SAMPLE]);
+                    active = true;
+                }
+            }
+        }
+        if (__ballot_sync(FULL, active) == 0) {
+            if (exhausted)
+                break;
+            continue;
+        }
+        if (active) {
+            if (shadePathCall<LIGHT, RESTIR>(c, st, traceClosest(c, st.org, st.dir), depth, pixel) &&
+                depth + 1 < c.p[P_MAX_DEPTH]) {
+                depth++;
+            } else {
+                finishPath<LIGHT, A, RESTIR>(c, st, pixel);
+                if (++k < n && !(adaptive && !pixelActive<A>(c, pixel))) {
+                    depth = 0;
+                    st = generatePathFor<LIGHT>(c, pixel % width, pixel / width, c.p[P_SAMPLE] + k);
+                } else {
+                    active = false;
+                }
+            }
+        }
+    }
+#else
     uint32_t x = blockIdx.x * 16 + (threadIdx.x & 15u);
     uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 4);
-    if (x >= c.p[P_WIDTH] || y >= c.p[P_HEIGHT])
+    if (x >= width || y >= c.p[P_HEIGHT])
         return;
-    uint32_t pixel = y * c.p[P_WIDTH] + x;
-    uint32_t n = c.p[P_SAMPLES_PER_DISPATCH];
-    if (n == 0 || (c.p[P_ADAPTIVE] != 0 && !pixelActive<A>(c, pixel)))
+    uint32_t pixel = y * width + x;
+    if (n == 0 || (adaptive && !pixelActive<A>(c, pixel)))
         return;
     uint32_t k = 0, depth = 0;
     PathState<LIGHT> st = generatePathFor<LIGHT>(c, x, y, c.p[P_SAMPLE]);
@@ -221,11 +278,12 @@ __global__ void VG_MK_BOUNDS mk_pathtrace(const __grid_constant__ Ctx c)
             continue;
         }
         finishPath<LIGHT, A, RESTIR>(c, st, pixel);
-        if (++k >= n || (c.p[P_ADAPTIVE] != 0 && !pixelActive<A>(c, pixel)))
+        if (++k >= n || (adaptive && !pixelActive<A>(c, pixel)))
             break;
         depth = 0;
         st = generatePathFor<LIGHT>(c, x, y, c.p[P_SAMPLE] + k);
     }
+#endif
 }
 
 // wf_args.slang:9-24 at depth 0: starts a sample. Every pixel's path is live unless adaptive

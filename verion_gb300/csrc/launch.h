@@ -16,7 +16,9 @@ struct Variant {
     int index() const { return (light ? 1 : 0) | (restir ? 2 : 0) | (f64 ? 4 : 0); }
 };
 
-cudaError_t launch_megakernel(Variant v, dim3 grid, cudaStream_t s, const vgd::Ctx& c);
+// The megakernel over a w x h frame; `next` is a device word (its pixel counter).
+cudaError_t launch_megakernel(Variant v, int sms, uint32_t w, uint32_t h, cudaStream_t s, const vgd::Ctx& c,
+                              uint32_t* next);
 cudaError_t launch_wf_shade(Variant v, int blocks, cudaStream_t s, const vgd::Ctx& c, const vgk::Wave& w, uint32_t d);
 int wf_shade_blocks_per_sm(Variant v);
 

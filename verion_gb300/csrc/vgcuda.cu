@@ -1068,13 +1068,15 @@ int vg_accumulate(VgRenderer* r, VgAccum* acc, uint32_t samples)
                                    r->integrator == VG_WAVEFRONT ? &w : nullptr)) != VG_OK)
             return st;
     } else if (!wavefront) {
-        dim3 grid((acc->width + 15) / 16, (acc->height + 7) / 8);
+        if (!acc->mk_next.p && (st = alloc(acc->mk_next, 16, s, true)) != VG_OK)
+            return st;
         uint32_t k = 0;
         while (k < samples) {
             c.p[P_SAMPLE] = sample0 + k;
             c.p[P_SAMPLES_PER_DISPATCH] = std::min<uint32_t>(samples - k, acc->restir.on ? 1u : 8u);
             k += c.p[P_SAMPLES_PER_DISPATCH];
-            VG_CHECK(vgx::launch_megakernel(v, grid, s, c), "megakernel launch");
+            VG_CHECK(vgx::launch_megakernel(v, r->ctx->sms, acc->width, acc->height, s, c, (uint32_t*)acc->mk_next.p),
+                     "megakernel launch");
             acc->launches++;
         }
     } else {
