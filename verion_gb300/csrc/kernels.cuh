@@ -217,7 +217,11 @@ __global__ void VG_MK_BOUNDS mk_pathtrace(const __grid_constant__ Ctx c, uint32_
     uint32_t n = c.p[P_SAMPLES_PER_DISPATCH];
     bool adaptive = c.p[P_ADAPTIVE] != 0;
 #if VG_MK_PERSISTENT
-    uint32_t npix = width * c.p[P_HEIGHT];
+    // Work items in 16 x 8 tiles (128 consecutive items per tile), so a warp's 32 pixels are a
+    // 16 x 2 block as in the one-tile-per-block form; items outside the frame are skipped.
+    uint32_t height = c.p[P_HEIGHT];
+    uint32_t tiles_x = (width + 15) / 16;
+    uint32_t nitems = tiles_x * ((height + 7) / 8) * 128u;
     uint32_t lane = lane_id(), lt = (1u << lane) - 1u;
     bool active = false, exhausted = n == 0;
     uint32_t pixel = 0, k = 0, depth = 0;
@@ -229,14 +233,16 @@ __global__ void VG_MK_BOUNDS mk_pathtrace(const __grid_constant__ Ctx c, uint32_
             if (lane == 0)
                 base = atomicAdd(next, cnt);
             base = __shfl_sync(FULL, base, 0);
-            exhausted = base + cnt >= npix;
+            exhausted = base + cnt >= nitems;
             if (!active) {
                 uint32_t idx = base + __popc(idle & lt);
-                if (idx < npix && !(adaptive && !pixelActive<A>(c, idx))) {
-                    pixel = idx;
+                uint32_t t = idx >> 7, r = idx & 127u;
+                uint32_t x = (t % tiles_x) * 16 + (r & 15u), y = (t / tiles_x) * 8 + (r >> 4);
+                if (idx < nitems && x < width && y < height && !(adaptive && !pixelActive<A>(c, y * width + x))) {
+                    pixel = y * width + x;
                     k = 0;
                     depth = 0;
-                    st = generatePathFor<LIGHT>(c, pixel % width, pixel / width, c.p[P_SAMPLE]);
+                    st = generatePathFor<LIGHT>(c, x, y, c.p[P_SAMPLE]);
                     active = true;
                 }
             }
