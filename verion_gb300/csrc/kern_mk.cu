@@ -9,20 +9,20 @@ namespace vgx {
 template <bool L, bool R, typename A>
 static cudaError_t mk(int sms, uint32_t w, uint32_t h, cudaStream_t s, const vgd::Ctx& c, uint32_t* next)
 {
-#if VG_MK_PERSISTENT
-    static int per_sm = 0;
-    if (per_sm == 0) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vgk::mk_pathtrace<L, R, A>, 128, 0) != cudaSuccess ||
-            per_sm < 1)
-            per_sm = 1;
+    if constexpr (vgk::mk_persistent(R)) {
+        static int per_sm = 0;
+        if (per_sm == 0) {
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vgk::mk_pathtrace<L, R, A>, 128, 0) != cudaSuccess ||
+                per_sm < 1)
+                per_sm = 1;
+        }
+        cudaError_t e = cudaMemsetAsync(next, 0, 4, s);
+        if (e != cudaSuccess)
+            return e;
+        vgk::mk_pathtrace<L, R, A><<<per_sm * sms, 128, 0, s>>>(c, next);
+    } else {
+        vgk::mk_pathtrace<L, R, A><<<dim3((w + 15) / 16, (h + 7) / 8), 128, 0, s>>>(c, next);
     }
-    cudaError_t e = cudaMemsetAsync(next, 0, 4, s);
-    if (e != cudaSuccess)
-        return e;
-    vgk::mk_pathtrace<L, R, A><<<per_sm * sms, 128, 0, s>>>(c, next);
-#else
-    vgk::mk_pathtrace<L, R, A><<<dim3((w + 15) / 16, (h + 7) / 8), 128, 0, s>>>(c, next);
-#endif
     return cudaGetLastError();
 }
 

@@ -204,92 +204,98 @@ __device__ __forceinline__ PathState<LIGHT> loadPath(const Ctx& c, const Wave& w
 #define VG_MK_PERSISTENT 1
 #endif
 
+// Whether a megakernel instantiation is the persistent form. ReSTIR frames keep one tile per block:
+// with one sample per launch the refills cost more than they save (the many-light ReSTIR frame
+// 15.6 ms persistent against 13.0 ms; plain frames 119.9 against 113.9 Mpaths/s on the
+// 1M-triangle workload, 5.9 against 6.7 ms per many-light frame).
+__host__ __device__ constexpr bool mk_persistent(bool restir) { return VG_MK_PERSISTENT && !restir; }
+
 // pathtrace.slang:9-26: params[35] samples from params[6] for every pixel, each pixel's samples in
 // order in one thread. One loop over bounces: a lane whose path ends adds it and starts its
-// pixel's next sample in the same iteration. Persistent (VG_MK_PERSISTENT): a grid that fills the
-// SMs once, whose warps take pixels from the work counter `next` (one atomic per refill) whenever at
-// least VG_MK_REFILL lanes have finished theirs, so a warp does not idle on its longest pixel.
-// Same samples, same order per pixel, same sums either way.
+// pixel's next sample in the same iteration. Persistent (mk_persistent: frames without ReSTIR): a
+// grid that fills the SMs once, whose warps take pixels from the work counter `next` (one atomic per
+// refill) whenever at least VG_MK_REFILL lanes have finished theirs, so a warp does not idle on its
+// longest pixel; else one 16 x 8 tile per block. Same samples, same order per pixel, same sums.
 template <bool LIGHT, bool RESTIR, typename A>
 __global__ void VG_MK_BOUNDS mk_pathtrace(const __grid_constant__ Ctx c, uint32_t* next)
 {
     uint32_t width = c.p[P_WIDTH];
     uint32_t n = c.p[P_SAMPLES_PER_DISPATCH];
     bool adaptive = c.p[P_ADAPTIVE] != 0;
-#if VG_MK_PERSISTENT
-    // Work items in 16 x 8 tiles (128 consecutive items per tile), so a warp's 32 pixels are a
-    // 16 x 2 block as in the one-tile-per-block form; items outside the frame are skipped.
-    uint32_t height = c.p[P_HEIGHT];
-    uint32_t tiles_x = (width + 15) / 16;
-    uint32_t nitems = tiles_x * ((height + 7) / 8) * 128u;
-    uint32_t lane = lane_id(), lt = (1u << lane) - 1u;
-    bool active = false, exhausted = n == 0;
-    uint32_t pixel = 0, k = 0, depth = 0;
-    PathState<LIGHT> st;
-    for (;;) {
-        uint32_t idle = __ballot_sync(FULL, !active);
-        if (!exhausted && (idle == FULL || (uint32_t)__popc(idle) >= VG_MK_REFILL)) {
-            uint32_t cnt = __popc(idle), base = 0;
-            if (lane == 0)
-                base = atomicAdd(next, cnt);
-            base = __shfl_sync(FULL, base, 0);
-            exhausted = base + cnt >= nitems;
-            if (!active) {
-                uint32_t idx = base + __popc(idle & lt);
-                uint32_t t = idx >> 7, r = idx & 127u;
-                uint32_t x = (t % tiles_x) * 16 + (r & 15u), y = (t / tiles_x) * 8 + (r >> 4);
-                if (idx < nitems && x < width && y < height && !(adaptive && !pixelActive<A>(c, y * width + x))) {
-                    pixel = y * width + x;
-                    k = 0;
-                    depth = 0;
-                    st = generatePathFor<LIGHT>(c, x, y, c.p[P_SAMPLE]);
-                    active = true;
+    if constexpr (mk_persistent(RESTIR)) {
+        // Work items in 16 x 8 tiles (128 consecutive items per tile), so a warp's 32 pixels are a
+        // 16 x 2 block as in the one-tile-per-block form; items outside the frame are skipped.
+        uint32_t height = c.p[P_HEIGHT];
+        uint32_t tiles_x = (width + 15) / 16;
+        uint32_t nitems = tiles_x * ((height + 7) / 8) * 128u;
+        uint32_t lane = lane_id(), lt = (1u << lane) - 1u;
+        bool active = false, exhausted = n == 0;
+        uint32_t pixel = 0, k = 0, depth = 0;
+        PathState<LIGHT> st;
+        for (;;) {
+            uint32_t idle = __ballot_sync(FULL, !active);
+            if (!exhausted && (idle == FULL || (uint32_t)__popc(idle) >= VG_MK_REFILL)) {
+                uint32_t cnt = __popc(idle), base = 0;
+                if (lane == 0)
+                    base = atomicAdd(next, cnt);
+                base = __shfl_sync(FULL, base, 0);
+                exhausted = base + cnt >= nitems;
+                if (!active) {
+                    uint32_t idx = base + __popc(idle & lt);
+                    uint32_t t = idx >> 7, r = idx & 127u;
+                    uint32_t x = (t % tiles_x) * 16 + (r & 15u), y = (t / tiles_x) * 8 + (r >> 4);
+                    if (idx < nitems && x < width && y < height && !(adaptive && !pixelActive<A>(c, y * width + x))) {
+                        pixel = y * width + x;
+                        k = 0;
+                        depth = 0;
+                        st = generatePathFor<LIGHT>(c, x, y, c.p[P_SAMPLE]);
+                        active = true;
+                    }
+                }
+            }
+            if (__ballot_sync(FULL, active) == 0) {
+                if (exhausted)
+                    break;
+                continue;
+            }
+            if (active) {
+                if (shadePathCall<LIGHT, RESTIR>(c, st, traceClosest(c, st.org, st.dir), depth, pixel) &&
+                    depth + 1 < c.p[P_MAX_DEPTH]) {
+                    depth++;
+                } else {
+                    finishPath<LIGHT, A, RESTIR>(c, st, pixel);
+                    if (++k < n && !(adaptive && !pixelActive<A>(c, pixel))) {
+                        depth = 0;
+                        st = generatePathFor<LIGHT>(c, pixel % width, pixel / width, c.p[P_SAMPLE] + k);
+                    } else {
+                        active = false;
+                    }
                 }
             }
         }
-        if (__ballot_sync(FULL, active) == 0) {
-            if (exhausted)
-                break;
-            continue;
-        }
-        if (active) {
+    } else {
+        uint32_t x = blockIdx.x * 16 + (threadIdx.x & 15u);
+        uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 4);
+        if (x >= width || y >= c.p[P_HEIGHT])
+            return;
+        uint32_t pixel = y * width + x;
+        if (n == 0 || (adaptive && !pixelActive<A>(c, pixel)))
+            return;
+        uint32_t k = 0, depth = 0;
+        PathState<LIGHT> st = generatePathFor<LIGHT>(c, x, y, c.p[P_SAMPLE]);
+        for (;;) {
             if (shadePathCall<LIGHT, RESTIR>(c, st, traceClosest(c, st.org, st.dir), depth, pixel) &&
                 depth + 1 < c.p[P_MAX_DEPTH]) {
                 depth++;
-            } else {
-                finishPath<LIGHT, A, RESTIR>(c, st, pixel);
-                if (++k < n && !(adaptive && !pixelActive<A>(c, pixel))) {
-                    depth = 0;
-                    st = generatePathFor<LIGHT>(c, pixel % width, pixel / width, c.p[P_SAMPLE] + k);
-                } else {
-                    active = false;
-                }
+                continue;
             }
+            finishPath<LIGHT, A, RESTIR>(c, st, pixel);
+            if (++k >= n || (adaptive && !pixelActive<A>(c, pixel)))
+                break;
+            depth = 0;
+            st = generatePathFor<LIGHT>(c, x, y, c.p[P_SAMPLE] + k);
         }
     }
-#else
-    uint32_t x = blockIdx.x * 16 + (threadIdx.x & 15u);
-    uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 4);
-    if (x >= width || y >= c.p[P_HEIGHT])
-        return;
-    uint32_t pixel = y * width + x;
-    if (n == 0 || (adaptive && !pixelActive<A>(c, pixel)))
-        return;
-    uint32_t k = 0, depth = 0;
-    PathState<LIGHT> st = generatePathFor<LIGHT>(c, x, y, c.p[P_SAMPLE]);
-    for (;;) {
-        if (shadePathCall<LIGHT, RESTIR>(c, st, traceClosest(c, st.org, st.dir), depth, pixel) &&
-            depth + 1 < c.p[P_MAX_DEPTH]) {
-            depth++;
-            continue;
-        }
-        finishPath<LIGHT, A, RESTIR>(c, st, pixel);
-        if (++k >= n || (adaptive && !pixelActive<A>(c, pixel)))
-            break;
-        depth = 0;
-        st = generatePathFor<LIGHT>(c, x, y, c.p[P_SAMPLE] + k);
-    }
-#endif
 }
 
 // wf_args.slang:9-24 at depth 0: starts a sample. Every pixel's path is live unless adaptive
